@@ -1,0 +1,330 @@
+#!/usr/bin/env python3
+"""Benchmark: particle-updates/s of the 2,097,152-particle SPH dam break on GB300.
+
+One step = hash -> LSD radix sort -> cellindices+permute -> density ->
+force+collision+leapfrog over all particles (the fused path of sph_step,
+replayed from a CUDA graph).  The workload is the 2M-particle configuration:
+unit box, lattice spacing 2^-8, h = 2s, dt = 0.001, 1000-step rollout, seeded
+synthetic dam-break lattice (no dataset exists for it).
+
+  value  device-resident throughput over K steps (CUDA events on the
+         library's stream, which is torch's current stream).
+  e2e    the same metric through the C ABI with the state on the host: each
+         step uploads pos/vel/veleval from pinned memory, steps, and
+         downloads them again.
+  roofline  the dominant kernel's algorithmic bytes / its mean duration
+         (per-kernel CUDA events, sph_step_profile) against the measured
+         HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (a port of the reference's kernels) on the
+         host cores for a bounded sample.
+
+`--impl reference` times the reference's CPU implementation instead: the
+reference's OpenCL kernels cannot run on these machines (no OpenCL driver),
+so its CPU stand-in is the oracle port, with all host threads.
+
+Multi-GPU: the path does not shard (one scene per GPU): under torchrun every
+rank runs its own replica, timing is max over ranks, value sums all ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 2097152
+DT = 0.001
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--exact", action="store_true", help="exact force arithmetic (bitwise oracle parity)")
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--profile-steps", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-n", type=int, default=131072, help="particles per step of the reference (CPU) arm")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def measured_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the GPU works."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "", 1).isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "", 1).isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        load = [v for v in sm if mx and v > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def algorithmic_bytes(n, c, passes):
+    """Compulsory bytes per launch of each kernel of the step (one read of each
+    input and one write of each output, physics fields only):
+      hash 24N (+4C: cell_start reset), sort 16N in all passes,
+      cellindices 4N+4C + permute 100N, density 20N+8C,
+      force 68N+8C + collision 64N + leapfrog 116N; total 412N + 24C."""
+    b = {"k_prologue": 0.0, "k_hash": 24.0 * n + 4.0 * c, "k_sort_reset": 0.0}
+    for p in range(passes):
+        b["k_radix_pass[%d]" % p] = 16.0 * n / passes
+    b["k_cells_permute"] = 104.0 * n + 4.0 * c
+    b["k_density"] = 20.0 * n + 8.0 * c
+    b["k_force(fused collision+leapfrog)"] = 248.0 * n + 8.0 * c
+    return b
+
+
+def cpu_baseline_port(n, seconds):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind
+    from enjaparticles_gb300 import abi, scenes
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n)
+    sim = oracle_bind.OracleSim(sp, g, gs, n)
+    sim.upload(pos, vel)
+    sim.step(DT, 1)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        sim.step(DT, 1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 200:
+            break
+    threads = oracle_bind.oracle().oracle_threads()
+    return {"value": n * steps / el, "unit": "particle-updates/s", "cores": threads, "kind": "port",
+            "sample": "%d particles of the same dam-break rule, %d steps after 1 warm-up step, %.1f s" % (
+                n, steps, el)}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bind
+    from enjaparticles_gb300 import abi, scenes
+    n = args.ref_n
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n)
+    sim = oracle_bind.OracleSim(sp, g, gs, n)
+    sim.upload(pos, vel)
+    sim.step(DT, args.warmup)
+    t0 = time.perf_counter()
+    sim.step(DT, args.steps)
+    el = time.perf_counter() - t0
+    value = n * args.steps / el
+    threads = oracle_bind.oracle().oracle_threads()
+    line = {
+        "metric": "particle-updates/s at 2M SPH", "value": value, "unit": "particle-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_block(args.n, None),
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads, "kind": "port",
+                         "sample": "each step: one full SPH step of a %d-particle dam break (same lattice rule and "
+                                   "physics as the 2,097,152-particle workload) on %d host threads; the reference's "
+                                   "OpenCL kernels need an OpenCL driver, which these machines lack, so the CPU "
+                                   "port of those kernels (bit-identical to them on the host) stands in" % (
+                                       n, threads)},
+        "e2e": {"value": value, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_block(n, c):
+    return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001, "
+                        "1000-step rollout config" % n,
+            "particles": n, "nb_cells": c, "dt": DT,
+            "l2": "no flush: each step streams > 0.3 GB (> 129 MB L2)", "parallelism": "replicas (one scene per GPU)"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, local_rank, world = dist_env()
+    import torch
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from enjaparticles_gb300 import abi, scenes
+    from enjaparticles_gb300.sph import SPH
+    import ctypes as C
+
+    n = args.n
+    sp, g, gs = abi.dambreak_params(n)
+    pos0, vel0 = scenes.dambreak(n)
+    s = SPH(sp, g, n, gs, exact=args.exact)
+    lib = s.lib
+    stream = torch.cuda.current_stream()
+    abi.check(lib, s.ctx, lib.sph_set_stream(s.ctx, C.c_void_p(stream.cuda_stream)))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    sampler = ClockSampler(torch.cuda.current_device())
+    # --- device-resident throughput (graph replay) --------------------------
+    s.upload(pos0, vel0)
+    s.step(DT, args.warmup)
+    s.sync()
+    sampler.start()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.step(DT, args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    t_ms = max_over_ranks(e0.elapsed_time(e1))
+    s.sync()
+    num_after = s.getNum()
+    # --- per-kernel breakdown over the same trajectory ------------------------
+    psteps = args.profile_steps or args.steps
+    s.upload(pos0, vel0)
+    s.step(DT, args.warmup)
+    s.sync()
+    cap = 16
+    ms = (C.c_float * cap)()
+    nk = C.c_int()
+    abi.check(lib, s.ctx, lib.sph_step_profile(s.ctx, DT, psteps, ms, cap, C.byref(nk)))
+    names = [lib.sph_profile_kernel_name(s.ctx, k).decode() for k in range(nk.value)]
+    kern_ms = {names[k]: ms[k] / psteps for k in range(nk.value)}
+    # --- end to end through the C ABI with host-resident state ----------------
+    pin = [torch.empty((n, 4), dtype=torch.float32, pin_memory=True) for _ in range(3)]
+    host = [p.numpy() for p in pin]
+    host[0][:] = pos0
+    host[1][:] = vel0
+    host[2][:] = 0
+    f_pos, f_vel, f_ve = abi.FIELDS["pos_u"], abi.FIELDS["vel_u"], abi.FIELDS["veleval_u"]
+    s.upload(host[0], host[1], host[2])
+    s.step(DT, 3)
+    s.sync()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        abi.check(lib, s.ctx, lib.sph_upload(s.ctx, host[0].ctypes.data, host[1].ctypes.data, host[2].ctypes.data, n))
+        abi.check(lib, s.ctx, lib.sph_step(s.ctx, DT, 1))
+        for fid, h in ((f_pos, host[0]), (f_vel, host[1]), (f_ve, host[2])):
+            abi.check(lib, s.ctx, lib.sph_download_async(s.ctx, fid, h.ctypes.data, n))
+        abi.check(lib, s.ctx, lib.sph_sync(s.ctx))
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    barrier()
+    clocks = sampler.stop()
+
+    steps = args.steps
+    value = n * steps * world / (t_ms / 1e3)
+    passes = nk.value - 6
+    c = g.nb_cells
+    ab = algorithmic_bytes(n, c, passes)
+    dom = max(kern_ms, key=lambda k: kern_ms[k])
+    peak, peak_kind = measured_hbm()
+    achieved = ab[dom] / (kern_ms[dom] / 1e3) / 1e9
+    b_step = sum(ab.values())
+    step_ms = t_ms / steps
+    line = {
+        "metric": "particle-updates/s at 2M SPH", "value": value, "unit": "particle-updates/s", "n_gpus": world,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break lattice, zero initial velocity)",
+        "config": config_block(n, c),
+        "e2e": {"value": n * args.e2e_steps * world / t_e2e, "unit": "particle-updates/s",
+                "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n,
+                "note": "state (pos, vel, veleval) uploaded from and downloaded to pinned host memory every step; "
+                        "%d steps" % args.e2e_steps},
+        "gpu_launches": nk.value * steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "algorithmic_bytes": ab[dom], "mean_launch_ms": kern_ms[dom]},
+        "step_roofline": {"algorithmic_bytes": b_step, "achieved": b_step / (step_ms / 1e3) / 1e9, "peak": peak,
+                          "frac": b_step / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s"},
+        "kernels_ms": kern_ms,
+        "particles_after": num_after,
+        "exact": bool(args.exact),
+    }
+    if clocks:
+        line["clocks"] = clocks
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_port(n, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line))
+    s.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,68 @@
+"""Build librtps_sph.so in-tree with nvcc for sm_103a (no cmake).
+
+Each translation unit compiles in parallel into enjaparticles_gb300/_build/,
+then one link step writes enjaparticles_gb300/librtps_sph.so.  Usage:
+    python -m enjaparticles_gb300.build_ext [-v] [--ptxas-verbose]
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "librtps_sph.so")
+
+SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cells.cu", "sph_neighbors.cu", "sph_integrate.cu", "sph_params.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _compile(src, ptxas_verbose):
+    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    path = os.path.join(CSRC, src)
+    cmd = [nvcc(), "-c", path, "-o", obj, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-fno-fast-math", "-I", os.path.join(PKG, "..", "include")]
+    if src.endswith(".cu"):
+        cmd += ARCH + ["--expt-relaxed-constexpr"]
+        if ptxas_verbose:
+            cmd += ["-Xptxas", "-v"]
+    else:
+        cmd += ["-x", "c++"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    return src, obj, r.returncode, r.stdout + r.stderr, " ".join(cmd)
+
+
+def build(verbose=False, ptxas_verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    objs, logs = [], []
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(SOURCES))) as ex:
+        for src, obj, rc, out, cmd in ex.map(lambda s: _compile(s, ptxas_verbose), SOURCES):
+            if verbose:
+                print(cmd)
+            if out.strip() and (verbose or ptxas_verbose or rc):
+                logs.append("== %s\n%s" % (src, out))
+            if rc:
+                raise RuntimeError("nvcc failed on %s:\n%s" % (src, out))
+            objs.append(obj)
+    tmp = LIB + ".tmp"
+    cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, LIB)
+    for line in logs:
+        print(line)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, ptxas_verbose="--ptxas-verbose" in sys.argv))

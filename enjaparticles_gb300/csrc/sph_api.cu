@@ -1,0 +1,805 @@
+// sph_api.cu — the C ABI of include/rtps_sph.h: context, buffers, stages, and
+// the CUDA-graph step.  Replaces the reference's OpenCL host layer
+// (rtpslib/opencl/{CLL,Kernel,Buffer}) and the buffer setup of
+// System::prepareSorted / SPH::prepareSorted (System.cpp:198-291,
+// SPH.cpp:482-520).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "sph_device.cuh"
+
+using sphk::StepParams;
+
+struct sph_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    SPHParams sp;
+    GridParams gp, gps;
+    StepParams P;
+    int max_num = 0;
+    int num_hint = 0;  // host upper bound of the particle count (grid sizing)
+    int passes = 1;
+    int exact = 0;
+    // device state
+    float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr;
+    float4 *pos_s = nullptr, *vel_s = nullptr, *veleval_s = nullptr, *force_s = nullptr, *xsph_s = nullptr;
+    float4 *del_pos = nullptr, *del_vel = nullptr;
+    float* density = nullptr;
+    uint32_t* nbr = nullptr;
+    uint32_t *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
+    uint32_t *keys_cur = nullptr, *idx_cur = nullptr;  // what SORT_HASHES / SORT_INDICES show
+    uint32_t *cell_start = nullptr, *cell_end = nullptr;
+    int* info = nullptr;
+    uint32_t* scratch = nullptr;
+    size_t scratch_words = 0;
+    uint32_t* hist = nullptr;    // [4][256]
+    uint32_t* status = nullptr;  // [passes][tiles][256]
+    int tiles_cap = 0;
+    int* host_info = nullptr;  // pinned
+    // graph of one fused step
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.f;
+    int graph_num = -1;
+    int graph_exact = -1;
+    unsigned params_version = 1, graph_version = 0;
+    std::string err;
+};
+
+static std::string g_create_error;
+
+static int set_err(sph_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c)
+        c->err = buf;
+    else
+        g_create_error = buf;
+    return code;
+}
+
+#define CK(ctx, call)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return set_err(ctx, SPH_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CK_LAUNCH(ctx)                                                                                       \
+    do {                                                                                                     \
+        cudaError_t e_ = cudaGetLastError();                                                                 \
+        if (e_ != cudaSuccess) return set_err(ctx, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+    } while (0)
+
+namespace {
+
+__global__ void k_fill_u32(uint32_t* p, size_t n, uint32_t v) {
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) p[k] = v;
+}
+__global__ void k_set_num(int* info, int n) {
+    info[sphk::kNum] = n;
+    info[sphk::kOutStart] = -1;
+    info[sphk::kDeleted] = 0;
+    info[sphk::kError] = 0;
+}
+
+void fill_u32(uint32_t* p, size_t n, uint32_t v, cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    blocks = blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks);
+    k_fill_u32<<<blocks, 256, 0, st>>>(p, n, v);
+}
+
+int bit_width(uint32_t v) {
+    int b = 0;
+    while (v) {
+        ++b;
+        v >>= 1;
+    }
+    return b;
+}
+
+float next_up(float x) { return std::nextafter(x, INFINITY); }
+float next_down(float x) { return std::nextafter(x, -INFINITY); }
+
+// Largest float t with sqrtf(t) <= h: |r| <= h  <=>  r2 <= t.
+float cutoff_r2(float h) {
+    float t = h * h;
+    while (t > 0.f && std::sqrt(t) > h) t = next_down(t);
+    while (std::sqrt(next_up(t)) <= h) t = next_up(t);
+    return t;
+}
+
+bool finite_params(const SPHParams& s) {
+    const float* f = reinterpret_cast<const float*>(&s);
+    for (int k = 0; k < 27; ++k)
+        if (!std::isfinite(f[k])) return false;
+    return std::isfinite(s.gravity.x) && std::isfinite(s.gravity.y) && std::isfinite(s.gravity.z) &&
+           std::isfinite(s.gravity.w);
+}
+
+float4 to_f4(const sph_float4& v) { return make_float4(v.x, v.y, v.z, v.w); }
+
+int build_step_params(sph_ctx* c) {
+    const SPHParams& s = c->sp;
+    StepParams& P = c->P;
+    if (!finite_params(s)) return set_err(c, SPH_EINVAL, "SPHParams holds a non-finite value");
+    if (!(s.smoothing_distance > 0.f)) return set_err(c, SPH_EINVAL, "smoothing_distance must be > 0");
+    if (!(s.simulation_scale > 0.f)) return set_err(c, SPH_EINVAL, "simulation_scale must be > 0");
+    P.sc = s.simulation_scale;
+    P.h = s.smoothing_distance;
+    P.h2 = s.smoothing_distance * s.smoothing_distance;
+    P.rcut2 = cutoff_r2(s.smoothing_distance);
+    P.mass = s.mass;
+    P.rho0 = s.rest_density;
+    P.K = s.K;
+    P.eps = s.EPSILON;
+    P.visc = s.viscosity;
+    P.wpoly6 = s.wpoly6_coef;
+    P.wspiky_d = s.wspiky_d_coef;
+    P.wvisc_dd = s.wvisc_dd_coef;
+    P.xsph_factor = s.xsph_factor;
+    P.vlimit = s.velocity_limit;
+    P.kwall = s.boundary_stiffness;
+    P.cwall = s.boundary_dampening;
+    P.bound = s.rest_distance * .5f;
+    P.gravity = to_f4(s.gravity);
+    P.dens_coef = s.wpoly6_coef * s.mass;
+    P.coef_b = (float)(-0.5 * (double)s.wspiky_d_coef);
+    P.coef_s = s.viscosity * s.wvisc_dd_coef;
+    P.coef_d = (float)(2.0 * (double)s.mass * (double)s.wpoly6_coef);
+    P.g_min = to_f4(c->gp.grid_min);
+    P.g_delta = to_f4(c->gp.grid_delta);
+    P.g_res = to_f4(c->gp.grid_res);
+    P.gs_min = to_f4(c->gps.grid_min);
+    P.gs_delta = to_f4(c->gps.grid_delta);
+    P.gs_res = to_f4(c->gps.grid_res);
+    P.gs_bnd_min = to_f4(c->gps.bnd_min);
+    P.gs_bnd_max = to_f4(c->gps.bnd_max);
+    P.nb_cells = c->gp.nb_cells;
+    P.res_x = (int)c->gps.grid_res.x;
+    P.res_y = (int)c->gps.grid_res.y;
+    P.res_z = (int)c->gps.grid_res.z;
+    const bool integral = (float)P.res_x == c->gps.grid_res.x && (float)P.res_y == c->gps.grid_res.y &&
+                          (float)P.res_z == c->gps.grid_res.z && P.res_x > 0 && P.res_y > 0 && P.res_z > 0;
+    const double span = (double)(P.res_x + 4) * (P.res_y + 4) * (P.res_z + 4);
+    P.int_hash_ok = (integral && span < 16777216.0) ? 1 : 0;
+    P.unit_scale = s.simulation_scale == 1.0f ? 1 : 0;
+    c->params_version++;
+    return SPH_OK;
+}
+
+size_t field_elem_bytes(int field) {
+    switch (field) {
+        case SPH_FIELD_DENSITY_S:
+        case SPH_FIELD_SORT_HASHES:
+        case SPH_FIELD_SORT_INDICES:
+        case SPH_FIELD_CELL_START:
+        case SPH_FIELD_CELL_END:
+        case SPH_FIELD_NEIGHBOR_COUNT:
+            return 4;
+        default:
+            return 16;
+    }
+}
+
+void* field_ptr(sph_ctx* c, int field) {
+    switch (field) {
+        case SPH_FIELD_POS_U: return c->pos_u;
+        case SPH_FIELD_VEL_U: return c->vel_u;
+        case SPH_FIELD_VELEVAL_U: return c->veleval_u;
+        case SPH_FIELD_POS_S: return c->pos_s;
+        case SPH_FIELD_VEL_S: return c->vel_s;
+        case SPH_FIELD_VELEVAL_S: return c->veleval_s;
+        case SPH_FIELD_DENSITY_S: return c->density;
+        case SPH_FIELD_FORCE_S: return c->force_s;
+        case SPH_FIELD_XSPH_S: return c->xsph_s;
+        case SPH_FIELD_SORT_HASHES: return c->keys_cur;
+        case SPH_FIELD_SORT_INDICES: return c->idx_cur;
+        case SPH_FIELD_CELL_START: return c->cell_start;
+        case SPH_FIELD_CELL_END: return c->cell_end;
+        case SPH_FIELD_NEIGHBOR_COUNT: return c->nbr;
+        default: return nullptr;
+    }
+}
+
+int field_capacity(sph_ctx* c, int field) {
+    return (field == SPH_FIELD_CELL_START || field == SPH_FIELD_CELL_END) ? c->gp.nb_cells + 1 : c->max_num;
+}
+
+void free_all(sph_ctx* c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
+                    c->del_pos, c->del_vel, c->density, c->nbr, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
+                    c->cell_start, c->cell_end, c->info, c->scratch};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->host_info) cudaFreeHost(c->host_info);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+}
+
+// Buffers the hash writes and the sort reads first, so that the last radix
+// pass lands in keys_a / idx_a.
+uint32_t* hash_keys(sph_ctx* c) { return (c->passes & 1) ? c->keys_b : c->keys_a; }
+uint32_t* hash_idx(sph_ctx* c) { return (c->passes & 1) ? c->idx_b : c->idx_a; }
+
+// --- launch sequences ------------------------------------------------------
+int enqueue_hash(sph_ctx* c) {
+    sphk::launch_prologue(c->hist, c->info, c->stream);
+    sphk::launch_hash(c->pos_u, hash_keys(c), hash_idx(c), c->cell_start, c->hist, c->info, c->P, c->num_hint,
+                      c->passes, 1, c->stream);
+    c->keys_cur = hash_keys(c);
+    c->idx_cur = hash_idx(c);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int enqueue_sort(sph_ctx* c) {
+    sphk::launch_sort_reset(c->status, (size_t)c->passes * c->tiles_cap * 256, c->info + sphk::kSortTiles,
+                            c->stream);
+    uint32_t *kin = hash_keys(c), *vin = hash_idx(c);
+    uint32_t *kout = (kin == c->keys_a) ? c->keys_b : c->keys_a, *vout = (vin == c->idx_a) ? c->idx_b : c->idx_a;
+    const int total_bits = bit_width((uint32_t)c->gp.nb_cells);
+    for (int ps = 0; ps < c->passes; ++ps) {
+        const int shift = ps * 8;
+        int bits = total_bits - shift;
+        bits = bits > 8 ? 8 : (bits < 1 ? 1 : bits);
+        sphk::launch_radix_pass(kin, vin, kout, vout, c->info, c->hist + ps * 256,
+                                c->status + (size_t)ps * c->tiles_cap * 256, c->info + sphk::kSortTiles + ps,
+                                c->info + sphk::kError, shift, bits, c->num_hint, c->stream);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    c->keys_cur = c->keys_a;
+    c->idx_cur = c->idx_a;
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int enqueue_fused_step(sph_ctx* c, float dt) {
+    int rc = enqueue_hash(c);
+    if (rc) return rc;
+    rc = enqueue_sort(c);
+    if (rc) return rc;
+    sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
+                               c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 1, c->stream);
+    sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_a, c->vel_u,
+                         c->vel_s, c->del_pos, c->del_vel, c->P, c->num_hint, c->stream);
+    sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
+                       c->xsph_s, c->idx_a, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, dt, 1,
+                       c->exact, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int read_info(sph_ctx* c) {
+    CK(c, cudaMemcpyAsync(c->host_info, c->info, sizeof(int) * sphk::kInfoSlots, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (c->host_info[sphk::kError] & sphk::kErrLookbackTimeout) {
+        return set_err(c, SPH_ETIMEOUT, "radix sort look-back wait expired; the step result is invalid");
+    }
+    return SPH_OK;
+}
+
+int check_ctx(sph_ctx* c) {
+    if (!c) return SPH_EINVAL;
+    int dev = -1;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev != c->device) CK(c, cudaSetDevice(c->device));
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+#define SPH_STR_(x) #x
+#define SPH_STR(x) SPH_STR_(x)
+const char* sph_build_info(void) {
+    return "librtps_sph: GB300 sm_103a SPH step (hash, 8-bit LSD radix sort, cellindices+permute, density, "
+           "force+collision+leapfrog); CUDART " SPH_STR(CUDART_VERSION);
+}
+
+int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* grid_scaled, int max_num,
+               sph_ctx** out) {
+    if (!sphp || !grid || !out) return set_err(nullptr, SPH_EINVAL, "null argument");
+    *out = nullptr;
+    if (max_num <= 0 || max_num >= (1 << 30)) return set_err(nullptr, SPH_EINVAL, "max_num out of range: %d", max_num);
+    if (grid->nb_cells <= 0 || grid->nb_cells + 1 >= (1 << 24))
+        return set_err(nullptr, SPH_EINVAL, "nb_cells must be in [1, 2^24-2] (float cell hashes), got %d",
+                       grid->nb_cells);
+    sph_ctx* c = new sph_ctx();
+    c->sp = *sphp;
+    c->gp = *grid;
+    if (grid_scaled) {
+        c->gps = *grid_scaled;
+    } else {
+        // System::setupDomain's scaled copy (System.cpp:318-325): lanes times
+        // sim_scale, delta times the float reciprocal of sim_scale.
+        const float sc = sphp->simulation_scale;
+        auto mul = [sc](sph_float4 v) { v.x = sc * v.x; v.y = sc * v.y; v.z = sc * v.z; v.w = sc * v.w; return v; };
+        auto div = [sc](sph_float4 v) {
+            const float d = 1.f / sc;
+            v.x = d * v.x; v.y = d * v.y; v.z = d * v.z; v.w = d * v.w;
+            return v;
+        };
+        c->gps = *grid;
+        c->gps.grid_min = mul(grid->grid_min);
+        c->gps.grid_max = mul(grid->grid_max);
+        c->gps.bnd_min = mul(grid->bnd_min);
+        c->gps.bnd_max = mul(grid->bnd_max);
+        c->gps.grid_size = mul(grid->grid_size);
+        c->gps.grid_delta = div(grid->grid_delta);
+    }
+    if (c->gps.nb_cells != c->gp.nb_cells) {
+        delete c;
+        return set_err(nullptr, SPH_EINVAL, "scaled grid nb_cells differs");
+    }
+    c->max_num = max_num;
+    c->sp.max_num = max_num;
+    if (build_step_params(c) != SPH_OK) {
+        g_create_error = c->err;
+        delete c;
+        return SPH_EINVAL;
+    }
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) {
+        delete c;
+        return set_err(nullptr, SPH_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    }
+    const int total_bits = bit_width((uint32_t)c->gp.nb_cells);
+    c->passes = (total_bits + 7) / 8;
+    if (c->passes < 1) c->passes = 1;
+    c->tiles_cap = sphk::radix_tiles(max_num);
+    const size_t N = (size_t)max_num, C1 = (size_t)c->gp.nb_cells + 1;
+    int rc = SPH_OK;
+#define ALLOC(ptr, bytes)                                                                                 \
+    do {                                                                                                  \
+        if (rc == SPH_OK) {                                                                               \
+            cudaError_t ae = cudaMalloc((void**)&(ptr), (bytes));                                         \
+            if (ae != cudaSuccess) {                                                                      \
+                rc = set_err(nullptr, SPH_ENOMEM, "cudaMalloc(%zu): %s", (size_t)(bytes), cudaGetErrorString(ae)); \
+                cudaGetLastError();                                                                       \
+            }                                                                                             \
+        }                                                                                                 \
+    } while (0)
+    ALLOC(c->pos_u, N * 16);
+    ALLOC(c->vel_u, N * 16);
+    ALLOC(c->veleval_u, N * 16);
+    ALLOC(c->pos_s, N * 16);
+    ALLOC(c->vel_s, N * 16);
+    ALLOC(c->veleval_s, N * 16);
+    ALLOC(c->force_s, N * 16);
+    ALLOC(c->xsph_s, N * 16);
+    ALLOC(c->del_pos, N * 16);
+    ALLOC(c->del_vel, N * 16);
+    ALLOC(c->density, N * 4);
+    ALLOC(c->nbr, N * 4);
+    ALLOC(c->keys_a, N * 4);
+    ALLOC(c->idx_a, N * 4);
+    ALLOC(c->keys_b, N * 4);
+    ALLOC(c->idx_b, N * 4);
+    ALLOC(c->cell_start, C1 * 4);
+    ALLOC(c->cell_end, C1 * 4);
+    ALLOC(c->info, sizeof(int) * sphk::kInfoSlots);
+    c->scratch_words = 4 * 256 + (size_t)c->passes * c->tiles_cap * 256;
+    ALLOC(c->scratch, c->scratch_words * 4);
+#undef ALLOC
+    if (rc == SPH_OK && cudaMallocHost((void**)&c->host_info, sizeof(int) * sphk::kInfoSlots) != cudaSuccess)
+        rc = set_err(nullptr, SPH_ENOMEM, "cudaMallocHost failed");
+    if (rc == SPH_OK && cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        rc = set_err(nullptr, SPH_ECUDA, "cudaStreamCreate failed");
+    if (rc != SPH_OK) {
+        free_all(c);
+        delete c;
+        return rc;
+    }
+    c->stream = c->own_stream;
+    c->hist = c->scratch;
+    c->status = c->scratch + 4 * 256;
+    c->keys_cur = c->keys_a;
+    c->idx_cur = c->idx_a;
+    // Initial contents as SPH::prepareSorted / System::prepareSorted leave them.
+    cudaStream_t st = c->stream;
+    cudaMemsetAsync(c->info, 0, sizeof(int) * sphk::kInfoSlots, st);
+    k_set_num<<<1, 1, 0, st>>>(c->info, 0);
+    const void* zero_f4[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s,
+                             c->xsph_s, c->del_pos, c->del_vel};
+    for (const void* p : zero_f4) cudaMemsetAsync((void*)p, 0, N * 16, st);
+    cudaMemsetAsync(c->density, 0, N * 4, st);
+    cudaMemsetAsync(c->nbr, 0, N * 4, st);
+    fill_u32(c->keys_a, N, 0x7fffffffu, st);
+    fill_u32(c->idx_a, N, 0x7fffffffu, st);
+    fill_u32(c->keys_b, N, 0x7fffffffu, st);
+    fill_u32(c->idx_b, N, 0x7fffffffu, st);
+    fill_u32(c->cell_start, C1, 666u, st);
+    fill_u32(c->cell_end, C1, 666u, st);
+    cudaMemsetAsync(c->scratch, 0, c->scratch_words * 4, st);
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_err(nullptr, SPH_ECUDA, "context init: %s", cudaGetErrorString(e));
+        free_all(c);
+        delete c;
+        return SPH_ECUDA;
+    }
+    *out = c;
+    return SPH_OK;
+}
+
+int sph_destroy(sph_ctx* c) {
+    if (!c) return SPH_EINVAL;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+    return SPH_OK;
+}
+
+int sph_set_params(sph_ctx* c, const SPHParams* sphp) {
+    if (!c || !sphp) return SPH_EINVAL;
+    SPHParams old = c->sp;
+    c->sp = *sphp;
+    c->sp.max_num = c->max_num;
+    int rc = build_step_params(c);
+    if (rc != SPH_OK) {
+        c->sp = old;
+        build_step_params(c);
+        return rc;
+    }
+    return SPH_OK;
+}
+
+int sph_get_params(sph_ctx* c, SPHParams* sphp, GridParams* grid, GridParams* grid_scaled) {
+    if (!c) return SPH_EINVAL;
+    if (sphp) *sphp = c->sp;
+    if (grid) *grid = c->gp;
+    if (grid_scaled) *grid_scaled = c->gps;
+    return SPH_OK;
+}
+
+int sph_set_stream(sph_ctx* c, void* stream) {
+    if (!c) return SPH_EINVAL;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    if (c->graph) {
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
+    return SPH_OK;
+}
+
+int sph_set_exact(sph_ctx* c, int exact) {
+    if (!c) return SPH_EINVAL;
+    c->exact = exact ? 1 : 0;
+    return SPH_OK;
+}
+
+int sph_upload(sph_ctx* c, const sph_float4* pos, const sph_float4* vel, const sph_float4* veleval, int n) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!pos || !vel || n < 0 || n > c->max_num) return set_err(c, SPH_EINVAL, "sph_upload: bad arguments (n=%d)", n);
+    const size_t b = (size_t)n * 16;
+    if (n > 0) {
+        CK(c, cudaMemcpyAsync(c->pos_u, pos, b, cudaMemcpyHostToDevice, c->stream));
+        CK(c, cudaMemcpyAsync(c->vel_u, vel, b, cudaMemcpyHostToDevice, c->stream));
+        if (veleval)
+            CK(c, cudaMemcpyAsync(c->veleval_u, veleval, b, cudaMemcpyHostToDevice, c->stream));
+        else
+            CK(c, cudaMemsetAsync(c->veleval_u, 0, b, c->stream));
+    }
+    k_set_num<<<1, 1, 0, c->stream>>>(c->info, n);
+    CK_LAUNCH(c);
+    c->num_hint = n;
+    return SPH_OK;
+}
+
+int sph_get_num(sph_ctx* c, int* num) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!num) return SPH_EINVAL;
+    rc = read_info(c);
+    const int out = c->host_info[sphk::kOutStart];
+    const int n = c->host_info[sphk::kNum];
+    *num = out >= 0 ? (out < n ? out : n) : n;
+    return rc;
+}
+
+int sph_push_particles(sph_ctx* c, const sph_float4* pos, const sph_float4* vel, int n) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!pos || !vel || n < 0) return set_err(c, SPH_EINVAL, "sph_push_particles: bad arguments");
+    int cur = 0;
+    rc = sph_get_num(c, &cur);
+    if (rc) return rc;
+    if (cur + n > c->max_num)
+        return set_err(c, SPH_EINVAL, "pushParticles: exceeded max nb (%d) of particles allowed", c->max_num);
+    if (n == 0) return SPH_OK;
+    const size_t b = (size_t)n * 16;
+    CK(c, cudaMemcpyAsync(c->pos_u + cur, pos, b, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->vel_u + cur, vel, b, cudaMemcpyHostToDevice, c->stream));
+    k_set_num<<<1, 1, 0, c->stream>>>(c->info, cur + n);
+    CK_LAUNCH(c);
+    c->num_hint = cur + n;
+    CK(c, cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_set_num(sph_ctx* c, int num) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (num < 0 || num > c->max_num) return set_err(c, SPH_EINVAL, "sph_set_num: %d out of range", num);
+    k_set_num<<<1, 1, 0, c->stream>>>(c->info, num);
+    CK_LAUNCH(c);
+    c->num_hint = num;
+    return SPH_OK;
+}
+
+int sph_download_async(sph_ctx* c, int field, void* host, int n) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!host || n < 0) return set_err(c, SPH_EINVAL, "sph_download: bad arguments");
+    if (field < 0 || field >= SPH_FIELD_COUNT_) return set_err(c, SPH_EINVAL, "unknown field %d", field);
+    if (n > field_capacity(c, field)) return set_err(c, SPH_EINVAL, "n=%d exceeds field capacity", n);
+    if (n == 0) return SPH_OK;
+    CK(c, cudaMemcpyAsync(host, field_ptr(c, field), (size_t)n * field_elem_bytes(field), cudaMemcpyDeviceToHost,
+                          c->stream));
+    return SPH_OK;
+}
+
+int sph_download(sph_ctx* c, int field, void* host, int n) {
+    int rc = sph_download_async(c, field, host, n);
+    if (rc) return rc;
+    return read_info(c);
+}
+
+int sph_get_device_ptr(sph_ctx* c, int field, void** dptr) {
+    if (!c || !dptr) return SPH_EINVAL;
+    void* p = field_ptr(c, field);
+    if (!p) return set_err(c, SPH_EINVAL, "unknown field %d", field);
+    *dptr = p;
+    return SPH_OK;
+}
+
+int sph_get_deleted(sph_ctx* c, sph_float4* pos, sph_float4* vel, int cap, int* count) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    rc = read_info(c);
+    if (rc) return rc;
+    const int nd = c->host_info[sphk::kDeleted];
+    if (count) *count = nd;
+    const int k = nd < cap ? nd : cap;
+    if (k > 0 && pos) CK(c, cudaMemcpy(pos, c->del_pos, (size_t)k * 16, cudaMemcpyDeviceToHost));
+    if (k > 0 && vel) CK(c, cudaMemcpy(vel, c->del_vel, (size_t)k * 16, cudaMemcpyDeviceToHost));
+    return SPH_OK;
+}
+
+// --- stages ----------------------------------------------------------------
+int sph_stage_hash(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    return enqueue_hash(c);
+}
+
+int sph_stage_sort(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    return enqueue_sort(c);
+}
+
+int sph_stage_cellindices(sph_ctx* c, int* nc) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    sphk::launch_cells_permute(c->keys_cur, c->idx_cur, c->cell_start, c->cell_end, c->pos_u, c->vel_u,
+                               c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint,
+                               0, c->stream);
+    CK_LAUNCH(c);
+    if (nc) {
+        uint32_t v = 0;
+        CK(c, cudaMemcpyAsync(&v, c->cell_start + c->gp.nb_cells, 4, cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        *nc = (int)v;
+    }
+    return SPH_OK;
+}
+
+int sph_stage_permute(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    sphk::launch_permute_only(c->idx_cur, c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info,
+                              c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int sph_stage_density(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_cur, c->vel_u,
+                         nullptr, nullptr, nullptr, c->P, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int sph_stage_force(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
+                       c->xsph_s, c->idx_cur, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, 0.f, 0,
+                       c->exact, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int sph_stage_collision(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    sphk::launch_collision(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int sph_stage_leapfrog(sph_ctx* c, float dt) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!std::isfinite(dt)) return set_err(c, SPH_EINVAL, "dt must be finite");
+    sphk::launch_leapfrog(c->pos_s, c->vel_s, c->force_s, c->xsph_s, c->idx_cur, c->pos_u, c->vel_u, c->veleval_u,
+                          c->info, c->P, dt, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int sph_update(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if ((rc = enqueue_hash(c))) return rc;
+    if ((rc = enqueue_sort(c))) return rc;
+    sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
+                               c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 2, c->stream);
+    sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
+                               c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
+    sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_a, c->vel_u,
+                         nullptr, nullptr, nullptr, c->P, c->num_hint, c->stream);
+    sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
+                       c->xsph_s, c->idx_a, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, 0.f, 0,
+                       c->exact, c->num_hint, c->stream);
+    sphk::launch_collision(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int sph_integrate(sph_ctx* c, float dt) { return sph_stage_leapfrog(c, dt); }
+
+int sph_step(sph_ctx* c, float dt, int nsteps) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (nsteps < 0 || !std::isfinite(dt)) return set_err(c, SPH_EINVAL, "sph_step: bad arguments");
+    if (nsteps == 0 || c->num_hint == 0) return SPH_OK;
+    const bool stale = !c->graph || c->graph_dt != dt || c->graph_num != c->num_hint || c->graph_exact != c->exact ||
+                       c->graph_version != c->params_version;
+    if (stale) {
+        if (c->graph) {
+            cudaGraphExecDestroy(c->graph);
+            c->graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_fused_step(c, dt);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return set_err(c, SPH_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            c->graph = nullptr;
+            return set_err(c, SPH_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        }
+        c->graph_dt = dt;
+        c->graph_num = c->num_hint;
+        c->graph_exact = c->exact;
+        c->graph_version = c->params_version;
+    }
+    for (int k = 0; k < nsteps; ++k) CK(c, cudaGraphLaunch(c->graph, c->stream));
+    c->keys_cur = c->keys_a;
+    c->idx_cur = c->idx_a;
+    return SPH_OK;
+}
+
+int sph_step_eager(sph_ctx* c, float dt, int nsteps) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (nsteps < 0 || !std::isfinite(dt)) return set_err(c, SPH_EINVAL, "sph_step_eager: bad arguments");
+    for (int k = 0; k < nsteps && c->num_hint > 0; ++k)
+        if ((rc = enqueue_fused_step(c, dt))) return rc;
+    return SPH_OK;
+}
+
+int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap, int* nkernels) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (nsteps < 0 || !std::isfinite(dt) || !kernel_ms || cap <= 0)
+        return set_err(c, SPH_EINVAL, "sph_step_profile: bad arguments");
+    // Launches of one fused step: prologue, hash, sort reset, radix passes,
+    // cells+permute, density, force+collision+leapfrog.
+    const int nk = 6 + c->passes;
+    if (nkernels) *nkernels = nk;
+    for (int k = 0; k < cap; ++k) kernel_ms[k] = 0.f;
+    cudaEvent_t ev[24];
+    for (int k = 0; k <= nk; ++k) CK(c, cudaEventCreate(&ev[k]));
+    cudaStream_t st = c->stream;
+    for (int step = 0; step < nsteps && c->num_hint > 0; ++step) {
+        int e = 0;
+        CK(c, cudaEventRecord(ev[e++], st));
+        sphk::launch_prologue(c->hist, c->info, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        sphk::launch_hash(c->pos_u, hash_keys(c), hash_idx(c), c->cell_start, c->hist, c->info, c->P, c->num_hint,
+                          c->passes, 1, st);
+        sphk::launch_sort_reset(c->status, (size_t)c->passes * c->tiles_cap * 256, c->info + sphk::kSortTiles, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        uint32_t *kin = hash_keys(c), *vin = hash_idx(c);
+        uint32_t *kout = (kin == c->keys_a) ? c->keys_b : c->keys_a, *vout = (vin == c->idx_a) ? c->idx_b : c->idx_a;
+        const int total_bits = bit_width((uint32_t)c->gp.nb_cells);
+        for (int ps = 0; ps < c->passes; ++ps) {
+            int bits = total_bits - ps * 8;
+            bits = bits > 8 ? 8 : (bits < 1 ? 1 : bits);
+            sphk::launch_radix_pass(kin, vin, kout, vout, c->info, c->hist + ps * 256,
+                                    c->status + (size_t)ps * c->tiles_cap * 256, c->info + sphk::kSortTiles + ps,
+                                    c->info + sphk::kError, ps * 8, bits, c->num_hint, st);
+            std::swap(kin, kout);
+            std::swap(vin, vout);
+            CK(c, cudaEventRecord(ev[e++], st));
+        }
+        sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
+                                   c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 1, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_a, c->vel_u,
+                             c->vel_s, c->del_pos, c->del_vel, c->P, c->num_hint, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
+                           c->xsph_s, c->idx_a, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, dt, 1,
+                           c->exact, c->num_hint, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        CK_LAUNCH(c);
+        CK(c, cudaEventSynchronize(ev[nk]));
+        for (int k = 0; k < nk && k < cap; ++k) {
+            float ms = 0.f;
+            CK(c, cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+            kernel_ms[k] += ms;
+        }
+    }
+    for (int k = 0; k <= nk; ++k) cudaEventDestroy(ev[k]);
+    c->keys_cur = c->keys_a;
+    c->idx_cur = c->idx_a;
+    return read_info(c);
+}
+
+const char* sph_profile_kernel_name(sph_ctx* c, int k) {
+    static const char* fixed[] = {"k_prologue", "k_hash", "k_sort_reset"};
+    static const char* tail[] = {"k_cells_permute", "k_density", "k_force(fused collision+leapfrog)"};
+    static const char* pass[] = {"k_radix_pass[0]", "k_radix_pass[1]", "k_radix_pass[2]", "k_radix_pass[3]"};
+    if (!c || k < 0) return "";
+    if (k < 3) return fixed[k];
+    if (k < 3 + c->passes) return pass[k - 3];
+    k -= 3 + c->passes;
+    return k < 3 ? tail[k] : "";
+}
+
+int sph_sync(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    return read_info(c);
+}
+
+int sph_last_error(sph_ctx* c, char* buf, int len) {
+    if (!buf || len <= 0) return SPH_EINVAL;
+    const std::string& s = c ? c->err : g_create_error;
+    std::snprintf(buf, (size_t)len, "%s", s.c_str());
+    return SPH_OK;
+}
+
+}  // extern "C"

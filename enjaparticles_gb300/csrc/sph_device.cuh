@@ -1,0 +1,118 @@
+// sph_device.cuh — shared device-side definitions of the GB300 SPH step.
+//
+// Layout in HBM (one context, capacity max_num particles, C = nb_cells):
+//   state, original order    pos_u, vel_u, veleval_u          float4[max_num]
+//   sorted copies            pos_s, veleval_s (vel_s, force_s, xsph_s: staged
+//                            path only)                          float4[max_num]
+//   density_s, neighbour count                                  float/u32[max_num]
+//   sort_hashes / sort_indices + radix ping-pong buffers        u32[max_num] x 4
+//   cell_start, cell_end                                        u32[C+1]
+//   counters (num, out-of-grid start, error word), radix scratch
+// All particle arrays are float4 AoS, 16 B per particle, read with 128-bit
+// loads.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/rtps_sph.h"
+
+namespace sphk {
+
+constexpr uint32_t kEmpty = 0xffffffffu;
+
+// Device counters block (ctx->info).
+enum InfoSlot : int {
+    kNum = 0,        // particle count at the start of the step
+    kOutStart = 1,   // first sorted index whose key is nb_cells, -1 if none
+    kError = 2,      // bit flags, see kErr*
+    kDeleted = 3,    // number of particles removed by the last out-of-grid deletion
+    kSortTiles = 4,  // 4 slots: tile counters of the radix passes
+    kInfoSlots = 16
+};
+constexpr int kErrLookbackTimeout = 1;
+
+// Parameters every kernel of the step needs, passed by value.
+struct StepParams {
+    // SPHParams (floats copied once on the host)
+    float sc, h, h2, rcut2, mass, rho0, K, eps, visc, wpoly6, wspiky_d, wvisc_dd, xsph_factor, vlimit;
+    float kwall, cwall, bound;  // boundary stiffness, dampening, rest_distance*0.5
+    float4 gravity;
+    float dens_coef;   // wpoly6 * mass (float product, as density.cl:120)
+    float coef_b;      // (float)(-0.5 * (double)wspiky_d)
+    float coef_s;      // viscosity * wvisc_dd (float)
+    float coef_d;      // (float)(2.0 * (double)mass * (double)wpoly6)
+    // unscaled grid (hash) and scaled grid (neighbour walk, walls)
+    float4 g_min, g_delta, g_res;
+    float4 gs_min, gs_delta, gs_res, gs_bnd_min, gs_bnd_max;
+    int nb_cells;
+    int res_x, res_y, res_z;      // integer grid_res of the scaled grid
+    int int_hash_ok;              // integer neighbour hashing equals the float formula
+    int unit_scale;               // simulation_scale == 1.0f
+};
+
+// float -> int as the kernels' (int) cast, truncating toward zero; the
+// hardware conversion saturates and maps NaN to 0.
+__device__ __forceinline__ int f2i_rz(float v) { return __float2int_rz(v); }
+
+// calcGridCell (system/common/cl_src/cl_hash.h:33-54), exact float ops.
+__device__ __forceinline__ int3 grid_cell(float px, float py, float pz, const float4& gmin, const float4& gdelta) {
+    int3 c;
+    c.x = f2i_rz(__fmul_rn(__fsub_rn(px, gmin.x), gdelta.x));
+    c.y = f2i_rz(__fmul_rn(__fsub_rn(py, gmin.y), gdelta.y));
+    c.z = f2i_rz(__fmul_rn(__fsub_rn(pz, gmin.z), gdelta.z));
+    return c;
+}
+
+// calcGridHash (cl_hash.h:57-114): ((gz*res.y + gy)*res.x + gx) in float,
+// every operation separately rounded, then (int).
+__device__ __forceinline__ int grid_hash_f(int gx, int gy, int gz, const float4& res) {
+    float a = __fmul_rn((float)gz, res.y);
+    float b = __fadd_rn(a, (float)gy);
+    float c = __fmul_rn(b, res.x);
+    float d = __fadd_rn(c, (float)gx);
+    return f2i_rz(d);
+}
+
+// |r|^2 with the reference's association ((x*x + y*y) + z*z), no contraction.
+__device__ __forceinline__ float dist2_exact(float dx, float dy, float dz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Launch helpers implemented in the .cu files.
+void launch_prologue(uint32_t* hist, int* info, cudaStream_t st);
+void launch_sort_reset(uint32_t* status, size_t words, int* tile_counters, cudaStream_t st);
+void launch_hash(const float4* pos_u, uint32_t* keys, uint32_t* idx, uint32_t* cell_start, uint32_t* hist,
+                 const int* info, const StepParams& p, int grid_items, int passes, int clear_cells,
+                 cudaStream_t st);
+void launch_radix_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, const int* info,
+                       const uint32_t* hist, uint32_t* status, int* tile_counter, int* err, int shift, int bits,
+                       int grid_items, cudaStream_t st);
+int radix_tiles(int n);
+void launch_cells_permute(const uint32_t* keys, const uint32_t* idx, uint32_t* cell_start, uint32_t* cell_end,
+                          const float4* pos_u, const float4* vel_u, const float4* veleval_u, float4* pos_s,
+                          float4* vel_s, float4* veleval_s, int* info, int nb_cells, int grid_items, int gather,
+                          cudaStream_t st);
+void launch_density(const float4* pos_s, float* density, uint32_t* nbr, const uint32_t* cell_start,
+                    const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
+                    float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
+                    cudaStream_t st);
+void launch_force(const float4* pos_s, const float* density, const float4* veleval_s, const uint32_t* cell_start,
+                  const uint32_t* cell_end, const int* info, float4* force_s, float4* xsph_s, uint32_t* idx,
+                  const float4* vel_u_in, const float4* vel_s, float4* pos_u, float4* vel_u, float4* veleval_u,
+                  const StepParams& p, float dt, int fused, int exact, int grid_items, cudaStream_t st);
+void launch_collision(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info,
+                      const StepParams& p, int grid_items, cudaStream_t st);
+void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
+                     uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
+                     const StepParams& p, float dt, int grid_items, cudaStream_t st);
+void launch_delete_staged(const float4* pos_s, const float4* vel_s, const float4* veleval_s, uint32_t* idx,
+                          float4* pos_u, float4* vel_u, float4* veleval_u, float4* del_pos, float4* del_vel, int* info,
+                          int grid_items, cudaStream_t st);
+void launch_permute_only(const uint32_t* idx, const float4* pos_u, const float4* vel_u, const float4* veleval_u,
+                         float4* pos_s, float4* vel_s, float4* veleval_s, const int* info, int grid_items,
+                         cudaStream_t st);
+
+}  // namespace sphk

@@ -1,0 +1,93 @@
+// sph_integrate.cu — the staged (unfused) elementwise stages.
+//   collision_wall: rtpslib/system/sph/cl_src/collision_wall.cl:31-118
+//   leapfrog:       rtpslib/system/sph/cl_src/leapfrog.cl:30-121
+//   out-of-grid deletion bookkeeping of SPH::updateGPU (SPH.cpp:220-250)
+// The fused step runs the same device functions (sph_physics.cuh) inside the
+// force kernel.
+#include "sph_physics.cuh"
+
+namespace sphk {
+
+__global__ void __launch_bounds__(256) k_collision(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
+                                                   float4* __restrict__ force_s, const int* __restrict__ info,
+                                                   const StepParams P) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = scaled(__ldg(pos_s + i), P);
+    force_s[i] = collide_walls(p, __ldg(vel_s + i), force_s[i], P);
+}
+
+void launch_collision(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info,
+                      const StepParams& p, int grid_items, cudaStream_t st) {
+    int blocks = (grid_items + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    k_collision<<<blocks, 256, 0, st>>>(pos_s, vel_s, force_s, info, p);
+}
+
+__global__ void __launch_bounds__(256) k_leapfrog(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
+                                                  const float4* __restrict__ force_s,
+                                                  const float4* __restrict__ xsph_s,
+                                                  const uint32_t* __restrict__ idx, float4* __restrict__ pos_u,
+                                                  float4* __restrict__ vel_u, float4* __restrict__ veleval_u,
+                                                  const int* __restrict__ info, const StepParams P, float dt) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = scaled(__ldg(pos_s + i), P);
+    float4 po, vo, eo;
+    leapfrog_core(p, __ldg(vel_s + i), __ldg(force_s + i), __ldg(xsph_s + i), dt, P, po, vo, eo);
+    const uint32_t o = __ldg(idx + i);
+    vel_u[o] = vo;
+    veleval_u[o] = eo;
+    pos_u[o] = po;
+}
+
+void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
+                     uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
+                     const StepParams& p, float dt, int grid_items, cudaStream_t st) {
+    int blocks = (grid_items + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    k_leapfrog<<<blocks, 256, 0, st>>>(pos_s, vel_s, force_s, xsph_s, idx, pos_u, vel_u, veleval_u, info, p, dt);
+}
+
+// Staged deletion: after cellindices + permute, when some particles left the
+// grid (cell_start[nb_cells] set), keep the first out_start sorted particles:
+// save the removed ones, and re-index the kept ones in sorted order
+// (call_prep(2) + hash_and_sort of SPH.cpp:236-247 give sort_indices = i,
+// the keys being already sorted).
+__global__ void __launch_bounds__(256) k_delete_staged(const float4* __restrict__ pos_s,
+                                                       const float4* __restrict__ vel_s,
+                                                       const float4* __restrict__ veleval_s,
+                                                       uint32_t* __restrict__ idx, float4* __restrict__ pos_u,
+                                                       float4* __restrict__ vel_u, float4* __restrict__ veleval_u,
+                                                       float4* __restrict__ del_pos, float4* __restrict__ del_vel,
+                                                       int* __restrict__ info) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (out < 0 || i >= n_old) return;
+    if (i < n) {
+        idx[i] = (uint32_t)i;
+        pos_u[i] = pos_s[i];
+        vel_u[i] = vel_s[i];
+        veleval_u[i] = veleval_s[i];
+    } else {
+        del_pos[i - n] = pos_s[i];
+        del_vel[i - n] = vel_s[i];
+        if (i == n) info[kDeleted] = n_old - n;
+    }
+}
+
+void launch_delete_staged(const float4* pos_s, const float4* vel_s, const float4* veleval_s, uint32_t* idx,
+                          float4* pos_u, float4* vel_u, float4* veleval_u, float4* del_pos, float4* del_vel, int* info,
+                          int grid_items, cudaStream_t st) {
+    int blocks = (grid_items + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    k_delete_staged<<<blocks, 256, 0, st>>>(pos_s, vel_s, veleval_s, idx, pos_u, vel_u, veleval_u, del_pos, del_vel,
+                                            info);
+}
+
+}  // namespace sphk

@@ -1,0 +1,319 @@
+// sph_neighbors.cu — the two neighbour passes (density, force), with the wall
+// collision and leapfrog integration fused into the force pass.
+//
+//   density: rtpslib/system/sph/cl_src/density.cl:44-126 (poly6,
+//            cl_sph_kernels.h:29-45; neighbour walk cl_sph_neighbors.h:49-140)
+//   force:   rtpslib/system/sph/cl_src/force.cl:43-186 (spiky gradient
+//            cl_sph_kernels.h:81-97, viscosity Laplacian :118-127, XSPH)
+//
+// Neighbour walk.  The reference visits 27 cells (z, y, x in [c-1, c+1]) and
+// each cell's sorted range.  Keys of the three cells x-1, x, x+1 of one row
+// are consecutive integers, so their particles are one contiguous run of the
+// sorted arrays: the walk here is 9 row runs, visited in the reference's
+// order.  Integer row hashing equals the reference's float hash formula
+// whenever every intermediate value is an integer below 2^24 in magnitude
+// (checked on the host: int_hash_ok); otherwise each of the 27 cells is hashed
+// with the float formula.
+//
+// Cutoff.  |r| <= h with |r| = sqrtf(r2) is the same test as r2 <= rcut2,
+// rcut2 being the largest float whose correctly rounded square root is <= h
+// (sqrt is monotonic); r2 is formed without contraction, so neighbour sets are
+// identical to the oracle's.
+//
+// Density keeps the reference's summation order and rounding: it equals the
+// FP32 oracle bit for bit.  Force collects each particle's accepted
+// neighbours into a per-thread list in shared memory, then runs the heavy
+// arithmetic over the list with all lanes busy; the list keeps the walk order.
+// Exact=true evaluates force with the oracle's exact operations (IEEE
+// divisions, no contraction: bitwise equal); Exact=false uses FMA and
+// reciprocals (within the FP32 tolerance of the tests).
+#include "sph_physics.cuh"
+
+namespace sphk {
+
+// Visit the sorted-index runs of the 27 neighbour cells of scaled position
+// (px,py,pz), in the reference's order; f(rs, re) gets each non-empty run.
+template <class F>
+__device__ __forceinline__ void walk_rows(const StepParams& P, const uint32_t* __restrict__ cs,
+                                          const uint32_t* __restrict__ ce, float px, float py, float pz, F&& f) {
+    const int3 c = grid_cell(px, py, pz, P.gs_min, P.gs_delta);
+    const uint32_t C = (uint32_t)P.nb_cells;
+    const bool fast = P.int_hash_ok && c.x >= -1 && c.x <= P.res_x && c.y >= -1 && c.y <= P.res_y && c.z >= -1 &&
+                      c.z <= P.res_z;
+    if (fast) {
+#pragma unroll 1
+        for (int dz = -1; dz <= 1; ++dz) {
+#pragma unroll 1
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int base = ((c.z + dz) * P.res_y + (c.y + dy)) * P.res_x + c.x;
+                uint32_t rs = kEmpty, last = 0;
+#pragma unroll
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const uint32_t h = (uint32_t)(base + dx);
+                    if (h < C) {
+                        const uint32_t s = __ldg(cs + h);
+                        if (s != kEmpty) {
+                            if (rs == kEmpty) rs = s;
+                            last = h;
+                        }
+                    }
+                }
+                if (rs != kEmpty) f(rs, __ldg(ce + last));
+            }
+        }
+    } else {
+#pragma unroll 1
+        for (int z = c.z - 1; z <= c.z + 1; ++z)
+#pragma unroll 1
+            for (int y = c.y - 1; y <= c.y + 1; ++y)
+#pragma unroll 1
+                for (int x = c.x - 1; x <= c.x + 1; ++x) {
+                    const uint32_t h = (uint32_t)grid_hash_f(x, y, z, P.gs_res);
+                    if (h >= C) continue;
+                    const uint32_t s = __ldg(cs + h);
+                    if (s != kEmpty) f(s, __ldg(ce + h));
+                }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Density.  One thread per sorted particle.  When called from the fused step
+// it also does the out-of-grid deletion bookkeeping (vel_s != nullptr).
+template <bool Unit>
+__global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_s, float* __restrict__ density,
+                                                 uint32_t* __restrict__ nbr, const uint32_t* __restrict__ cs,
+                                                 const uint32_t* __restrict__ ce, int* __restrict__ info,
+                                                 const uint32_t* __restrict__ idx, const float4* __restrict__ vel_u,
+                                                 float4* __restrict__ vel_s, float4* __restrict__ del_pos,
+                                                 float4* __restrict__ del_vel, const StepParams P) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vel_s != nullptr && out >= 0 && i < n_old) {
+        // SPH.cpp:220-250: the kept particles' velocities in sorted order
+        // (call_prep copies vel_s to vel_u), the removed ones saved.
+        const float4 v = __ldg(vel_u + __ldg(idx + i));
+        if (i < n) {
+            vel_s[i] = v;
+        } else {
+            del_pos[i - n] = __ldg(pos_s + i);
+            del_vel[i - n] = v;
+            if (i == n) info[kDeleted] = n_old - n;
+        }
+    }
+    if (i >= n) return;
+    float4 pi = __ldg(pos_s + i);
+    if (!Unit) pi = v4scale(pi, P.sc);
+    const float rc2 = P.rcut2, h2 = P.h2;
+    float acc = 0.f;
+    uint32_t cnt = 0;
+    walk_rows(P, cs, ce, pi.x, pi.y, pi.z, [&](uint32_t rs, uint32_t re) {
+        for (uint32_t j = rs; j < re; ++j) {
+            float4 pj = __ldg(pos_s + j);
+            if (!Unit) pj = v4scale(pj, P.sc);
+            const float r2 = dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
+            if (r2 <= rc2) {
+                const float hr2 = __fsub_rn(h2, r2);
+                acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(hr2, hr2), hr2));
+                ++cnt;
+            }
+        }
+    });
+    density[i] = __fmul_rn(P.dens_coef, acc);
+    if (nbr) nbr[i] = cnt;
+}
+
+void launch_density(const float4* pos_s, float* density, uint32_t* nbr, const uint32_t* cell_start,
+                    const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
+                    float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
+                    cudaStream_t st) {
+    const int threads = 256;
+    int blocks = (grid_items + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+    if (p.unit_scale)
+        k_density<true><<<blocks, threads, 0, st>>>(pos_s, density, nbr, cell_start, cell_end, (int*)info, idx, vel_u,
+                                                    vel_s, del_pos, del_vel, p);
+    else
+        k_density<false><<<blocks, threads, 0, st>>>(pos_s, density, nbr, cell_start, cell_end, (int*)info, idx,
+                                                     vel_u, vel_s, del_pos, del_vel, p);
+}
+
+// ---------------------------------------------------------------------------
+// Force (+ collision + leapfrog when Fused).
+constexpr int kForceThreads = 128;
+constexpr int kListCap = 64;
+
+template <bool Exact>
+struct ForceAcc {
+    float fx = 0.f, fy = 0.f, fz = 0.f, vx = 0.f, vy = 0.f, vz = 0.f, xx = 0.f, xy = 0.f, xz = 0.f;
+};
+
+template <bool Fused, bool Exact, bool Unit>
+__global__ void __launch_bounds__(kForceThreads) k_force(
+    const float4* __restrict__ pos_s, const float* __restrict__ density, const float4* __restrict__ veleval_s,
+    const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const int* __restrict__ info,
+    float4* __restrict__ force_s, float4* __restrict__ xsph_s, uint32_t* __restrict__ idx,
+    const float4* __restrict__ vel_s, float4* __restrict__ pos_u, float4* __restrict__ vel_u,
+    float4* __restrict__ veleval_u, const StepParams P, const float dt) {
+    __shared__ uint32_t s_list[kListCap][kForceThreads];
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int t = threadIdx.x;
+
+    float4 pi = __ldg(pos_s + i);
+    if (!Unit) pi = v4scale(pi, P.sc);
+    const float4 vi = __ldg(veleval_s + i);
+    const float di = __ldg(density + i);
+    const float h = P.h, h2 = P.h2, rc2 = P.rcut2, eps = P.eps;
+    const float Pi = __fmul_rn(P.K, __fsub_rn(di, P.rho0));
+    ForceAcc<Exact> a;
+
+    auto flush = [&](int cnt) {
+        for (int k = 0; k < cnt; ++k) {
+            const uint32_t j = s_list[k][t];
+            float4 pj = __ldg(pos_s + j);
+            if (!Unit) pj = v4scale(pj, P.sc);
+            const float dx = __fsub_rn(pi.x, pj.x), dy = __fsub_rn(pi.y, pj.y), dz = __fsub_rn(pi.z, pj.z);
+            const float r2 = dist2_exact(dx, dy, dz);
+            const float dj = __ldg(density + j);
+            const float4 vj = __ldg(veleval_s + j);
+            const float dvx = __fsub_rn(vj.x, vi.x), dvy = __fsub_rn(vj.y, vi.y), dvz = __fsub_rn(vj.z, vi.z);
+            const float hr2 = __fsub_rn(h2, r2);
+            const float w6 = __fmul_rn(__fmul_rn(hr2, hr2), hr2);
+            const float Pj = __fmul_rn(P.K, __fsub_rn(dj, P.rho0));
+            const float dsum = __fadd_rn(di, dj);
+            if (Exact) {
+                float rlen = __fsqrt_rn(r2);
+                rlen = rlen < eps ? eps : rlen;
+                const float hr = __fsub_rn(h, rlen);
+                const float dWdr = __fdiv_rn(__fmul_rn(hr, hr), rlen);
+                const float idj = __frcp_rn(dj);
+                const float kern = __fmul_rn(__fmul_rn(dWdr, __fadd_rn(Pi, Pj)), idj);
+                a.vx = __fadd_rn(a.vx, __fmul_rn(__fmul_rn(dvx, hr), idj));
+                a.vy = __fadd_rn(a.vy, __fmul_rn(__fmul_rn(dvy, hr), idj));
+                a.vz = __fadd_rn(a.vz, __fmul_rn(__fmul_rn(dvz, hr), idj));
+                a.xx = __fadd_rn(a.xx, __fdiv_rn(__fmul_rn(w6, dvx), dsum));
+                a.xy = __fadd_rn(a.xy, __fdiv_rn(__fmul_rn(w6, dvy), dsum));
+                a.xz = __fadd_rn(a.xz, __fdiv_rn(__fmul_rn(w6, dvz), dsum));
+                a.fx = __fadd_rn(a.fx, __fmul_rn(dx, kern));
+                a.fy = __fadd_rn(a.fy, __fmul_rn(dy, kern));
+                a.fz = __fadd_rn(a.fz, __fmul_rn(dz, kern));
+            } else {
+                // r2 == 0 (coincident particles) gives NaN here and is
+                // caught by the same clamp as rlen < EPSILON.
+                const float inv_r = rsqrtf(r2);
+                float rlen = r2 * inv_r;
+                float irl = inv_r;
+                if (!(rlen >= eps)) {
+                    rlen = eps;
+                    irl = __frcp_rn(eps);
+                }
+                const float hr = h - rlen;
+                const float dWdr = hr * hr * irl;
+                const float idj = __frcp_rn(dj);
+                const float kern = dWdr * (Pi + Pj) * idj;
+                const float vh = hr * idj;
+                a.vx = fmaf(dvx, vh, a.vx);
+                a.vy = fmaf(dvy, vh, a.vy);
+                a.vz = fmaf(dvz, vh, a.vz);
+                const float wx = w6 * __frcp_rn(dsum);
+                a.xx = fmaf(wx, dvx, a.xx);
+                a.xy = fmaf(wx, dvy, a.xy);
+                a.xz = fmaf(wx, dvz, a.xz);
+                a.fx = fmaf(dx, kern, a.fx);
+                a.fy = fmaf(dy, kern, a.fy);
+                a.fz = fmaf(dz, kern, a.fz);
+            }
+        }
+    };
+
+    int cnt = 0;
+    walk_rows(P, cs, ce, pi.x, pi.y, pi.z, [&](uint32_t rs, uint32_t re) {
+        for (uint32_t j = rs; j < re; ++j) {
+            float4 pj = __ldg(pos_s + j);
+            if (!Unit) pj = v4scale(pj, P.sc);
+            const float r2 = dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
+            // The self term is multiplied by iej = 0 in the reference
+            // (force.cl:67,113,131,137): it adds a signed zero, so it is skipped.
+            if (r2 <= rc2 && j != (uint32_t)i) {
+                s_list[cnt][t] = j;
+                if (++cnt == kListCap) {
+                    flush(cnt);
+                    cnt = 0;
+                }
+            }
+        }
+    });
+    flush(cnt);
+
+    // force.cl:180-185: force = (mass/di)*(-0.5*wspiky_d*F + visc*wvisc_dd*V),
+    // xsph = 2*mass*wpoly6*X; the w lanes are zero.
+    float A;
+    if (Exact)
+        A = (float)((double)P.mass * (1.0 / (double)di));
+    else
+        A = P.mass * __frcp_rn(di);
+    float4 f, xs;
+    f.x = __fmul_rn(A, __fadd_rn(__fmul_rn(P.coef_b, a.fx), __fmul_rn(P.coef_s, a.vx)));
+    f.y = __fmul_rn(A, __fadd_rn(__fmul_rn(P.coef_b, a.fy), __fmul_rn(P.coef_s, a.vy)));
+    f.z = __fmul_rn(A, __fadd_rn(__fmul_rn(P.coef_b, a.fz), __fmul_rn(P.coef_s, a.vz)));
+    f.w = 0.f;
+    xs = make_float4(__fmul_rn(P.coef_d, a.xx), __fmul_rn(P.coef_d, a.xy), __fmul_rn(P.coef_d, a.xz), 0.f);
+    if (!Fused) {
+        force_s[i] = f;
+        xsph_s[i] = xs;
+        return;
+    }
+    // Fused collision_wall + leapfrog for particle i.  After an out-of-grid
+    // deletion the kept particles are re-indexed in sorted order (sort_indices
+    // becomes the identity and their velocities were gathered into vel_s).
+    uint32_t orig;
+    float4 v;
+    if (out >= 0) {
+        orig = (uint32_t)i;
+        v = vel_s[i];
+        idx[i] = (uint32_t)i;
+    } else {
+        orig = __ldg(idx + i);
+        v = vel_u[orig];
+    }
+    const float4 p = __ldg(pos_s + i);
+    const float4 psc = Unit ? p : v4scale(p, P.sc);
+    f = collide_walls(psc, v, f, P);
+    float4 po, vo, eo;
+    leapfrog_core(psc, v, f, xs, dt, P, po, vo, eo);
+    vel_u[orig] = vo;
+    veleval_u[orig] = eo;
+    pos_u[orig] = po;
+}
+
+void launch_force(const float4* pos_s, const float* density, const float4* veleval_s, const uint32_t* cell_start,
+                  const uint32_t* cell_end, const int* info, float4* force_s, float4* xsph_s, uint32_t* idx,
+                  const float4* /*vel_u_in*/, const float4* vel_s, float4* pos_u, float4* vel_u, float4* veleval_u,
+                  const StepParams& p, float dt, int fused, int exact, int grid_items, cudaStream_t st) {
+    const int threads = kForceThreads;
+    int blocks = (grid_items + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+#define SPH_FORCE_LAUNCH(F, E, U)                                                                               \
+    k_force<F, E, U><<<blocks, threads, 0, st>>>(pos_s, density, veleval_s, cell_start, cell_end, info, force_s, \
+                                                 xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, p, dt)
+    const bool u = p.unit_scale != 0;
+    if (fused) {
+        if (exact) {
+            if (u) SPH_FORCE_LAUNCH(true, true, true); else SPH_FORCE_LAUNCH(true, true, false);
+        } else {
+            if (u) SPH_FORCE_LAUNCH(true, false, true); else SPH_FORCE_LAUNCH(true, false, false);
+        }
+    } else {
+        if (exact) {
+            if (u) SPH_FORCE_LAUNCH(false, true, true); else SPH_FORCE_LAUNCH(false, true, false);
+        } else {
+            if (u) SPH_FORCE_LAUNCH(false, false, true); else SPH_FORCE_LAUNCH(false, false, false);
+        }
+    }
+#undef SPH_FORCE_LAUNCH
+}
+
+}  // namespace sphk

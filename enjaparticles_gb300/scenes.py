@@ -1,0 +1,70 @@
+"""Seeded synthetic scenes of the SPH benchmarks (dam break on a jittered lattice).
+
+The reference fills boxes with System::addBox -> addRect (rtpslib/domain/IV.cpp:
+165-202): a lattice enumerated z, then y, then x, stopping after `num` points.
+The benchmark scenes use the same enumeration on a lattice of spacing
+s = (0.125/N)^(1/3) at points ((i+1/2)s, (j+1/2)s, (k+1/2)s), i, j < ceil(0.5/s),
+each coordinate jittered by U(-0.01 s, +0.01 s).  Random numbers come from a
+counter-based splitmix64 stream, so every scene is reproducible on any host.
+"""
+import math
+
+import numpy as np
+
+_GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed, count, offset=0):
+    """The first `count` outputs (after `offset` skipped) of splitmix64(seed)."""
+    with np.errstate(over="ignore"):
+        k = np.arange(offset + 1, offset + count + 1, dtype=np.uint64)
+        z = np.uint64(seed) + k * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed, count, offset=0):
+    """Doubles in [0, 1) with 53 random bits."""
+    return (splitmix64(seed, count, offset) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def normal(seed, count, sigma=1.0):
+    """Box-Muller normals, two uniforms per value (cosine branch only)."""
+    u = uniform(seed, 2 * count).reshape(count, 2)
+    u1 = 1.0 - u[:, 0]  # (0, 1]
+    return sigma * np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u[:, 1])
+
+
+def lattice_spacing(n):
+    """s = (0.125 / n)^(1/3), the spacing that puts n points in [0, 0.5]^3."""
+    return float(np.float32((0.125 / n) ** (1.0 / 3.0)))
+
+
+def dambreak_positions(n, seed=20250101, spacing=None):
+    """float32 (n, 4) positions, w = 1, of the jittered dam-break lattice."""
+    s = lattice_spacing(n) if spacing is None else float(spacing)
+    side = int(math.ceil(0.5 / s - 1e-9))
+    layer = side * side
+    k = np.arange(n, dtype=np.int64)
+    iz, rem = np.divmod(k, layer)
+    iy, ix = np.divmod(rem, side)
+    jit = (2.0 * uniform(seed, 3 * n).reshape(n, 3) - 1.0) * (0.01 * s)
+    pos = np.empty((n, 4), dtype=np.float32)
+    pos[:, 0] = (ix + 0.5) * s + jit[:, 0]
+    pos[:, 1] = (iy + 0.5) * s + jit[:, 1]
+    pos[:, 2] = (iz + 0.5) * s + jit[:, 2]
+    pos[:, 3] = 1.0
+    return pos
+
+
+def dambreak(n, scene=0, velocity_sigma=0.0, velocity_seed=11):
+    """(pos, vel) float32 (n, 4) of a dam-break scene; vel ~ N(0, sigma^2) per
+    component when velocity_sigma > 0 (w lanes 0), else zero."""
+    pos = dambreak_positions(n, seed=20250101 + scene)
+    vel = np.zeros((n, 4), dtype=np.float32)
+    if velocity_sigma > 0:
+        vel[:, :3] = normal(velocity_seed, 3 * n, velocity_sigma).reshape(n, 3).astype(np.float32)
+    return pos, vel

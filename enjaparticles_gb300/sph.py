@@ -1,0 +1,167 @@
+"""Python mirror of the reference's rtps::SPH system over the C ABI.
+
+Method names follow rtpslib/system/System.h:61-186 and SPH.h:56-155 (update,
+integrate, pushParticles, addBox, getNum, ...), with the per-stage entry points
+of SPH::updateGPU (SPH.cpp:149-300) exposed for tests.  All compute runs in
+librtps_sph.so on the GPU; this class only moves host arrays.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class SPH:
+    def __init__(self, sphp, grid, max_num, grid_scaled=None, exact=False):
+        self.lib = abi.load_library()
+        self.ctx = C.c_void_p()
+        gs = C.byref(grid_scaled) if grid_scaled is not None else None
+        abi.check(self.lib, None, self.lib.sph_create(C.byref(sphp), C.byref(grid), gs, int(max_num),
+                                                      C.byref(self.ctx)))
+        self.max_num = int(max_num)
+        self.nb_cells = int(grid.nb_cells)
+        if exact:
+            self.set_exact(True)
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if self.ctx:
+            self.lib.sph_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc):
+        return abi.check(self.lib, self.ctx, rc)
+
+    # -- parameters -------------------------------------------------------
+    def set_exact(self, on=True):
+        self._ck(self.lib.sph_set_exact(self.ctx, 1 if on else 0))
+
+    def updateParams(self, sphp):
+        self._ck(self.lib.sph_set_params(self.ctx, C.byref(sphp)))
+
+    def params(self):
+        sp, g, gs = abi.SPHParams(), abi.GridParams(), abi.GridParams()
+        self._ck(self.lib.sph_get_params(self.ctx, C.byref(sp), C.byref(g), C.byref(gs)))
+        return sp, g, gs
+
+    # -- particles --------------------------------------------------------
+    @staticmethod
+    def _f4(a, n=None):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        if a.ndim != 2 or a.shape[1] != 4:
+            raise ValueError("expected an (n, 4) float32 array")
+        if n is not None and a.shape[0] != n:
+            raise ValueError("array length mismatch")
+        return a
+
+    def upload(self, pos, vel, veleval=None):
+        pos = self._f4(pos)
+        n = pos.shape[0]
+        vel = self._f4(vel, n)
+        ve = None if veleval is None else self._f4(veleval, n)
+        self._keep = (pos, vel, ve)  # host memory must outlive the asynchronous copy
+        self._ck(self.lib.sph_upload(self.ctx, pos.ctypes.data, vel.ctypes.data,
+                                     None if ve is None else ve.ctypes.data, n))
+        self.sync()
+
+    def pushParticles(self, pos, vel):
+        pos = self._f4(pos)
+        vel = self._f4(vel, pos.shape[0])
+        self._ck(self.lib.sph_push_particles(self.ctx, pos.ctypes.data, vel.ctypes.data, pos.shape[0]))
+
+    def getNum(self):
+        n = C.c_int()
+        self._ck(self.lib.sph_get_num(self.ctx, C.byref(n)))
+        return n.value
+
+    def get(self, field, n=None):
+        """Blocking copy of a field (see abi.FIELDS) to a new numpy array."""
+        dt, w = abi.FIELD_DTYPE[field]
+        if n is None:
+            n = self.nb_cells + 1 if field in ("cell_start", "cell_end") else self.getNum()
+        out = np.empty((n, w) if w > 1 else (n,), dtype=dt)
+        self._ck(self.lib.sph_download(self.ctx, abi.FIELDS[field], out.ctypes.data, n))
+        return out
+
+    def device_ptr(self, field):
+        p = C.c_void_p()
+        self._ck(self.lib.sph_get_device_ptr(self.ctx, abi.FIELDS[field], C.byref(p)))
+        return p.value
+
+    def getDeleted(self):
+        cnt = C.c_int()
+        self._ck(self.lib.sph_get_deleted(self.ctx, None, None, 0, C.byref(cnt)))
+        pos = np.empty((cnt.value, 4), np.float32)
+        vel = np.empty((cnt.value, 4), np.float32)
+        if cnt.value:
+            self._ck(self.lib.sph_get_deleted(self.ctx, pos.ctypes.data, vel.ctypes.data, cnt.value, C.byref(cnt)))
+        return pos, vel
+
+    # -- stages (SPH::updateGPU order) -----------------------------------
+    def hash(self):
+        self._ck(self.lib.sph_stage_hash(self.ctx))
+
+    def sort(self):
+        self._ck(self.lib.sph_stage_sort(self.ctx))
+
+    def cellindices(self):
+        nc = C.c_int()
+        self._ck(self.lib.sph_stage_cellindices(self.ctx, C.byref(nc)))
+        return nc.value
+
+    def permute(self):
+        self._ck(self.lib.sph_stage_permute(self.ctx))
+
+    def density(self):
+        self._ck(self.lib.sph_stage_density(self.ctx))
+
+    def force(self):
+        self._ck(self.lib.sph_stage_force(self.ctx))
+
+    def collision(self):
+        self._ck(self.lib.sph_stage_collision(self.ctx))
+
+    def leapfrog(self, dt):
+        self._ck(self.lib.sph_stage_leapfrog(self.ctx, float(dt)))
+
+    # -- whole steps --------------------------------------------------------
+    def update(self):
+        """SPH::update: hash ... collision."""
+        self._ck(self.lib.sph_update(self.ctx))
+
+    def integrate(self, dt):
+        """SPH::integrate (leapfrog)."""
+        self._ck(self.lib.sph_integrate(self.ctx, float(dt)))
+
+    def step(self, dt, nsteps=1):
+        """nsteps fused update+integrate steps, replayed from a CUDA graph."""
+        self._ck(self.lib.sph_step(self.ctx, float(dt), int(nsteps)))
+
+    def step_eager(self, dt, nsteps=1):
+        self._ck(self.lib.sph_step_eager(self.ctx, float(dt), int(nsteps)))
+
+    def sync(self):
+        self._ck(self.lib.sph_sync(self.ctx))
+
+
+def dambreak_system(n, viscosity=0.01, max_num=None, exact=False, velocity_sigma=0.0, scene=0):
+    """An SPH system holding the dam-break scene of n particles."""
+    from .scenes import dambreak
+    sp, g, gs = abi.dambreak_params(n, viscosity)
+    s = SPH(sp, g, max_num or n, gs, exact=exact)
+    pos, vel = dambreak(n, scene=scene, velocity_sigma=velocity_sigma)
+    s.upload(pos, vel)
+    return s, (sp, g, gs), (pos, vel)

@@ -1,0 +1,301 @@
+/*
+ * rtps_sph.h — C ABI of librtps_sph.so, the GB300 (sm_103a) SPH particle step.
+ *
+ * This boundary replaces the OpenCL host layer of the RTPS / EnjaParticles
+ * reference (rtpslib/opencl: CL context CLL.h:46-87, Kernel::execute/setArg
+ * Kernel.h:46-77, Buffer<T> copies Buffer.h:44-106) for the SPH path
+ * SPH::updateGPU (rtpslib/system/SPH.cpp:149-300) + SPH::integrate
+ * (SPH.cpp:389-441).  Every stage object of that path has one entry point
+ * here, and the whole per-frame sequence has one more (sph_step).
+ *
+ * Conventions
+ *   - Plain C: no C++ or torch types.  All particle arrays are float4
+ *     array-of-structs (16 bytes per particle), as in the reference.
+ *   - "_u" fields are in original (unsorted) particle order, "_s" fields in
+ *     the order of the last sort (cell key, then original index).
+ *   - Every function returns an int status: SPH_OK (0) or a negative code.
+ *     sph_last_error() gives the message of the last failure on a context.
+ *   - A context owns one CUDA stream and all device memory of one particle
+ *     system.  Calls are asynchronous with respect to the host unless their
+ *     comment says otherwise; sph_sync() waits.  A context is not
+ *     thread-safe: one host thread drives it at a time.
+ */
+#ifndef RTPS_SPH_H
+#define RTPS_SPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__) || defined(__clang__)
+#define SPH_ALIGN16 __attribute__((aligned(16)))
+#else
+#define SPH_ALIGN16
+#endif
+
+/* rtpslib/structs.h:403-578 — float4, 16-byte aligned. */
+typedef struct sph_float4 {
+    float x, y, z, w;
+} SPH_ALIGN16 sph_float4;
+
+/* SPHParams, byte-compatible with rtpslib/system/SPHSettings.h:38-136 and its
+ * OpenCL copy rtpslib/system/sph/cl_src/cl_sph_structs.h:30-75 (144 bytes). */
+typedef struct SPHParams {
+    float rest_density;        /*   0 */
+    float mass;                /*   4 */
+    float rest_distance;       /*   8 */
+    float smoothing_distance;  /*  12  h */
+    float simulation_scale;    /*  16 */
+    float boundary_stiffness;  /*  20 */
+    float boundary_dampening;  /*  24 */
+    float boundary_distance;   /*  28 */
+    float K;                   /*  32  gas constant */
+    float viscosity;           /*  36 */
+    float velocity_limit;      /*  40  (clamps the acceleration norm) */
+    float xsph_factor;         /*  44 */
+    float friction_coef;       /*  48 */
+    float restitution_coef;    /*  52 */
+    float shear;               /*  56 */
+    float attraction;          /*  60 */
+    float spring;              /*  64 */
+    float EPSILON;             /*  68 */
+    float wpoly6_coef;         /*  72 */
+    float wpoly6_d_coef;       /*  76 */
+    float wpoly6_dd_coef;      /*  80 */
+    float wspiky_coef;         /*  84 */
+    float wspiky_d_coef;       /*  88 */
+    float wspiky_dd_coef;      /*  92 */
+    float wvisc_coef;          /*  96 */
+    float wvisc_d_coef;        /* 100 */
+    float wvisc_dd_coef;       /* 104 */
+    int   num;                 /* 108 */
+    int   max_num;             /* 112 */
+    sph_float4 gravity;        /* 128 */
+} SPH_ALIGN16 SPHParams;
+
+/* GridParams, byte-compatible with rtpslib/domain/Domain.h:144-158 and
+ * rtpslib/system/common/cl_src/cl_structs.h:29-43 (128 bytes).  grid_res is
+ * float, as in the reference. */
+typedef struct GridParams {
+    sph_float4 grid_size;   /*   0 */
+    sph_float4 grid_min;    /*  16 */
+    sph_float4 grid_max;    /*  32 */
+    sph_float4 bnd_min;     /*  48 */
+    sph_float4 bnd_max;     /*  64 */
+    sph_float4 grid_res;    /*  80 */
+    sph_float4 grid_delta;  /*  96  cells per unit length */
+    int        nb_cells;    /* 112 */
+} SPH_ALIGN16 GridParams;
+
+#ifdef __cplusplus
+static_assert(sizeof(SPHParams) == 144, "SPHParams must be 144 bytes");
+static_assert(offsetof(SPHParams, EPSILON) == 68, "SPHParams.EPSILON offset");
+static_assert(offsetof(SPHParams, wvisc_dd_coef) == 104, "SPHParams.wvisc_dd_coef offset");
+static_assert(offsetof(SPHParams, num) == 108, "SPHParams.num offset");
+static_assert(offsetof(SPHParams, max_num) == 112, "SPHParams.max_num offset");
+static_assert(offsetof(SPHParams, gravity) == 128, "SPHParams.gravity offset");
+static_assert(sizeof(GridParams) == 128, "GridParams must be 128 bytes");
+static_assert(offsetof(GridParams, grid_res) == 80, "GridParams.grid_res offset");
+static_assert(offsetof(GridParams, grid_delta) == 96, "GridParams.grid_delta offset");
+static_assert(offsetof(GridParams, nb_cells) == 112, "GridParams.nb_cells offset");
+#else
+_Static_assert(sizeof(SPHParams) == 144, "SPHParams must be 144 bytes");
+_Static_assert(sizeof(GridParams) == 128, "GridParams must be 128 bytes");
+#endif
+
+/* Status codes. */
+#define SPH_OK         0
+#define SPH_EINVAL    -1  /* bad argument (null pointer, n > capacity, NaN parameter, ...) */
+#define SPH_ENOMEM    -2  /* device allocation failed */
+#define SPH_ECUDA     -3  /* a CUDA runtime call failed; see sph_last_error */
+#define SPH_EOOB      -4  /* particles left the grid (reported, not trapped) */
+#define SPH_ETIMEOUT  -5  /* a bounded device-side wait expired; the step is invalid */
+#define SPH_ESTATE    -6  /* call not valid in the context's current state */
+
+/* Value of an empty cell in cell_start (CellIndices.cpp:58-62). */
+#define SPH_EMPTY_CELL 0xffffffffu
+
+/* Fields for sph_download / sph_get_device_ptr. */
+enum sph_field {
+    SPH_FIELD_POS_U = 0,      /* float4[max_num] original order */
+    SPH_FIELD_VEL_U = 1,      /* float4[max_num] */
+    SPH_FIELD_VELEVAL_U = 2,  /* float4[max_num] */
+    SPH_FIELD_POS_S = 3,      /* float4[max_num] sorted order */
+    SPH_FIELD_VEL_S = 4,      /* float4[max_num] (written by sph_stage_permute only) */
+    SPH_FIELD_VELEVAL_S = 5,  /* float4[max_num] */
+    SPH_FIELD_DENSITY_S = 6,  /* float[max_num] */
+    SPH_FIELD_FORCE_S = 7,    /* float4[max_num] (written by the staged path only) */
+    SPH_FIELD_XSPH_S = 8,     /* float4[max_num] (written by the staged path only) */
+    SPH_FIELD_SORT_HASHES = 9,   /* uint32[max_num] */
+    SPH_FIELD_SORT_INDICES = 10, /* uint32[max_num] */
+    SPH_FIELD_CELL_START = 11,   /* uint32[nb_cells+1] */
+    SPH_FIELD_CELL_END = 12,     /* uint32[nb_cells+1] */
+    SPH_FIELD_NEIGHBOR_COUNT = 13, /* uint32[max_num] neighbours within h, self included (density stage) */
+    SPH_FIELD_COUNT_ = 14
+};
+
+typedef struct sph_ctx sph_ctx;
+
+/* ---------------------------------------------------------------------------
+ * Host-side parameter helpers (no device work; usable without a GPU).
+ * ------------------------------------------------------------------------- */
+
+/* Domain::calculateCells + System::setupDomain (rtpslib/domain/Domain.cpp:38-81,
+ * rtpslib/system/System.cpp:294-329): pad [bnd_min, bnd_max] by 2*cell_size,
+ * res = ceil(size/cell), delta = res/size, nb_cells = res.x*res.y*res.z.
+ * Writes the unscaled grid and the copy scaled by sim_scale. */
+int sph_setup_domain(const sph_float4* bnd_min, const sph_float4* bnd_max,
+                     float cell_size, float sim_scale,
+                     GridParams* grid, GridParams* grid_scaled);
+
+/* The settings store of the reference keeps every derived number as a string
+ * written at 6 significant digits (rtpslib/RTPSSettings.h:78-85); this returns
+ * the float that such a round trip yields. */
+float sph_settings_round(float value);
+
+/* Kernel coefficients of SPH::calculate (rtpslib/system/SPHSettings.cpp:111-119)
+ * for smoothing distance h, each passed through sph_settings_round. */
+int sph_kernel_coefficients(float h, SPHParams* sphp);
+
+/* The dam-break parameter set of the benchmark configurations: lattice
+ * spacing s, h = 2s, rest_distance = s, mass = rest_density*s^3, unit-box
+ * domain, with the constants given (viscosity, gas constant, wall stiffness
+ * and damping, velocity limit, XSPH factor, gravity z).  Coefficients and
+ * derived values are rounded as sph_settings_round does. */
+int sph_dambreak_params(int num, float spacing, float viscosity,
+                        SPHParams* sphp, GridParams* grid, GridParams* grid_scaled);
+
+/* ---------------------------------------------------------------------------
+ * Context lifetime (System::System / SPH::SPH / prepareSorted,
+ * System.cpp:47-89,198-291, SPH.cpp:50-99,482-520).
+ * ------------------------------------------------------------------------- */
+
+/* Allocate a context for up to max_num particles on the current CUDA device.
+ * grid_scaled may be NULL, in which case it is derived from grid and
+ * sphp->simulation_scale as System::setupDomain does.  Requires
+ * grid->nb_cells + 1 < 2^24 (the reference computes cell hashes in float).
+ * Blocking. */
+int sph_create(const SPHParams* sphp, const GridParams* grid,
+               const GridParams* grid_scaled, int max_num, sph_ctx** out);
+int sph_destroy(sph_ctx* ctx);
+
+/* SPH::updateParams (SPHSettings.cpp:149-200): replace the parameter block.
+ * sphp->num is ignored (the particle count is owned by the context). */
+int sph_set_params(sph_ctx* ctx, const SPHParams* sphp);
+int sph_get_params(sph_ctx* ctx, SPHParams* sphp, GridParams* grid, GridParams* grid_scaled);
+
+/* Use an external CUDA stream (cudaStream_t passed as void*); NULL restores the
+ * context's own stream. */
+int sph_set_stream(sph_ctx* ctx, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Particle data (Buffer<T>::copyToDevice/copyToHost, SPH::pushParticles
+ * SPH.cpp:560-602).
+ * ------------------------------------------------------------------------- */
+
+/* Replace the state with n particles.  veleval may be NULL: it is then zero,
+ * as in the reference, where pushParticles never writes veleval.  Host
+ * pointers; pinned memory makes the copy asynchronous. */
+int sph_upload(sph_ctx* ctx, const sph_float4* pos, const sph_float4* vel,
+               const sph_float4* veleval, int n);
+/* Append n particles after the current ones (pushParticles; veleval of the
+ * new particles keeps whatever the buffer held, zero on a fresh context). */
+int sph_push_particles(sph_ctx* ctx, const sph_float4* pos, const sph_float4* vel, int n);
+/* Copy n elements of a field to host memory.  Blocking. */
+int sph_download(sph_ctx* ctx, int field, void* host, int n);
+/* Same, without waiting: the copy is ordered on the context stream; call
+ * sph_sync before reading host memory (which should be pinned). */
+int sph_download_async(sph_ctx* ctx, int field, void* host, int n);
+/* Device address of a field, for zero-copy use (e.g. torch.from_blob). */
+int sph_get_device_ptr(sph_ctx* ctx, int field, void** dptr);
+/* Current particle count (after any out-of-grid deletion).  Blocking. */
+int sph_get_num(sph_ctx* ctx, int* num);
+/* Set the particle count after writing state through sph_get_device_ptr. */
+int sph_set_num(sph_ctx* ctx, int num);
+
+/* ---------------------------------------------------------------------------
+ * Stages.  One entry point per stage object of SPH::updateGPU / integrate.
+ * ------------------------------------------------------------------------- */
+
+/* Hash::execute (Hash.cpp:42-75; hash.cl:50-157): sort_hashes[i] = cell key of
+ * pos_u[i] from the unscaled grid (nb_cells when outside), sort_indices[i] = i. */
+int sph_stage_hash(sph_ctx* ctx);
+/* System::bitonic_sort (System.cpp:407-480), replaced by a stable LSD radix
+ * sort: ascending keys, equal keys in ascending original index. */
+int sph_stage_sort(sph_ctx* ctx);
+/* CellIndices::execute (CellIndices.cpp:42-169; cellindices.cl:12-107).
+ * cell_start = first sorted index of each cell (SPH_EMPTY_CELL if empty),
+ * cell_end = one past the last (only written for occupied cells).  *nc gets
+ * cell_start[nb_cells] as int (-1 when no particle is outside the grid).
+ * nc may be NULL; when not NULL the call blocks. */
+int sph_stage_cellindices(sph_ctx* ctx, int* nc);
+/* Permute::execute (Permute.cpp:45-108; permute.cl:10-46): X_s[i] = X_u[idx[i]]
+ * for pos, vel, veleval. */
+int sph_stage_permute(sph_ctx* ctx);
+/* Density::execute (sph/Density.cpp:52-92; density.cl:44-126). */
+int sph_stage_density(sph_ctx* ctx);
+/* Force::execute (sph/Force.cpp:52-94; force.cl:43-186): force_s, xsph_s. */
+int sph_stage_force(sph_ctx* ctx);
+/* CollisionWall::execute (sph/Collision_wall.cpp:39-67; collision_wall.cl:31-118):
+ * force_s += wall repulsion and friction. */
+int sph_stage_collision(sph_ctx* ctx);
+/* LeapFrog::execute (sph/LeapFrog.cpp:42-83; leapfrog.cl:30-121): integrate and
+ * scatter to pos_u, vel_u, veleval_u. */
+int sph_stage_leapfrog(sph_ctx* ctx, float dt);
+
+/* SPH::update (SPH.cpp:117-125 -> updateGPU :149-300) with the wall collision
+ * of SPH::collision (SPH.cpp:303-336) enabled after gravity: hash, sort,
+ * cellindices, permute, out-of-grid deletion, density, force, collision. */
+int sph_update(sph_ctx* ctx);
+/* SPH::integrate (SPH.cpp:389-441), leapfrog integrator. */
+int sph_integrate(sph_ctx* ctx, float dt);
+
+/* nsteps x (update + integrate) on the fused path: hash -> sort ->
+ * cellindices+permute -> density -> force+collision+leapfrog, replayed from a
+ * captured CUDA graph.  Results equal nsteps staged update()+integrate()
+ * calls.  Asynchronous. */
+int sph_step(sph_ctx* ctx, float dt, int nsteps);
+
+/* The same fused step launched kernel by kernel, without a graph (for
+ * profiling and for callers that capture their own graphs). */
+int sph_step_eager(sph_ctx* ctx, float dt, int nsteps);
+
+/* nsteps fused steps launched kernel by kernel with a CUDA event between
+ * launches on the context stream, for per-kernel timing.  kernel_ms[k]
+ * accumulates the device time of launch k of the step (k < cap); *nkernels
+ * gets the number of launches per step; names come from
+ * sph_profile_kernel_name.  Blocking. */
+int sph_step_profile(sph_ctx* ctx, float dt, int nsteps, float* kernel_ms, int cap, int* nkernels);
+const char* sph_profile_kernel_name(sph_ctx* ctx, int k);
+
+/* Force-stage arithmetic.  0 (default): FMA and reciprocals, within the
+ * FP32 tolerance of the oracle.  1: the oracle's exact operation sequence
+ * (IEEE divisions and square roots, no contraction), bitwise equal to the
+ * FP32 oracle.  Hash, sort, cell ranges, permute, density, collision and
+ * leapfrog are always exact. */
+int sph_set_exact(sph_ctx* ctx, int exact);
+
+/* Particles removed by the last out-of-grid deletion (SPH.cpp:220-250 keeps
+ * them in deleted_pos / deleted_vel, getDeletedPos/Vel SPH.h:83-84): copies up
+ * to cap of them and stores their number in *count.  Blocking. */
+int sph_get_deleted(sph_ctx* ctx, sph_float4* pos, sph_float4* vel, int cap, int* count);
+
+/* Wait for all work on the context stream; reports device-side errors
+ * (SPH_ETIMEOUT) and out-of-grid deletions are visible through sph_get_num. */
+int sph_sync(sph_ctx* ctx);
+
+/* Copy the message of the last error on ctx (or of the last failed
+ * sph_create when ctx is NULL) into buf. */
+int sph_last_error(sph_ctx* ctx, char* buf, int len);
+
+/* Library identification string (build flags, arch). */
+const char* sph_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTPS_SPH_H */

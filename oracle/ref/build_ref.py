@@ -1,0 +1,100 @@
+#!/usr/bin/env python3
+"""Build oracle/_ref/librtps_ref.so: the reference's own SPH kernels, run on the host.
+
+TEST INFRASTRUCTURE.  The reference (RTPS / EnjaParticles) cannot run as
+shipped: its host code needs a GL context and its kernels need an OpenCL
+driver, and neither exists on these machines.  Its OpenCL C kernel sources are
+plain arithmetic, though, so this recipe compiles them for the host with g++:
+
+  1. copy the kernel sources the SPH step uses from the reference tree
+     (rtpslib/system/common/cl_src, rtpslib/system/sph/cl_src) into a
+     temporary directory laid out as the reference's build lays them out
+     (cl_common/, cl_sph/; rtpslib/system/sph/CMakeLists.txt:3-11);
+  2. rewrite two pieces of OpenCL-only syntax there, nothing else:
+       `(float4)(a, b, c, d)` / `(int4)(...)`  ->  `make_float4(...)` / `make_int4(...)`
+       kernel-scope `__local T name[N];` arrays  ->  `static T name[N];`
+     (work-groups run one at a time, so a static array is the group's local
+     memory);
+  3. compile them with clshim.hpp (vector types, built-ins, barrier) and the
+     ref_*.cpp drivers, plus the reference's host Domain.cpp / structs.cpp
+     unchanged, into oracle/_ref/librtps_ref.so.  -ffp-contract=off keeps
+     every multiply and add separately rounded, as written.
+
+The temporary copies are deleted; only the shared library is kept, under
+oracle/_ref/ (git-ignored).  Nothing from the reference is written into the
+repository.  Usage: python oracle/ref/build_ref.py [--reference DIR].
+"""
+import argparse
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE = os.path.dirname(HERE)
+OUT_DIR = os.path.join(ORACLE, "_ref")
+OUT_LIB = os.path.join(OUT_DIR, "librtps_ref.so")
+
+COMMON = ["hash.cl", "cl_hash.h", "cl_structs.h", "cl_macros.h", "cellindices.cl", "permute.cl", "bitonic.cl"]
+SPH = ["density.cl", "force.cl", "collision_wall.cl", "leapfrog.cl", "cl_sph_kernels.h", "cl_sph_neighbors.h",
+       "cl_sph_structs.h", "cl_sph_collision.h", "cl_sph_macros.h"]
+DRIVERS = ["ref_runtime.cpp", "ref_hash.cpp", "ref_bitonic.cpp", "ref_cellindices.cpp", "ref_permute.cpp",
+           "ref_density.cpp", "ref_force.cpp", "ref_collision.cpp", "ref_leapfrog.cpp", "ref_domain.cpp"]
+
+VEC_LITERAL = re.compile(r"\((float4|int4)\)\s*\(")
+LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
+
+
+def rewrite(text):
+    text = VEC_LITERAL.sub(lambda m: "make_%s(" % m.group(1), text)
+    text = LOCAL_ARRAY.sub(r"\1static\2", text)
+    return text
+
+
+def build(reference, verbose=False):
+    src_common = os.path.join(reference, "rtpslib", "system", "common", "cl_src")
+    src_sph = os.path.join(reference, "rtpslib", "system", "sph", "cl_src")
+    rtpslib = os.path.join(reference, "rtpslib")
+    for d in (src_common, src_sph):
+        if not os.path.isdir(d):
+            raise FileNotFoundError(d)
+    os.makedirs(OUT_DIR, exist_ok=True)
+    tmp = tempfile.mkdtemp(prefix="rtps_ref_")
+    try:
+        for sub, names, src in (("cl_common", COMMON, src_common), ("cl_sph", SPH, src_sph)):
+            os.makedirs(os.path.join(tmp, sub))
+            for name in names:
+                with open(os.path.join(src, name), "r", errors="replace") as f:
+                    text = f.read()
+                with open(os.path.join(tmp, sub, name), "w") as f:
+                    f.write(rewrite(text))
+        cxx = os.environ.get("CXX", "g++")
+        cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+               "-w", "-I", tmp, "-I", HERE, "-I", rtpslib]
+        cmd += [os.path.join(HERE, d) for d in DRIVERS]
+        cmd += [os.path.join(rtpslib, "domain", "Domain.cpp"), os.path.join(rtpslib, "structs.cpp")]
+        cmd += ["-o", OUT_LIB]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return OUT_LIB
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("-v", "--verbose", action="store_true")
+    a = ap.parse_args()
+    if not os.path.isdir(a.reference):
+        print("reference tree not found at %s; nothing built" % a.reference)
+        return 0
+    print(build(a.reference, a.verbose))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,21 @@
+// TEST INFRASTRUCTURE: C entry points of oracle/_ref/librtps_ref.so, the
+// reference's own OpenCL kernels compiled for the host (see build_ref.py).
+#pragma once
+#include <cstdint>
+extern "C" {
+void ref_hash(int n, const float* pos_u, const void* gp, uint32_t* keys, uint32_t* idx);
+void ref_bitonic_sort(int n, uint32_t* keys, uint32_t* idx);
+int ref_cellindices(int n, const uint32_t* keys, const uint32_t* idx, uint32_t* start, uint32_t* end, const void* gp);
+void ref_permute(int n, const uint32_t* idx, const float* pos_u, const float* vel_u, const float* veleval_u,
+                 float* pos_s, float* vel_s, float* veleval_s);
+void ref_density(int n, const float* pos_s, float* density, const uint32_t* start, const uint32_t* end,
+                 const void* gps, const void* sphp);
+void ref_force(int n, const float* pos_s, const float* density, const float* veleval_s, float* force, float* xsph,
+               const uint32_t* start, const uint32_t* end, const void* gps, const void* sphp);
+void ref_collision_wall(int n, const float* pos_s, const float* vel_s, float* force, const void* gps,
+                        const void* sphp);
+void ref_leapfrog(int n, float* pos_u, const float* pos_s, float* vel_u, const float* vel_s, float* veleval_u,
+                  const float* force, const float* xsph, const uint32_t* idx, const void* sphp, float dt);
+void ref_setup_domain(const float* bnd_min, const float* bnd_max, float cell_size, float sim_scale, void* grid,
+                      void* grid_scaled);
+}

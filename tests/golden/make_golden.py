@@ -1,0 +1,124 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures of tests/golden/ from the reference's own kernels.
+
+Needs oracle/_ref/librtps_ref.so (python oracle/ref/build_ref.py, which reads
+the reference tree).  Every array here comes from the reference's OpenCL
+kernels compiled for the host and driven in SPH::updateGPU order by
+tests/ref_driver.py, with the (unstable) bitonic sort canonicalised within
+equal keys by original index.  The inputs are the seeded scenes of
+enjaparticles_gb300.scenes and the parameter blocks of sph_dambreak_params;
+both are stored too, so the fixtures stand alone.
+
+Fixtures
+  stages_n4096.npz   dam-break rule at N=4096, v0 ~ N(0, 0.1^2): every stage
+                     output of step 1, and pos/vel/veleval after steps 2 and 10
+  ragged_n1000.npz   N=1000 (not a multiple of any block size), 3 steps
+  outofgrid_n512.npz N=512 with 37 particles placed outside the grid: the
+                     out-of-grid deletion path of SPH.cpp:220-250, 2 steps
+  cfg0_n16384.npz    the 16,384-particle dam break: pos/vel after 1, 10, 100 steps
+Usage: python tests/golden/make_golden.py
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from enjaparticles_gb300 import abi, scenes  # noqa: E402
+import ref_driver  # noqa: E402
+
+DT = 0.001
+
+
+def params_blob(sp, g, gs):
+    return {"sphp": np.frombuffer(bytes(sp), np.uint8).copy(), "grid": np.frombuffer(bytes(g), np.uint8).copy(),
+            "grid_scaled": np.frombuffer(bytes(gs), np.uint8).copy()}
+
+
+def state(R, prefix):
+    n = R.num
+    return {prefix + "pos_u": R.pos_u[:n].copy(), prefix + "vel_u": R.vel_u[:n].copy(),
+            prefix + "veleval_u": R.veleval_u[:n].copy(), prefix + "num": np.int32(n)}
+
+
+def stages_fixture(n, sigma, steps_after=(2, 10)):
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n, velocity_sigma=sigma)
+    R = ref_driver.RefSystem(sp, g, gs, n)
+    R.upload(pos, vel)
+    out = dict(params_blob(sp, g, gs))
+    out.update({"in_pos": pos, "in_vel": vel, "dt": np.float32(DT)})
+    R.update()
+    out.update({"s1_hash_keys": R.trace["hash_keys"], "s1_sort_hashes": R.keys[:n].copy(),
+                "s1_sort_indices": R.idx[:n].copy(), "s1_cell_start": R.start.copy(), "s1_cell_end": R.end.copy(),
+                "s1_nc": np.int32(R.trace["nc"]), "s1_pos_s": R.pos_s[:n].copy(), "s1_vel_s": R.vel_s[:n].copy(),
+                "s1_veleval_s": R.veleval_s[:n].copy(), "s1_density_s": R.density_s[:n].copy(),
+                "s1_force_pre": R.trace["force_pre_collision"], "s1_force_s": R.force_s[:n].copy(),
+                "s1_xsph_s": R.xsph_s[:n].copy()})
+    R.integrate(DT)
+    out.update(state(R, "s1_"))
+    done = 1
+    for k in steps_after:
+        R.step(DT, k - done)
+        done = k
+        out.update(state(R, "s%d_" % k))
+    return out
+
+
+def outofgrid_fixture():
+    n = 512
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n, velocity_sigma=0.05)
+    rng_u = scenes.uniform(77, 37 * 3).reshape(37, 3)
+    far = np.where(rng_u < 0.5, -0.6 - rng_u, 1.6 + rng_u).astype(np.float32)
+    sel = (np.arange(37) * 13 + 5) % n
+    pos[sel, :3] = far
+    R = ref_driver.RefSystem(sp, g, gs, n)
+    R.upload(pos, vel)
+    out = dict(params_blob(sp, g, gs))
+    out.update({"in_pos": pos, "in_vel": vel, "dt": np.float32(DT)})
+    R.update()
+    out.update({"s1_nc": np.int32(R.trace["nc"]), "s1_deleted_pos": R.deleted_pos.copy(),
+                "s1_deleted_vel": R.deleted_vel.copy(), "s1_sort_indices": R.idx[:R.num].copy(),
+                "s1_density_s": R.density_s[:R.num].copy()})
+    R.integrate(DT)
+    out.update(state(R, "s1_"))
+    R.step(DT, 1)
+    out.update(state(R, "s2_"))
+    return out
+
+
+def cfg0_fixture():
+    n = 16384
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n)
+    R = ref_driver.RefSystem(sp, g, gs, n)
+    R.upload(pos, vel)
+    out = dict(params_blob(sp, g, gs))
+    out.update({"in_pos": pos, "in_vel": vel, "dt": np.float32(DT)})
+    done = 0
+    for k in (1, 10, 100):
+        R.step(DT, k - done)
+        done = k
+        out["s%d_pos_u" % k] = R.pos_u[:n].copy()
+        out["s%d_vel_u" % k] = R.vel_u[:n].copy()
+    return out
+
+
+def main():
+    np.savez_compressed(os.path.join(HERE, "stages_n4096.npz"), **stages_fixture(4096, 0.1))
+    np.savez_compressed(os.path.join(HERE, "ragged_n1000.npz"), **stages_fixture(1000, 0.1, steps_after=(3,)))
+    np.savez_compressed(os.path.join(HERE, "outofgrid_n512.npz"), **outofgrid_fixture())
+    np.savez_compressed(os.path.join(HERE, "cfg0_n16384.npz"), **cfg0_fixture())
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

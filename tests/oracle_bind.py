@@ -1,0 +1,157 @@
+"""ctypes bindings of the CPU oracle (oracle/_build/libsph_oracle.so) and of the
+reference's own kernels compiled for the host (oracle/_ref/librtps_ref.so).
+
+Test infrastructure only: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libsph_oracle.so")
+REF_LIB = os.path.join(ORACLE_DIR, "_ref", "librtps_ref.so")
+
+_P = C.c_void_p
+_I = C.c_int
+_F = C.c_float
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+    return ORACLE_LIB
+
+
+_oracle = None
+_ref = None
+
+
+def oracle():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_LIB):
+            build_oracle()
+        lib = C.CDLL(ORACLE_LIB)
+        sig = {
+            "oracle_info": (C.c_char_p, []),
+            "oracle_threads": (_I, []),
+            "oracle_set_threads": (None, [_I]),
+            "oracle_hash": (None, [_I, _P, _P, _P, _P]),
+            "oracle_sort": (None, [_I, _P, _P]),
+            "oracle_sort_std": (None, [_I, _P, _P]),
+            "oracle_cellindices": (_I, [_I, _P, _P, _P, _I]),
+            "oracle_permute": (None, [_I, _P, _P, _P, _P, _P, _P, _P]),
+            "oracle_density": (None, [_I, _I, _P, _P, _P, _P, _P, _P, _P]),
+            "oracle_force": (None, [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+            "oracle_collision": (None, [_I, _I, _P, _P, _P, _P, _P]),
+            "oracle_leapfrog": (None, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P]),
+            "oracle_sim_create": (_P, [_P, _P, _P, _I, _I]),
+            "oracle_sim_destroy": (None, [_P]),
+            "oracle_sim_set_params": (None, [_P, _P]),
+            "oracle_sim_upload": (_I, [_P, _P, _P, _P, _I]),
+            "oracle_sim_update": (None, [_P]),
+            "oracle_sim_integrate": (None, [_P, _F]),
+            "oracle_sim_step": (None, [_P, _F, _I]),
+            "oracle_sim_num": (_I, [_P]),
+            "oracle_sim_last_nc": (_I, [_P]),
+            "oracle_sim_get": (_I, [_P, _I, _P, _I]),
+            "oracle_sim_deleted": (_I, [_P, _P, _P, _I]),
+        }
+        for k, (r, a) in sig.items():
+            f = getattr(lib, k)
+            f.restype = r
+            f.argtypes = a
+        _oracle = lib
+    return _oracle
+
+
+def ref_available():
+    return os.path.exists(REF_LIB)
+
+
+def ref():
+    """The reference's kernels (built only where the reference tree exists)."""
+    global _ref
+    if _ref is None:
+        lib = C.CDLL(REF_LIB)
+        sig = {
+            "ref_hash": (None, [_I, _P, _P, _P, _P]),
+            "ref_bitonic_sort": (None, [_I, _P, _P]),
+            "ref_cellindices": (_I, [_I, _P, _P, _P, _P, _P]),
+            "ref_permute": (None, [_I, _P, _P, _P, _P, _P, _P, _P]),
+            "ref_density": (None, [_I, _P, _P, _P, _P, _P, _P]),
+            "ref_force": (None, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+            "ref_collision_wall": (None, [_I, _P, _P, _P, _P, _P]),
+            "ref_leapfrog": (None, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _F]),
+            "ref_setup_domain": (None, [_P, _P, _F, _F, _P, _P]),
+        }
+        for k, (r, a) in sig.items():
+            f = getattr(lib, k)
+            f.restype = r
+            f.argtypes = a
+        _ref = lib
+    return _ref
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+FIELD_IDS = {"pos_u": 0, "vel_u": 1, "veleval_u": 2, "pos_s": 3, "vel_s": 4, "veleval_s": 5, "density_s": 6,
+             "force_s": 7, "xsph_s": 8, "sort_hashes": 9, "sort_indices": 10, "cell_start": 11, "cell_end": 12,
+             "neighbor_count": 13}
+
+
+class OracleSim:
+    """The oracle's whole-system stepper (SPH::updateGPU + collision + integrate)."""
+
+    def __init__(self, sphp, grid, grid_scaled, max_num, f64=False):
+        self.lib = oracle()
+        self.h = self.lib.oracle_sim_create(C.addressof(sphp), C.addressof(grid), C.addressof(grid_scaled),
+                                            int(max_num), 1 if f64 else 0)
+        self.nb_cells = grid.nb_cells
+
+    def close(self):
+        if self.h:
+            self.lib.oracle_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_params(self, sphp):
+        self.lib.oracle_sim_set_params(self.h, C.addressof(sphp))
+
+    def upload(self, pos, vel, veleval=None):
+        pos = np.ascontiguousarray(pos, np.float32)
+        vel = np.ascontiguousarray(vel, np.float32)
+        ve = None if veleval is None else np.ascontiguousarray(veleval, np.float32)
+        assert self.lib.oracle_sim_upload(self.h, ptr(pos), ptr(vel), ptr(ve), pos.shape[0]) == 0
+
+    def update(self):
+        self.lib.oracle_sim_update(self.h)
+
+    def integrate(self, dt):
+        self.lib.oracle_sim_integrate(self.h, dt)
+
+    def step(self, dt, n=1):
+        self.lib.oracle_sim_step(self.h, dt, n)
+
+    @property
+    def num(self):
+        return self.lib.oracle_sim_num(self.h)
+
+    def get(self, field, n=None):
+        if n is None:
+            n = self.nb_cells + 1 if field in ("cell_start", "cell_end") else self.num
+        if field in ("density_s",):
+            out = np.empty(n, np.float32)
+        elif field in ("sort_hashes", "sort_indices", "cell_start", "cell_end", "neighbor_count"):
+            out = np.empty(n, np.uint32)
+        else:
+            out = np.empty((n, 4), np.float32)
+        assert self.lib.oracle_sim_get(self.h, FIELD_IDS[field], ptr(out), n) == 0
+        return out

@@ -1,0 +1,106 @@
+"""The CPU oracle against the golden fixtures made from the reference's own
+kernels (tests/golden/make_golden.py): every stage and every rollout must be
+bit-identical (within-cell order canonicalised by original index)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import golden_io
+import oracle_bind as ob
+
+P = ob.ptr
+
+
+def run_stages(d, sp, g, gs):
+    O = ob.oracle()
+    n = d["in_pos"].shape[0]
+    pos, vel = d["in_pos"], d["in_vel"]
+    keys = np.empty(n, np.uint32)
+    idx = np.empty(n, np.uint32)
+    O.oracle_hash(n, P(pos), C.addressof(g), P(keys), P(idx))
+    out = {"hash_keys": keys.copy()}
+    O.oracle_sort(n, P(keys), P(idx))
+    out["sort_hashes"], out["sort_indices"] = keys, idx
+    start = np.full(g.nb_cells + 1, 666, np.uint32)
+    end = np.full(g.nb_cells + 1, 666, np.uint32)
+    out["nc"] = O.oracle_cellindices(n, P(keys), P(start), P(end), g.nb_cells)
+    out["cell_start"], out["cell_end"] = start, end
+    ve = np.zeros_like(pos)
+    ps, vs, ves = np.empty_like(pos), np.empty_like(pos), np.empty_like(pos)
+    O.oracle_permute(n, P(idx), P(pos), P(vel), P(ve), P(ps), P(vs), P(ves))
+    out.update(pos_s=ps, vel_s=vs, veleval_s=ves)
+    dens = np.empty(n, np.float32)
+    O.oracle_density(0, n, P(ps), P(start), P(end), C.addressof(gs), C.addressof(sp), P(dens), None)
+    out["density_s"] = dens
+    f, x = np.empty_like(pos), np.empty_like(pos)
+    O.oracle_force(0, n, P(ps), P(dens), P(ves), P(start), P(end), C.addressof(gs), C.addressof(sp), P(f), P(x))
+    out["force_pre"], out["xsph_s"] = f.copy(), x
+    O.oracle_collision(0, n, P(ps), P(vs), P(f), C.addressof(gs), C.addressof(sp))
+    out["force_s"] = f
+    pu, vu, eu = pos.copy(), vel.copy(), ve.copy()
+    O.oracle_leapfrog(0, n, P(ps), P(vs), P(f), P(x), P(idx), C.addressof(sp), float(d["dt"]), P(pu), P(vu), P(eu))
+    out.update(pos_u=pu, vel_u=vu, veleval_u=eu)
+    return out
+
+
+@pytest.mark.parametrize("name", ["stages_n4096.npz", "ragged_n1000.npz"])
+def test_oracle_stages_match_reference_golden(name):
+    d, sp, g, gs = golden_io.load(name)
+    o = run_stages(d, sp, g, gs)
+    for k in ("hash_keys", "sort_hashes", "sort_indices", "cell_start", "cell_end", "pos_s", "vel_s", "veleval_s",
+              "density_s", "force_pre", "force_s", "xsph_s", "pos_u", "vel_u", "veleval_u"):
+        np.testing.assert_array_equal(o[k], d["s1_" + k], err_msg=k)
+    assert o["nc"] == int(d["s1_nc"])
+
+
+@pytest.mark.parametrize("name,steps", [("stages_n4096.npz", (1, 2, 10)), ("ragged_n1000.npz", (1, 3))])
+def test_oracle_rollout_matches_reference_golden(name, steps):
+    d, sp, g, gs = golden_io.load(name)
+    n = d["in_pos"].shape[0]
+    sim = ob.OracleSim(sp, g, gs, n)
+    sim.upload(d["in_pos"], d["in_vel"])
+    done = 0
+    for k in steps:
+        sim.step(float(d["dt"]), k - done)
+        done = k
+        for f in ("pos_u", "vel_u", "veleval_u"):
+            np.testing.assert_array_equal(sim.get(f), d["s%d_%s" % (k, f)], err_msg="step %d %s" % (k, f))
+
+
+def test_oracle_out_of_grid_deletion_matches_reference_golden():
+    d, sp, g, gs = golden_io.load("outofgrid_n512.npz")
+    n = d["in_pos"].shape[0]
+    sim = ob.OracleSim(sp, g, gs, n)
+    sim.upload(d["in_pos"], d["in_vel"])
+    sim.update()
+    nc = int(d["s1_nc"])
+    assert 0 <= nc < n and sim.num == nc
+    assert sim.lib.oracle_sim_last_nc(sim.h) == nc
+    dp = np.empty((n - nc, 4), np.float32)
+    dv = np.empty((n - nc, 4), np.float32)
+    assert sim.lib.oracle_sim_deleted(sim.h, P(dp), P(dv), n - nc) == n - nc
+    np.testing.assert_array_equal(dp, d["s1_deleted_pos"])
+    np.testing.assert_array_equal(dv, d["s1_deleted_vel"])
+    np.testing.assert_array_equal(sim.get("sort_indices"), d["s1_sort_indices"])
+    np.testing.assert_array_equal(sim.get("density_s"), d["s1_density_s"])
+    sim.integrate(float(d["dt"]))
+    for f in ("pos_u", "vel_u", "veleval_u"):
+        np.testing.assert_array_equal(sim.get(f), d["s1_" + f])
+    sim.step(float(d["dt"]), 1)
+    for f in ("pos_u", "vel_u", "veleval_u"):
+        np.testing.assert_array_equal(sim.get(f), d["s2_" + f])
+
+
+@pytest.mark.slow
+def test_oracle_cfg0_rollout_matches_reference_golden():
+    d, sp, g, gs = golden_io.load("cfg0_n16384.npz")
+    n = d["in_pos"].shape[0]
+    sim = ob.OracleSim(sp, g, gs, n)
+    sim.upload(d["in_pos"], d["in_vel"])
+    done = 0
+    for k in (1, 10, 100):
+        sim.step(float(d["dt"]), k - done)
+        done = k
+        np.testing.assert_array_equal(sim.get("pos_u"), d["s%d_pos_u" % k])
+        np.testing.assert_array_equal(sim.get("vel_u"), d["s%d_vel_u" % k])
