@@ -29,7 +29,12 @@ struct sph_ctx {
     float4 *pos_s = nullptr, *vel_s = nullptr, *veleval_s = nullptr, *force_s = nullptr, *xsph_s = nullptr;
     float4 *del_pos = nullptr, *del_vel = nullptr;
     float* density = nullptr;
+    float4* rec_pd = nullptr;    // (scaled pos, rho) per sorted particle
+    float4* rec_vi = nullptr;    // (veleval, 1/rho) per sorted particle
+    int* fctr = nullptr;         // force tile counters [nsm + 1]
+    int nsm = 1;
     uint32_t* nbr = nullptr;
+    uint32_t* mask = nullptr;    // neighbour bitmask [kMaskWords][max_num]
     uint32_t *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
     uint32_t *keys_cur = nullptr, *idx_cur = nullptr;  // what SORT_HASHES / SORT_INDICES show
     uint32_t *cell_start = nullptr, *cell_end = nullptr;
@@ -214,7 +219,7 @@ int field_capacity(sph_ctx* c, int field) {
 void free_all(sph_ctx* c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
-                    c->del_pos, c->del_vel, c->density, c->nbr, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
+                    c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->fctr, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
                     c->cell_start, c->cell_end, c->info, c->scratch};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -260,6 +265,20 @@ int enqueue_sort(sph_ctx* c) {
     return SPH_OK;
 }
 
+// Density over the sorted arrays; with_deletion: also the fused step's
+// out-of-grid bookkeeping.
+void density_launch(sph_ctx* c, const uint32_t* idx, bool with_deletion, cudaStream_t st) {
+    sphk::launch_density(c->pos_s, c->veleval_s, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask,
+                         (size_t)c->max_num, c->cell_start, c->cell_end, c->info, idx, c->vel_u,
+                         with_deletion ? c->vel_s : nullptr, c->del_pos, c->del_vel, c->P, c->num_hint, st);
+}
+
+void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {
+    sphk::launch_force(c->pos_s, c->rec_pd, c->rec_vi, c->mask, (size_t)c->max_num, c->cell_start, c->cell_end,
+                       c->info, c->fctr, c->nsm, c->force_s, c->xsph_s, idx, c->vel_s, c->pos_u, c->vel_u,
+                       c->veleval_u, c->P, dt, fused ? 1 : 0, c->exact, c->num_hint, st);
+}
+
 int enqueue_fused_step(sph_ctx* c, float dt) {
     int rc = enqueue_hash(c);
     if (rc) return rc;
@@ -267,11 +286,8 @@ int enqueue_fused_step(sph_ctx* c, float dt) {
     if (rc) return rc;
     sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
                                c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 1, c->stream);
-    sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_a, c->vel_u,
-                         c->vel_s, c->del_pos, c->del_vel, c->P, c->num_hint, c->stream);
-    sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
-                       c->xsph_s, c->idx_a, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, dt, 1,
-                       c->exact, c->num_hint, c->stream);
+    density_launch(c, c->idx_a, true, c->stream);
+    force_launch(c, c->idx_a, true, dt, c->stream);
     CK_LAUNCH(c);
     return SPH_OK;
 }
@@ -350,6 +366,9 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
         delete c;
         return set_err(nullptr, SPH_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     }
+    int nsm = 1;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
+    c->nsm = nsm > 1000 ? 1000 : nsm;
     const int total_bits = bit_width((uint32_t)c->gp.nb_cells);
     c->passes = (total_bits + 7) / 8;
     if (c->passes < 1) c->passes = 1;
@@ -378,6 +397,10 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->del_vel, N * 16);
     ALLOC(c->density, N * 4);
     ALLOC(c->nbr, N * 4);
+    ALLOC(c->rec_pd, N * 16);
+    ALLOC(c->rec_vi, N * 16);
+    ALLOC(c->fctr, sizeof(int) * 1024);
+    ALLOC(c->mask, N * 4 * sphk::kMaskWords);
     ALLOC(c->keys_a, N * 4);
     ALLOC(c->idx_a, N * 4);
     ALLOC(c->keys_b, N * 4);
@@ -411,6 +434,10 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     for (const void* p : zero_f4) cudaMemsetAsync((void*)p, 0, N * 16, st);
     cudaMemsetAsync(c->density, 0, N * 4, st);
     cudaMemsetAsync(c->nbr, 0, N * 4, st);
+    cudaMemsetAsync(c->rec_pd, 0, N * 16, st);
+    cudaMemsetAsync(c->rec_vi, 0, N * 16, st);
+    cudaMemsetAsync(c->fctr, 0, sizeof(int) * 1024, st);
+    cudaMemsetAsync(c->mask, 0, N * 4 * sphk::kMaskWords, st);
     fill_u32(c->keys_a, N, 0x7fffffffu, st);
     fill_u32(c->idx_a, N, 0x7fffffffu, st);
     fill_u32(c->keys_b, N, 0x7fffffffu, st);
@@ -617,8 +644,7 @@ int sph_stage_permute(sph_ctx* c) {
 int sph_stage_density(sph_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
-    sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_cur, c->vel_u,
-                         nullptr, nullptr, nullptr, c->P, c->num_hint, c->stream);
+    density_launch(c, c->idx_cur, false, c->stream);
     CK_LAUNCH(c);
     return SPH_OK;
 }
@@ -626,9 +652,7 @@ int sph_stage_density(sph_ctx* c) {
 int sph_stage_force(sph_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
-    sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
-                       c->xsph_s, c->idx_cur, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, 0.f, 0,
-                       c->exact, c->num_hint, c->stream);
+    force_launch(c, c->idx_cur, false, 0.f, c->stream);
     CK_LAUNCH(c);
     return SPH_OK;
 }
@@ -660,11 +684,8 @@ int sph_update(sph_ctx* c) {
                                c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 2, c->stream);
     sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
                                c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
-    sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_a, c->vel_u,
-                         nullptr, nullptr, nullptr, c->P, c->num_hint, c->stream);
-    sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
-                       c->xsph_s, c->idx_a, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, 0.f, 0,
-                       c->exact, c->num_hint, c->stream);
+    density_launch(c, c->idx_a, false, c->stream);
+    force_launch(c, c->idx_a, false, 0.f, c->stream);
     sphk::launch_collision(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
     CK_LAUNCH(c);
     return SPH_OK;
@@ -739,6 +760,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_hash(c->pos_u, hash_keys(c), hash_idx(c), c->cell_start, c->hist, c->info, c->P, c->num_hint,
                           c->passes, 1, st);
+        CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_sort_reset(c->status, (size_t)c->passes * c->tiles_cap * 256, c->info + sphk::kSortTiles, st);
         CK(c, cudaEventRecord(ev[e++], st));
         uint32_t *kin = hash_keys(c), *vin = hash_idx(c);
@@ -757,12 +779,9 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
                                    c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 1, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_density(c->pos_s, c->density, c->nbr, c->cell_start, c->cell_end, c->info, c->idx_a, c->vel_u,
-                             c->vel_s, c->del_pos, c->del_vel, c->P, c->num_hint, st);
+        density_launch(c, c->idx_a, true, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_force(c->pos_s, c->density, c->veleval_s, c->cell_start, c->cell_end, c->info, c->force_s,
-                           c->xsph_s, c->idx_a, c->vel_u, c->vel_s, c->pos_u, c->vel_u, c->veleval_u, c->P, dt, 1,
-                           c->exact, c->num_hint, st);
+        force_launch(c, c->idx_a, true, dt, st);
         CK(c, cudaEventRecord(ev[e++], st));
         CK_LAUNCH(c);
         CK(c, cudaEventSynchronize(ev[nk]));

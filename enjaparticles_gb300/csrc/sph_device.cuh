@@ -32,6 +32,12 @@ enum InfoSlot : int {
 };
 constexpr int kErrLookbackTimeout = 1;
 
+// Neighbour bitmask written by the density pass: bit b of particle i says
+// whether its b-th candidate (in walk order) is a neighbour other than itself;
+// word w of particle i lives at mask[w * stride + i].
+constexpr int kMaskWords = 16;
+constexpr int kMaskBits = 32 * kMaskWords;
+
 // Parameters every kernel of the step needs, passed by value.
 struct StepParams {
     // SPHParams (floats copied once on the host)
@@ -95,14 +101,17 @@ void launch_cells_permute(const uint32_t* keys, const uint32_t* idx, uint32_t* c
                           const float4* pos_u, const float4* vel_u, const float4* veleval_u, float4* pos_s,
                           float4* vel_s, float4* veleval_s, int* info, int nb_cells, int grid_items, int gather,
                           cudaStream_t st);
-void launch_density(const float4* pos_s, float* density, uint32_t* nbr, const uint32_t* cell_start,
+void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
+                    uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
                     float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
                     cudaStream_t st);
-void launch_force(const float4* pos_s, const float* density, const float4* veleval_s, const uint32_t* cell_start,
-                  const uint32_t* cell_end, const int* info, float4* force_s, float4* xsph_s, uint32_t* idx,
-                  const float4* vel_u_in, const float4* vel_s, float4* pos_u, float4* vel_u, float4* veleval_u,
-                  const StepParams& p, float dt, int fused, int exact, int grid_items, cudaStream_t st);
+// tile_ctr: nsm + 1 ints, zero before the first launch; the kernel leaves them zero.
+void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                  size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                  int* tile_ctr, int nsm, float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s,
+                  float4* pos_u, float4* vel_u, float4* veleval_u, const StepParams& p, float dt, int fused,
+                  int exact, int grid_items, cudaStream_t st);
 void launch_collision(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info,
                       const StepParams& p, int grid_items, cudaStream_t st);
 void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,

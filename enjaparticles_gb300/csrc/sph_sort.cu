@@ -61,7 +61,8 @@ void launch_sort_reset(uint32_t* status, size_t words, int* tile_counters, cudaS
 }
 
 // ---------------------------------------------------------------------------
-// Hash.  One thread per particle of original order.
+// Hash.  Grid-stride over particles in original order (a few blocks per SM),
+// so that the per-block digit histograms reach global memory with few atomics.
 template <int PASSES>
 __global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos_u, uint32_t* __restrict__ keys,
                                               uint32_t* __restrict__ idx, uint32_t* __restrict__ cell_start,
@@ -71,34 +72,37 @@ __global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos_u, 
     const int n = info[kNum];
     const int tid = threadIdx.x;
     for (int k = tid; k < PASSES * kRadixSize; k += blockDim.x) (&s_hist[0][0])[k] = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
     // Fused cell_start clear (CellIndices.cpp:58-62).
     if (clear_cells) {
-        const size_t stride = (size_t)gridDim.x * blockDim.x;
         for (size_t k = (size_t)blockIdx.x * blockDim.x + tid; k <= (size_t)p.nb_cells; k += stride)
             cell_start[k] = kEmpty;
     }
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + tid;
-    const bool valid = i < n;
-    uint32_t key = 0;
-    if (valid) {
-        const float4 q = ldg4(pos_u + i);
-        const int3 c = grid_cell(q.x, q.y, q.z, p.g_min, p.g_delta);
-        int h = grid_hash_f(c.x, c.y, c.z, p.g_res);
-        h = h > p.nb_cells ? p.nb_cells : h;
-        h = h < 0 ? p.nb_cells : h;
-        key = (uint32_t)h;
-        keys[i] = key;
-        idx[i] = (uint32_t)i;
-    }
-    // Digit histograms, aggregated per warp with match_any.
     const unsigned lane = tid & 31;
+    // The loop bound is uniform per warp (base is the warp's first index), so
+    // match_any always sees the full warp.
+    for (size_t base = (size_t)blockIdx.x * blockDim.x + (tid & ~31); base < (size_t)n; base += stride) {
+        const size_t i = base + lane;
+        const bool valid = i < (size_t)n;
+        uint32_t key = 0;
+        if (valid) {
+            const float4 q = ldg4(pos_u + i);
+            const int3 c = grid_cell(q.x, q.y, q.z, p.g_min, p.g_delta);
+            int h = grid_hash_f(c.x, c.y, c.z, p.g_res);
+            h = h > p.nb_cells ? p.nb_cells : h;
+            h = h < 0 ? p.nb_cells : h;
+            key = (uint32_t)h;
+            keys[i] = key;
+            idx[i] = (uint32_t)i;
+        }
 #pragma unroll
-    for (int ps = 0; ps < PASSES; ++ps) {
-        const uint32_t d = valid ? ((key >> (ps * kRadixBits)) & (kRadixSize - 1)) : 0x100u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const int leader = 31 - __clz(peers);
-        if (valid && (int)lane == leader) atomicAdd(&s_hist[ps][d], (uint32_t)__popc(peers));
+        for (int ps = 0; ps < PASSES; ++ps) {
+            const uint32_t d = valid ? ((key >> (ps * kRadixBits)) & (kRadixSize - 1)) : 0x100u;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const int leader = 31 - __clz(peers);
+            if (valid && (int)lane == leader) atomicAdd(&s_hist[ps][d], (uint32_t)__popc(peers));
+        }
     }
     __syncthreads();
     for (int k = tid; k < PASSES * kRadixSize; k += blockDim.x) {
@@ -110,9 +114,10 @@ __global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos_u, 
 void launch_hash(const float4* pos_u, uint32_t* keys, uint32_t* idx, uint32_t* cell_start, uint32_t* hist,
                  const int* info, const StepParams& p, int grid_items, int passes, int clear_cells,
                  cudaStream_t st) {
-    int threads = 256;
+    const int threads = 256;
     int blocks = (grid_items + threads - 1) / threads;
-    if (blocks < 1) blocks = 1;
+    const int cap = 152 * 8;  // a few resident blocks per SM
+    blocks = blocks < 1 ? 1 : (blocks > cap ? cap : blocks);
     switch (passes) {
         case 0: k_hash<0><<<blocks, threads, 0, st>>>(pos_u, keys, idx, cell_start, hist, info, p, clear_cells); break;
         case 1: k_hash<1><<<blocks, threads, 0, st>>>(pos_u, keys, idx, cell_start, hist, info, p, clear_cells); break;
