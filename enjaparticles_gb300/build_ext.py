@@ -15,7 +15,11 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librtps_sph.so")
 
-SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cells.cu", "sph_neighbors.cu", "sph_integrate.cu", "sph_params.cpp"]
+SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cells.cu", "sph_density.cu", "sph_force.cu", "sph_integrate.cu",
+           "sph_params.cpp"]
+# Per-file flags: the density pass relies on every multiply and add being
+# rounded on its own.
+EXTRA = {"sph_density.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -32,7 +36,7 @@ def _compile(src, ptxas_verbose):
     cmd = [nvcc(), "-c", path, "-o", obj, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-fno-fast-math", "-I", os.path.join(PKG, "..", "include")]
     if src.endswith(".cu"):
-        cmd += ARCH + ["--expt-relaxed-constexpr"]
+        cmd += ARCH + ["--expt-relaxed-constexpr"] + EXTRA.get(src, [])
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]
     else:

@@ -268,7 +268,9 @@ int enqueue_sort(sph_ctx* c) {
 // Density over the sorted arrays; with_deletion: also the fused step's
 // out-of-grid bookkeeping.
 void density_launch(sph_ctx* c, const uint32_t* idx, bool with_deletion, cudaStream_t st) {
-    sphk::launch_density(c->pos_s, c->veleval_s, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask,
+    // the fused step (with_deletion) skips the neighbour counts
+    sphk::launch_density(c->pos_s, c->veleval_s, c->density, c->rec_pd, c->rec_vi, with_deletion ? nullptr : c->nbr,
+                         c->mask,
                          (size_t)c->max_num, c->cell_start, c->cell_end, c->info, idx, c->vel_u,
                          with_deletion ? c->vel_s : nullptr, c->del_pos, c->del_vel, c->P, c->num_hint, st);
 }

@@ -1,0 +1,120 @@
+// sph_density.cu — density pass (rtpslib/system/sph/cl_src/density.cl:44-126,
+// poly6 cl_sph_kernels.h:29-45).
+//
+// Density keeps the reference's summation order and rounding: it equals the
+// FP32 oracle bit for bit.  Every multiply and add is a separately rounded
+// scalar operation.  (Packed two-lane FP32 arithmetic was tried and rejected:
+// with this compiler a packed multiply followed by a packed add does not give
+// the separately rounded result, even with contraction disabled, which would
+// change |r|^2 and with it the neighbour sets.)
+//
+// nbr (neighbour counts) is optional: the fused step leaves it out.
+//
+// While it tests the candidates the pass also records, per particle, which of
+// its first kMaskBits candidates (in walk order) are neighbours (self
+// excluded) as a bitmask, and the 32-byte record (position, rho),
+// (veleval, 1/rho) the force pass reads for every neighbour.
+#include "sph_walk.cuh"
+
+namespace sphk {
+
+// When called from the fused step the kernel also does the out-of-grid
+// deletion bookkeeping (vel_s != nullptr).
+template <bool Unit, bool WantCount>
+__global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ veleval_s,
+                                                 float* __restrict__ density, float4* __restrict__ rec_pd,
+                                                 float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
+                                                 uint32_t* __restrict__ mask, const size_t mstride,
+                                                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                                                 int* __restrict__ info, const uint32_t* __restrict__ idx,
+                                                 const float4* __restrict__ vel_u, float4* __restrict__ vel_s,
+                                                 float4* __restrict__ del_pos, float4* __restrict__ del_vel,
+                                                 const StepParams P) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vel_s != nullptr && out >= 0 && i < n_old) {
+        // SPH.cpp:220-250: the kept particles' velocities in sorted order
+        // (call_prep copies vel_s to vel_u), the removed ones saved.
+        const float4 v = __ldg(vel_u + __ldg(idx + i));
+        if (i < n) {
+            vel_s[i] = v;
+        } else {
+            del_pos[i - n] = __ldg(pos_s + i);
+            del_vel[i - n] = v;
+            if (i == n) info[kDeleted] = n_old - n;
+        }
+    }
+    if (i >= n) return;
+    float4 pi = __ldg(pos_s + i);
+    if (!Unit) pi = v4scale(pi, P.sc);
+    const float rc2 = P.rcut2, h2 = P.h2;
+    float acc = 0.f;
+    uint32_t cnt = 0;
+    // bitmask: `cur` collects the bits of word p >> 5, p the walk position;
+    // candidates are taken in chunks that end at a word boundary
+    uint32_t cur = 0, p = 0;
+    uint32_t* mrow = mask + i;
+    auto run = [&](uint32_t rs, uint32_t re) {
+        uint32_t j = rs;
+        while (j < re) {
+            const uint32_t b0 = p & 31u;
+            uint32_t k = 32u - b0;
+            if (k > re - j) k = re - j;
+            const uint32_t jend = j + k;
+            uint32_t bit = 1u << b0;
+#pragma unroll 2
+            for (; j < jend; ++j, bit <<= 1) {
+                float4 q = __ldg(pos_s + j);
+                if (!Unit) q = v4scale(q, P.sc);
+                const float r2 = dist2_exact(__fsub_rn(pi.x, q.x), __fsub_rn(pi.y, q.y), __fsub_rn(pi.z, q.z));
+                if (r2 <= rc2) {
+                    const float hr2 = __fsub_rn(h2, r2);
+                    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(hr2, hr2), hr2));
+                    if (WantCount) ++cnt;
+                    if (j != (uint32_t)i) cur |= bit;
+                }
+            }
+            p += k;
+            if ((p & 31u) == 0) {
+                const uint32_t w = (p >> 5) - 1;
+                if (w < (uint32_t)kMaskWords) mrow[(size_t)w * mstride] = cur;
+                cur = 0;
+            }
+        }
+    };
+    const int3 c = grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
+    if (cell_fast(P, c))
+        walk_rows_fast(P, cs, ce, c, run);
+    else
+        walk_rows_slow(P, cs, ce, c, run);
+    if ((p & 31u) != 0 && (p >> 5) < (uint32_t)kMaskWords) mrow[(size_t)(p >> 5) * mstride] = cur;
+    const float rho = __fmul_rn(P.dens_coef, acc);
+    density[i] = rho;
+    const float4 ve = __ldg(veleval_s + i);
+    rec_pd[i] = make_float4(pi.x, pi.y, pi.z, rho);
+    rec_vi[i] = make_float4(ve.x, ve.y, ve.z, __frcp_rn(rho));
+    if (WantCount) nbr[i] = cnt;
+}
+
+void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
+                    uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
+                    const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
+                    float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
+                    cudaStream_t st) {
+    const int threads = 256;
+    int blocks = (grid_items + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+#define SPH_DENSITY_LAUNCH(U, W)                                                                              \
+    k_density<U, W><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, \
+                                                cell_start, cell_end, (int*)info, idx, vel_u, vel_s, del_pos,      \
+                                                del_vel, p)
+    if (p.unit_scale) {
+        if (nbr) SPH_DENSITY_LAUNCH(true, true); else SPH_DENSITY_LAUNCH(true, false);
+    } else {
+        if (nbr) SPH_DENSITY_LAUNCH(false, true); else SPH_DENSITY_LAUNCH(false, false);
+    }
+#undef SPH_DENSITY_LAUNCH
+}
+
+}  // namespace sphk

@@ -87,6 +87,8 @@ __device__ __forceinline__ float dist2_exact(float dx, float dy, float dz) {
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
+
+
 // Launch helpers implemented in the .cu files.
 void launch_prologue(uint32_t* hist, int* info, cudaStream_t st);
 void launch_sort_reset(uint32_t* status, size_t words, int* tile_counters, cudaStream_t st);

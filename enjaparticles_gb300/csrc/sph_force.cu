@@ -1,188 +1,11 @@
-// sph_neighbors.cu — the two neighbour passes (density, force), with the wall
-// collision and leapfrog integration fused into the force pass.
-//
-//   density: rtpslib/system/sph/cl_src/density.cl:44-126 (poly6,
-//            cl_sph_kernels.h:29-45; neighbour walk cl_sph_neighbors.h:49-140)
-//   force:   rtpslib/system/sph/cl_src/force.cl:43-186 (spiky gradient
-//            cl_sph_kernels.h:81-97, viscosity Laplacian :118-127, XSPH)
-//
-// Neighbour walk.  The reference visits 27 cells (z, y, x in [c-1, c+1]) and
-// each cell's sorted range.  Keys of the three cells x-1, x, x+1 of one row
-// are consecutive integers, so their particles are one contiguous run of the
-// sorted arrays: the walk here is 9 row runs, visited in the reference's
-// order.  Integer row hashing equals the reference's float hash formula
-// whenever every intermediate value is an integer below 2^24 in magnitude
-// (checked on the host: int_hash_ok); otherwise each of the 27 cells is hashed
-// with the float formula.
-//
-// Cutoff.  |r| <= h with |r| = sqrtf(r2) is the same test as r2 <= rcut2,
-// rcut2 being the largest float whose correctly rounded square root is <= h
-// (sqrt is monotonic); r2 is formed without contraction, so neighbour sets are
-// identical to the oracle's.
-//
-// Density keeps the reference's summation order and rounding: it equals the
-// FP32 oracle bit for bit.  While it tests the candidates it also records,
-// per particle, which of its first kMaskBits candidates (in walk order) are
-// neighbours (self excluded) as a bitmask, and (rho, 1/rho, K(rho-rho0)).
-// Force does not test those candidates again: it decodes the bitmask into a
-// per-thread list in shared memory (candidates past kMaskBits are tested
-// directly) and runs the heavy arithmetic over the list with all lanes busy;
-// the list keeps the walk order.
-// Exact=true evaluates force with the oracle's exact operations (IEEE
-// divisions, no contraction: bitwise equal); Exact=false uses FMA and
-// reciprocals (within the FP32 tolerance of the tests).
-#include <climits>
-
-#include "sph_physics.cuh"
+// sph_force.cu — force pass (rtpslib/system/sph/cl_src/force.cl:43-186:
+// spiky gradient cl_sph_kernels.h:81-97, viscosity Laplacian :118-127,
+// XSPH), with the wall collision and leapfrog integration of the step fused in.
+// Compiled with FMA contraction allowed: the default (fast) arithmetic uses
+// it; the exact variant spells every operation with a rounding intrinsic.
+#include "sph_walk.cuh"
 
 namespace sphk {
-
-// Integer row hashing applies: every intermediate of the float hash formula is
-// an integer below 2^24 for cells within one cell of the grid.
-__device__ __forceinline__ bool cell_fast(const StepParams& P, const int3& c) {
-    return P.int_hash_ok && c.x >= -1 && c.x <= P.res_x && c.y >= -1 && c.y <= P.res_y && c.z >= -1 &&
-           c.z <= P.res_z;
-}
-
-// The 9 row runs of cell c (at most 9 calls of f(rs, re), in walk order).
-template <class F>
-__device__ __forceinline__ void walk_rows_fast(const StepParams& P, const uint32_t* __restrict__ cs,
-                                               const uint32_t* __restrict__ ce, const int3& c, F&& f) {
-    const uint32_t C = (uint32_t)P.nb_cells;
-#pragma unroll 1
-    for (int dz = -1; dz <= 1; ++dz) {
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int base = ((c.z + dz) * P.res_y + (c.y + dy)) * P.res_x + c.x;
-            uint32_t rs = kEmpty, last = 0;
-#pragma unroll
-            for (int dx = -1; dx <= 1; ++dx) {
-                const uint32_t h = (uint32_t)(base + dx);
-                if (h < C) {
-                    const uint32_t s = __ldg(cs + h);
-                    if (s != kEmpty) {
-                        if (rs == kEmpty) rs = s;
-                        last = h;
-                    }
-                }
-            }
-            if (rs != kEmpty) f(rs, __ldg(ce + last));
-        }
-    }
-}
-
-// The 27 cells one by one with the reference's float hash (up to 27 calls).
-template <class F>
-__device__ __forceinline__ void walk_rows_slow(const StepParams& P, const uint32_t* __restrict__ cs,
-                                               const uint32_t* __restrict__ ce, const int3& c, F&& f) {
-    const uint32_t C = (uint32_t)P.nb_cells;
-#pragma unroll 1
-    for (int z = c.z - 1; z <= c.z + 1; ++z)
-#pragma unroll 1
-        for (int y = c.y - 1; y <= c.y + 1; ++y)
-#pragma unroll 1
-            for (int x = c.x - 1; x <= c.x + 1; ++x) {
-                const uint32_t h = (uint32_t)grid_hash_f(x, y, z, P.gs_res);
-                if (h >= C) continue;
-                const uint32_t s = __ldg(cs + h);
-                if (s != kEmpty) f(s, __ldg(ce + h));
-            }
-}
-
-// Visit the sorted-index runs of the 27 neighbour cells of scaled position
-// (px,py,pz), in the reference's order; f(rs, re) gets each non-empty run.
-template <class F>
-__device__ __forceinline__ void walk_rows(const StepParams& P, const uint32_t* __restrict__ cs,
-                                          const uint32_t* __restrict__ ce, float px, float py, float pz, F&& f) {
-    const int3 c = grid_cell(px, py, pz, P.gs_min, P.gs_delta);
-    if (cell_fast(P, c))
-        walk_rows_fast(P, cs, ce, c, f);
-    else
-        walk_rows_slow(P, cs, ce, c, f);
-}
-
-// ---------------------------------------------------------------------------
-// Density.  One thread per sorted particle.  When called from the fused step
-// it also does the out-of-grid deletion bookkeeping (vel_s != nullptr).
-template <bool Unit>
-__global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ veleval_s,
-                                                 float* __restrict__ density, float4* __restrict__ rec_pd,
-                                                 float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
-                                                 uint32_t* __restrict__ mask, const size_t mstride,
-                                                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-                                                 int* __restrict__ info, const uint32_t* __restrict__ idx,
-                                                 const float4* __restrict__ vel_u, float4* __restrict__ vel_s,
-                                                 float4* __restrict__ del_pos, float4* __restrict__ del_vel,
-                                                 const StepParams P) {
-    int n_old, out;
-    const int n = effective_num(info, n_old, out);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vel_s != nullptr && out >= 0 && i < n_old) {
-        // SPH.cpp:220-250: the kept particles' velocities in sorted order
-        // (call_prep copies vel_s to vel_u), the removed ones saved.
-        const float4 v = __ldg(vel_u + __ldg(idx + i));
-        if (i < n) {
-            vel_s[i] = v;
-        } else {
-            del_pos[i - n] = __ldg(pos_s + i);
-            del_vel[i - n] = v;
-            if (i == n) info[kDeleted] = n_old - n;
-        }
-    }
-    if (i >= n) return;
-    float4 pi = __ldg(pos_s + i);
-    if (!Unit) pi = v4scale(pi, P.sc);
-    const float rc2 = P.rcut2, h2 = P.h2;
-    float acc = 0.f;
-    uint32_t cnt = 0, cur = 0, bit = 1, word = 0;
-    uint32_t* mrow = mask + i;
-    walk_rows(P, cs, ce, pi.x, pi.y, pi.z, [&](uint32_t rs, uint32_t re) {
-        for (uint32_t j = rs; j < re; ++j) {
-            float4 pj = __ldg(pos_s + j);
-            if (!Unit) pj = v4scale(pj, P.sc);
-            const float r2 = dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
-            if (r2 <= rc2) {
-                const float hr2 = __fsub_rn(h2, r2);
-                acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(hr2, hr2), hr2));
-                ++cnt;
-                if (j != (uint32_t)i) cur |= bit;
-            }
-            bit <<= 1;
-            if (bit == 0) {
-                if (word < kMaskWords) mrow[word * mstride] = cur;
-                ++word;
-                cur = 0;
-                bit = 1;
-            }
-        }
-    });
-    if (bit != 1 && word < kMaskWords) mrow[word * mstride] = cur;
-    const float rho = __fmul_rn(P.dens_coef, acc);
-    density[i] = rho;
-    // Neighbour records for the force pass: 32 bytes per particle.
-    const float4 ve = __ldg(veleval_s + i);
-    rec_pd[i] = make_float4(pi.x, pi.y, pi.z, rho);
-    rec_vi[i] = make_float4(ve.x, ve.y, ve.z, __frcp_rn(rho));
-    if (nbr) nbr[i] = cnt;
-}
-
-void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
-                    uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
-                    const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
-                    float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
-                    cudaStream_t st) {
-    const int threads = 256;
-    int blocks = (grid_items + threads - 1) / threads;
-    if (blocks < 1) blocks = 1;
-    if (p.unit_scale)
-        k_density<true><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride,
-                                                    cell_start, cell_end, (int*)info, idx, vel_u, vel_s, del_pos,
-                                                    del_vel, p);
-    else
-        k_density<false><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask,
-                                                     mask_stride, cell_start, cell_end, (int*)info, idx, vel_u,
-                                                     vel_s, del_pos, del_vel, p);
-}
 
 // ---------------------------------------------------------------------------
 // Force (+ collision + leapfrog when Fused).

@@ -1,0 +1,89 @@
+// sph_walk.cuh — the neighbour walk shared by the density and force passes
+// (rtpslib/system/sph/cl_src/cl_sph_neighbors.h:49-140).
+//
+// The reference visits 27 cells (z, y, x in [c-1, c+1]) and each cell's
+// sorted range.  Keys of the three cells x-1, x, x+1 of one row are
+// consecutive integers, so their particles are one contiguous run of the
+// sorted arrays: the walk here is 9 row runs, visited in the reference's
+// order.  Integer row hashing equals the reference's float hash formula
+// whenever every intermediate value is an integer below 2^24 in magnitude
+// (checked on the host: int_hash_ok); otherwise each of the 27 cells is
+// hashed with the float formula.
+//
+// Cutoff.  |r| <= h with |r| = sqrtf(r2) is the same test as r2 <= rcut2,
+// rcut2 being the largest float whose correctly rounded square root is <= h
+// (sqrt is monotonic); r2 is formed without contraction, so neighbour sets
+// are identical to the oracle's.
+#pragma once
+
+#include <climits>
+
+#include "sph_physics.cuh"
+
+namespace sphk {
+
+// Integer row hashing applies: every intermediate of the float hash formula is
+// an integer below 2^24 for cells within one cell of the grid.
+__device__ __forceinline__ bool cell_fast(const StepParams& P, const int3& c) {
+    return P.int_hash_ok && c.x >= -1 && c.x <= P.res_x && c.y >= -1 && c.y <= P.res_y && c.z >= -1 &&
+           c.z <= P.res_z;
+}
+
+// The 9 row runs of cell c (at most 9 calls of f(rs, re), in walk order).
+template <class F>
+__device__ __forceinline__ void walk_rows_fast(const StepParams& P, const uint32_t* __restrict__ cs,
+                                               const uint32_t* __restrict__ ce, const int3& c, F&& f) {
+    const uint32_t C = (uint32_t)P.nb_cells;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; ++dz) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int base = ((c.z + dz) * P.res_y + (c.y + dy)) * P.res_x + c.x;
+            uint32_t rs = kEmpty, last = 0;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                const uint32_t h = (uint32_t)(base + dx);
+                if (h < C) {
+                    const uint32_t s = __ldg(cs + h);
+                    if (s != kEmpty) {
+                        if (rs == kEmpty) rs = s;
+                        last = h;
+                    }
+                }
+            }
+            if (rs != kEmpty) f(rs, __ldg(ce + last));
+        }
+    }
+}
+
+// The 27 cells one by one with the reference's float hash (up to 27 calls).
+template <class F>
+__device__ __forceinline__ void walk_rows_slow(const StepParams& P, const uint32_t* __restrict__ cs,
+                                               const uint32_t* __restrict__ ce, const int3& c, F&& f) {
+    const uint32_t C = (uint32_t)P.nb_cells;
+#pragma unroll 1
+    for (int z = c.z - 1; z <= c.z + 1; ++z)
+#pragma unroll 1
+        for (int y = c.y - 1; y <= c.y + 1; ++y)
+#pragma unroll 1
+            for (int x = c.x - 1; x <= c.x + 1; ++x) {
+                const uint32_t h = (uint32_t)grid_hash_f(x, y, z, P.gs_res);
+                if (h >= C) continue;
+                const uint32_t s = __ldg(cs + h);
+                if (s != kEmpty) f(s, __ldg(ce + h));
+            }
+}
+
+// Visit the sorted-index runs of the 27 neighbour cells of scaled position
+// (px,py,pz), in the reference's order; f(rs, re) gets each non-empty run.
+template <class F>
+__device__ __forceinline__ void walk_rows(const StepParams& P, const uint32_t* __restrict__ cs,
+                                          const uint32_t* __restrict__ ce, float px, float py, float pz, F&& f) {
+    const int3 c = grid_cell(px, py, pz, P.gs_min, P.gs_delta);
+    if (cell_fast(P, c))
+        walk_rows_fast(P, cs, ce, c, f);
+    else
+        walk_rows_slow(P, cs, ce, c, f);
+}
+
+}  // namespace sphk

@@ -133,7 +133,7 @@ enum sph_field {
     SPH_FIELD_SORT_INDICES = 10, /* uint32[max_num] */
     SPH_FIELD_CELL_START = 11,   /* uint32[nb_cells+1] */
     SPH_FIELD_CELL_END = 12,     /* uint32[nb_cells+1] */
-    SPH_FIELD_NEIGHBOR_COUNT = 13, /* uint32[max_num] neighbours within h, self included (density stage) */
+    SPH_FIELD_NEIGHBOR_COUNT = 13, /* uint32[max_num] neighbours within h, self included (staged density only) */
     SPH_FIELD_COUNT_ = 14
 };
 
