@@ -93,6 +93,7 @@ SIGNATURES = {
     "sph_profile_kernel_name": (C.c_char_p, [_P, _I]),
     "sph_sync": (_I, [_P]),
     "sph_last_error": (_I, [_P, C.c_char_p, _I]),
+    "sph_sort_pairs_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P]),
     "sph_build_info": (C.c_char_p, []),
 }
 

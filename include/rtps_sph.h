@@ -291,6 +291,28 @@ int sph_sync(sph_ctx* ctx);
  * sph_create when ctx is NULL) into buf. */
 int sph_last_error(sph_ctx* ctx, char* buf, int len);
 
+/* Sort n (key, value) pairs held in caller-owned device memory, without
+ * allocating any device memory.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: a host application that owns all
+ * device memory through its own pool, a real-time frame loop that cannot take
+ * the synchronisation an allocation may bring, or code that has no access to
+ * the allocator.  Same stable LSD radix sort as sph_stage_sort: ascending keys
+ * (the low key_bits bits of each key are the sort key; keys must fit in them),
+ * equal keys keep their input order.  keys_in/vals_in are read only;
+ * keys_out/vals_out must be distinct from them.  stream is a cudaStream_t
+ * (NULL: the legacy default stream).
+ *
+ * Limit: n <= 1,048,576 (SPH_EINVAL above).  All scratch memory lives in one
+ * statically sized device array of the library (about 9 MiB, held by every
+ * GPU that loads the library until the process exits).  The first call on a
+ * device looks up that array's device address; make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race and corrupt each other.  Blocking: returns
+ * when the sort has finished. */
+int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                           uint32_t* vals_out, int n, int key_bits, void* stream);
+
 /* Library identification string (build flags, arch). */
 const char* sph_build_info(void);
 
