@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-n", type=int, default=131072, help="particles per step of the reference (CPU) arm")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--serial-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -195,6 +199,65 @@ def run_reference(args):
     return 0
 
 
+def bench_batched(args, torch):
+    """The batched-scenes configuration: 256 dam breaks with N_s ~ U{2048..32768}
+    (seed 7) and viscosity ~ U[0.005, 0.05], each with its own lattice, h and
+    grid.  Batched: all scenes per step in one graph (sph_batch_step).  Serial:
+    the same scenes, each in its own context, stepped one after the other
+    (one graph launch per scene per step).  scenes/s = scenes * steps / time."""
+    from enjaparticles_gb300 import abi, scenes
+    from enjaparticles_gb300.batch import Batch, dambreak_batch_scenes
+    from enjaparticles_gb300.sph import SPH
+    import ctypes as C
+    S = args.batch_scenes
+    ns, mus = dambreak_batch_scenes(S)
+    params = [abi.dambreak_params(n, mu) for n, mu in zip(ns, mus)]
+    data = [scenes.dambreak(n, scene=k) for k, n in enumerate(ns)]
+    stream = torch.cuda.current_stream()
+    b = Batch(params, ns)
+    b.set_stream(stream.cuda_stream)
+    for k, (pos, vel) in enumerate(data):
+        b.upload(k, pos, vel)
+    b.step(DT, 5)
+    b.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.step(DT, args.batch_steps)
+    e1.record(stream)
+    e1.synchronize()
+    t_batch = e0.elapsed_time(e1) / 1e3
+    b.sync()
+    frozen = b.out_of_grid()
+    b.close()
+    ctxs = []
+    for (sp, g, gs), (pos, vel), n in zip(params, data, ns):
+        s = SPH(sp, g, n, gs)
+        abi.check(s.lib, s.ctx, s.lib.sph_set_stream(s.ctx, C.c_void_p(stream.cuda_stream)))
+        s.upload(pos, vel)
+        ctxs.append(s)
+    for _ in range(2):
+        for s in ctxs:
+            s.step(DT, 1)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.serial_steps):
+        for s in ctxs:
+            s.step(DT, 1)
+    e1.record(stream)
+    e1.synchronize()
+    t_serial = e0.elapsed_time(e1) / 1e3
+    for s in ctxs:
+        s.close()
+    batched = S * args.batch_steps / t_batch
+    serial = S * args.serial_steps / t_serial
+    return {"metric": "scenes/s", "scenes": S, "particles": int(sum(ns)), "value": batched,
+            "serial_value": serial, "speedup_vs_serial": batched / serial, "batch_steps": args.batch_steps,
+            "serial_steps": args.serial_steps, "ms_per_batch_step": 1e3 * t_batch / args.batch_steps,
+            "frozen_out_of_grid": frozen,
+            "note": "each scene of a batch steps bit-identically to the same scene in its own context"}
+
+
 def config_block(n, c):
     return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001, "
                         "1000-step rollout config" % n,
@@ -331,6 +394,8 @@ def main():
     }
     if clocks:
         line["clocks"] = clocks
+    if rank == 0 and not args.no_batched:
+        line["batched"] = bench_batched(args, torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(n, args.cpu_seconds)
     if rank == 0:

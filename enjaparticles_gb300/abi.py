@@ -93,6 +93,16 @@ SIGNATURES = {
     "sph_profile_kernel_name": (C.c_char_p, [_P, _I]),
     "sph_sync": (_I, [_P]),
     "sph_last_error": (_I, [_P, C.c_char_p, _I]),
+    "sph_batch_create": (_I, [_I, _P, _P, _P, _P, C.POINTER(_P)]),
+    "sph_batch_destroy": (_I, [_P]),
+    "sph_batch_set_stream": (_I, [_P, _P]),
+    "sph_batch_set_exact": (_I, [_P, _I]),
+    "sph_batch_upload": (_I, [_P, _I, _P, _P, _P, _I]),
+    "sph_batch_step": (_I, [_P, _F, _I]),
+    "sph_batch_download": (_I, [_P, _I, _I, _P, _I]),
+    "sph_batch_out_of_grid": (_I, [_P, C.POINTER(_I)]),
+    "sph_batch_sync": (_I, [_P]),
+    "sph_batch_last_error": (_I, [_P, C.c_char_p, _I]),
     "sph_sort_pairs_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P]),
     "sph_build_info": (C.c_char_p, []),
 }

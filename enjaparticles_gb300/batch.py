@@ -1,0 +1,84 @@
+"""Python view of the batch API (sph_batch_*): many independent scenes stepped
+together with one launch sequence per step."""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class Batch:
+    def __init__(self, params, max_num, exact=False):
+        """params: list of (SPHParams, GridParams, GridParams scaled) per scene."""
+        self.lib = abi.load_library()
+        n = len(params)
+        SP = (abi.SPHParams * n)(*[p[0] for p in params])
+        G = (abi.GridParams * n)(*[p[1] for p in params])
+        GS = (abi.GridParams * n)(*[p[2] for p in params])
+        M = (C.c_int * n)(*[int(m) for m in max_num])
+        self.h = C.c_void_p()
+        rc = self.lib.sph_batch_create(n, C.cast(SP, C.c_void_p), C.cast(G, C.c_void_p), C.cast(GS, C.c_void_p),
+                                       C.cast(M, C.c_void_p), C.byref(self.h))
+        if rc != abi.SPH_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.sph_batch_last_error(None, buf, 512)
+            raise abi.SPHError(rc, buf.value.decode())
+        self.nscenes = n
+        self.num = [0] * n
+        if exact:
+            self._ck(self.lib.sph_batch_set_exact(self.h, 1))
+
+    def _ck(self, rc):
+        if rc != abi.SPH_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.sph_batch_last_error(self.h, buf, 512)
+            raise abi.SPHError(rc, buf.value.decode())
+
+    def close(self):
+        if self.h:
+            self.lib.sph_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, handle):
+        self._ck(self.lib.sph_batch_set_stream(self.h, C.c_void_p(handle)))
+
+    def upload(self, scene, pos, vel, veleval=None):
+        pos = np.ascontiguousarray(pos, np.float32)
+        vel = np.ascontiguousarray(vel, np.float32)
+        ve = None if veleval is None else np.ascontiguousarray(veleval, np.float32)
+        self._ck(self.lib.sph_batch_upload(self.h, scene, pos.ctypes.data, vel.ctypes.data,
+                                           None if ve is None else ve.ctypes.data, pos.shape[0]))
+        self.num[scene] = pos.shape[0]
+
+    def step(self, dt, nsteps=1):
+        self._ck(self.lib.sph_batch_step(self.h, float(dt), int(nsteps)))
+
+    def sync(self):
+        self._ck(self.lib.sph_batch_sync(self.h))
+
+    def get(self, scene, field):
+        out = np.empty((self.num[scene], 4), np.float32)
+        self._ck(self.lib.sph_batch_download(self.h, scene, abi.FIELDS[field], out.ctypes.data, self.num[scene]))
+        return out
+
+    def out_of_grid(self):
+        c = C.c_int()
+        self._ck(self.lib.sph_batch_out_of_grid(self.h, C.byref(c)))
+        return c.value
+
+
+def dambreak_batch_scenes(nscenes, seed_n=7, seed_mu=None, n_lo=2048, n_hi=32768, mu_lo=0.005, mu_hi=0.05):
+    """Scene sizes N_s ~ U{n_lo..n_hi} and viscosities mu_s ~ U[mu_lo, mu_hi]
+    from the seeded streams of enjaparticles_gb300.scenes."""
+    from .scenes import uniform
+    u = uniform(seed_n, nscenes)
+    ns = [int(n_lo + min(int(x * (n_hi - n_lo + 1)), n_hi - n_lo)) for x in u]
+    mu_u = uniform(seed_n + 1000 if seed_mu is None else seed_mu, nscenes)
+    mus = [float(np.float32(mu_lo + x * (mu_hi - mu_lo))) for x in mu_u]
+    return ns, mus

@@ -129,12 +129,23 @@ bool finite_params(const SPHParams& s) {
 
 float4 to_f4(const sph_float4& v) { return make_float4(v.x, v.y, v.z, v.w); }
 
-int build_step_params(sph_ctx* c) {
-    const SPHParams& s = c->sp;
-    StepParams& P = c->P;
-    if (!finite_params(s)) return set_err(c, SPH_EINVAL, "SPHParams holds a non-finite value");
-    if (!(s.smoothing_distance > 0.f)) return set_err(c, SPH_EINVAL, "smoothing_distance must be > 0");
-    if (!(s.simulation_scale > 0.f)) return set_err(c, SPH_EINVAL, "simulation_scale must be > 0");
+}  // namespace
+
+// Per-step kernel parameters of one system (also used by the batch API).
+int sph_make_step_params(const SPHParams& s, const GridParams& gp, const GridParams& gps, StepParams& P,
+                         std::string& err) {
+    if (!finite_params(s)) {
+        err = "SPHParams holds a non-finite value";
+        return SPH_EINVAL;
+    }
+    if (!(s.smoothing_distance > 0.f)) {
+        err = "smoothing_distance must be > 0";
+        return SPH_EINVAL;
+    }
+    if (!(s.simulation_scale > 0.f)) {
+        err = "simulation_scale must be > 0";
+        return SPH_EINVAL;
+    }
     P.sc = s.simulation_scale;
     P.h = s.smoothing_distance;
     P.h2 = s.smoothing_distance * s.smoothing_distance;
@@ -157,23 +168,54 @@ int build_step_params(sph_ctx* c) {
     P.coef_b = (float)(-0.5 * (double)s.wspiky_d_coef);
     P.coef_s = s.viscosity * s.wvisc_dd_coef;
     P.coef_d = (float)(2.0 * (double)s.mass * (double)s.wpoly6_coef);
-    P.g_min = to_f4(c->gp.grid_min);
-    P.g_delta = to_f4(c->gp.grid_delta);
-    P.g_res = to_f4(c->gp.grid_res);
-    P.gs_min = to_f4(c->gps.grid_min);
-    P.gs_delta = to_f4(c->gps.grid_delta);
-    P.gs_res = to_f4(c->gps.grid_res);
-    P.gs_bnd_min = to_f4(c->gps.bnd_min);
-    P.gs_bnd_max = to_f4(c->gps.bnd_max);
-    P.nb_cells = c->gp.nb_cells;
-    P.res_x = (int)c->gps.grid_res.x;
-    P.res_y = (int)c->gps.grid_res.y;
-    P.res_z = (int)c->gps.grid_res.z;
-    const bool integral = (float)P.res_x == c->gps.grid_res.x && (float)P.res_y == c->gps.grid_res.y &&
-                          (float)P.res_z == c->gps.grid_res.z && P.res_x > 0 && P.res_y > 0 && P.res_z > 0;
+    P.g_min = to_f4(gp.grid_min);
+    P.g_delta = to_f4(gp.grid_delta);
+    P.g_res = to_f4(gp.grid_res);
+    P.gs_min = to_f4(gps.grid_min);
+    P.gs_delta = to_f4(gps.grid_delta);
+    P.gs_res = to_f4(gps.grid_res);
+    P.gs_bnd_min = to_f4(gps.bnd_min);
+    P.gs_bnd_max = to_f4(gps.bnd_max);
+    P.nb_cells = gp.nb_cells;
+    P.res_x = (int)gps.grid_res.x;
+    P.res_y = (int)gps.grid_res.y;
+    P.res_z = (int)gps.grid_res.z;
+    const bool integral = (float)P.res_x == gps.grid_res.x && (float)P.res_y == gps.grid_res.y &&
+                          (float)P.res_z == gps.grid_res.z && P.res_x > 0 && P.res_y > 0 && P.res_z > 0;
     const double span = (double)(P.res_x + 4) * (P.res_y + 4) * (P.res_z + 4);
     P.int_hash_ok = (integral && span < 16777216.0) ? 1 : 0;
     P.unit_scale = s.simulation_scale == 1.0f ? 1 : 0;
+    return SPH_OK;
+}
+
+// System::setupDomain's scaled copy (System.cpp:318-325): lanes times
+// sim_scale, delta times the float reciprocal of sim_scale.
+GridParams sph_scaled_grid(const GridParams& g, float sc) {
+    auto mul = [sc](sph_float4 v) {
+        v.x = sc * v.x; v.y = sc * v.y; v.z = sc * v.z; v.w = sc * v.w;
+        return v;
+    };
+    auto div = [sc](sph_float4 v) {
+        const float d = 1.f / sc;
+        v.x = d * v.x; v.y = d * v.y; v.z = d * v.z; v.w = d * v.w;
+        return v;
+    };
+    GridParams s = g;
+    s.grid_min = mul(g.grid_min);
+    s.grid_max = mul(g.grid_max);
+    s.bnd_min = mul(g.bnd_min);
+    s.bnd_max = mul(g.bnd_max);
+    s.grid_size = mul(g.grid_size);
+    s.grid_delta = div(g.grid_delta);
+    return s;
+}
+
+namespace {
+
+int build_step_params(sph_ctx* c) {
+    std::string err;
+    const int rc = sph_make_step_params(c->sp, c->gp, c->gps, c->P, err);
+    if (rc != SPH_OK) return set_err(c, rc, "%s", err.c_str());
     c->params_version++;
     return SPH_OK;
 }
@@ -332,26 +374,7 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     sph_ctx* c = new sph_ctx();
     c->sp = *sphp;
     c->gp = *grid;
-    if (grid_scaled) {
-        c->gps = *grid_scaled;
-    } else {
-        // System::setupDomain's scaled copy (System.cpp:318-325): lanes times
-        // sim_scale, delta times the float reciprocal of sim_scale.
-        const float sc = sphp->simulation_scale;
-        auto mul = [sc](sph_float4 v) { v.x = sc * v.x; v.y = sc * v.y; v.z = sc * v.z; v.w = sc * v.w; return v; };
-        auto div = [sc](sph_float4 v) {
-            const float d = 1.f / sc;
-            v.x = d * v.x; v.y = d * v.y; v.z = d * v.z; v.w = d * v.w;
-            return v;
-        };
-        c->gps = *grid;
-        c->gps.grid_min = mul(grid->grid_min);
-        c->gps.grid_max = mul(grid->grid_max);
-        c->gps.bnd_min = mul(grid->bnd_min);
-        c->gps.bnd_max = mul(grid->bnd_max);
-        c->gps.grid_size = mul(grid->grid_size);
-        c->gps.grid_delta = div(grid->grid_delta);
-    }
+    c->gps = grid_scaled ? *grid_scaled : sph_scaled_grid(*grid, sphp->simulation_scale);
     if (c->gps.nb_cells != c->gp.nb_cells) {
         delete c;
         return set_err(nullptr, SPH_EINVAL, "scaled grid nb_cells differs");

@@ -1,0 +1,475 @@
+// sph_batch.cu — many independent SPH systems ("scenes") stepped together.
+//
+// No counterpart in the reference, which steps one system per SPH object; a
+// batch gives each scene its own SPHParams and grid and advances all of them
+// with one launch sequence per step (captured in one CUDA graph):
+//
+//   hash     every particle slot of every scene; key = scene << cell_bits |
+//            cell (the scene's own grid and out-of-grid cell C_s); unused
+//            slots get a key above every scene's keys
+//   sort     the same stable LSD radix sort over the segmented key space:
+//            scenes come out in order, each in its own cell order
+//   cells    cell ranges into per-scene segments of one cell array, and the
+//            gather of pos / veleval into sorted order
+//   density, force+collision+leapfrog: the neighbour passes with the scene of
+//            each particle looked up from its key (ManyScenes)
+//
+// Per particle the arithmetic is the single-system one, so every scene of a
+// batch steps exactly as it would alone.  Particles that leave their scene's
+// grid are frozen (counted by sph_batch_out_of_grid); a lone system would
+// delete them.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sph_device.cuh"
+
+using sphk::StepParams;
+
+namespace {
+
+constexpr int kBatchFrozen = 5;  // info slot: frozen particles seen by the last step
+
+__global__ void __launch_bounds__(256) k_bhash(const float4* __restrict__ pos_u, uint32_t* __restrict__ keys,
+                                               uint32_t* __restrict__ idx, uint32_t* __restrict__ cell_start,
+                                               size_t ncell_words, uint32_t* __restrict__ hist,
+                                               const uint16_t* __restrict__ scene_of,
+                                               const uint32_t* __restrict__ slot_off,
+                                               const int* __restrict__ num, const StepParams* __restrict__ table,
+                                               int nslots, int cell_bits, uint32_t invalid_key, int passes) {
+    __shared__ uint32_t s_hist[4][256];
+    const int tid = threadIdx.x;
+    for (int k = tid; k < 4 * 256; k += blockDim.x) (&s_hist[0][0])[k] = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + tid; k < ncell_words; k += stride) cell_start[k] = sphk::kEmpty;
+    __syncthreads();
+    const unsigned lane = tid & 31;
+    for (size_t base = (size_t)blockIdx.x * blockDim.x + (tid & ~31); base < (size_t)nslots; base += stride) {
+        const size_t t = base + lane;
+        const bool inside = t < (size_t)nslots;
+        uint32_t key = invalid_key;
+        if (inside) {
+            const uint32_t s = scene_of[t];
+            if ((int)(t - slot_off[s]) < num[s]) {
+                const StepParams& P = table[s];
+                const float4 q = __ldg(pos_u + t);
+                const int3 c = sphk::grid_cell(q.x, q.y, q.z, P.g_min, P.g_delta);
+                int h = sphk::grid_hash_f(c.x, c.y, c.z, P.g_res);
+                h = h > P.nb_cells ? P.nb_cells : h;
+                h = h < 0 ? P.nb_cells : h;
+                key = (s << cell_bits) | (uint32_t)h;
+            }
+            keys[t] = key;
+            idx[t] = (uint32_t)t;
+        }
+        for (int ps = 0; ps < passes; ++ps) {
+            const uint32_t d = inside ? ((key >> (8 * ps)) & 255u) : 0x100u;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            if (inside && (int)lane == 31 - __clz(peers)) atomicAdd(&s_hist[ps][d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int k = tid; k < passes * 256; k += blockDim.x) {
+        const uint32_t c = (&s_hist[0][0])[k];
+        if (c) atomicAdd(hist + k, c);
+    }
+}
+
+// Cell ranges (cellindices.cl semantics per scene segment) and the gather.
+__global__ void __launch_bounds__(256) k_bcells(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ idx,
+                                                uint32_t* __restrict__ cell_start, uint32_t* __restrict__ cell_end,
+                                                const uint32_t* __restrict__ cbase,
+                                                const StepParams* __restrict__ table, const float4* __restrict__ pos_u,
+                                                const float4* __restrict__ veleval_u, float4* __restrict__ pos_s,
+                                                float4* __restrict__ veleval_s, int* __restrict__ info, int nvalid,
+                                                int cell_bits) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const uint32_t key = i < nvalid ? keys[i] : 0xffffffffu;
+    uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+    if (lane == 0 && i > 0 && i < nvalid) prev = keys[i - 1];
+    if (i >= nvalid) return;
+    const uint32_t cmask = (1u << cell_bits) - 1u;
+    const uint32_t s = key >> cell_bits, cell = key & cmask;
+    const uint32_t g = cbase[s] + cell;
+    if (i == 0) {
+        cell_start[g] = 0;
+    } else if (prev != key) {
+        cell_start[g] = (uint32_t)i;
+        cell_end[cbase[prev >> cell_bits] + (prev & cmask)] = (uint32_t)i;
+    }
+    if (i == nvalid - 1) cell_end[g] = (uint32_t)nvalid;
+    if (cell == (uint32_t)table[s].nb_cells) atomicAdd(info + kBatchFrozen, 1);
+    const uint32_t o = __ldg(idx + i);
+    pos_s[i] = __ldg(pos_u + o);
+    veleval_s[i] = __ldg(veleval_u + o);
+}
+
+__global__ void k_bset(int* p, int v) { *p = v; }
+__global__ void k_bzero_int(int* p) { *p = 0; }
+
+int bit_width_u(uint32_t v) {
+    int b = 0;
+    while (v) {
+        ++b;
+        v >>= 1;
+    }
+    return b;
+}
+
+}  // namespace
+
+struct sph_batch {
+    int device = 0, nscenes = 0, exact = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    std::vector<SPHParams> sp;
+    std::vector<GridParams> gp, gps;
+    std::vector<StepParams> P;
+    std::vector<int> max_num, num;
+    std::vector<uint32_t> slot_off, cbase;
+    int nslots = 0, nvalid = 0, cell_bits = 0, scene_bits = 0, passes = 1, tiles_cap = 0, unit = 1;
+    size_t ncells_total = 0;
+    uint32_t invalid_key = 0;
+    // device
+    float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr, *pos_s = nullptr, *veleval_s = nullptr;
+    float4 *rec_pd = nullptr, *rec_vi = nullptr;
+    float* density = nullptr;
+    uint32_t *mask = nullptr, *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
+    uint32_t *cell_start = nullptr, *cell_end = nullptr;
+    uint16_t* scene_of = nullptr;
+    uint32_t *d_slot_off = nullptr, *d_cbase = nullptr;
+    int* d_num = nullptr;
+    StepParams* d_table = nullptr;
+    int *info_sort = nullptr, *info_nb = nullptr;
+    uint32_t *hist = nullptr, *status = nullptr;
+    int* host_info = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.f;
+    int graph_valid = -1, graph_exact = -1;
+    std::string err;
+};
+
+static std::string g_batch_create_error;
+
+static int berr(sph_batch* b, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    (b ? b->err : g_batch_create_error) = buf;
+    return code;
+}
+
+#define BCK(b, call)                                                                                  \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return berr(b, SPH_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));    \
+    } while (0)
+
+static void batch_free(sph_batch* b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    void* ptrs[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi, b->density,
+                    b->mask, b->keys_a, b->idx_a, b->keys_b, b->idx_b, b->cell_start, b->cell_end, b->scene_of,
+                    b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->info_sort, b->info_nb, b->hist, b->status};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (b->host_info) cudaFreeHost(b->host_info);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+}
+
+static sphk::ManyScenes batch_scenes(const sph_batch* b) {
+    return sphk::ManyScenes{b->d_table, b->d_cbase, b->keys_a, b->cell_bits};
+}
+
+static int batch_enqueue_step(sph_batch* b, float dt) {
+    cudaStream_t st = b->stream;
+    uint32_t* hkeys = (b->passes & 1) ? b->keys_b : b->keys_a;
+    uint32_t* hidx = (b->passes & 1) ? b->idx_b : b->idx_a;
+    sphk::launch_prologue(b->hist, b->info_sort, st);
+    int blocks = (b->nslots + 255) / 256;
+    blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
+    k_bhash<<<blocks, 256, 0, st>>>(b->pos_u, hkeys, hidx, b->cell_start, b->ncells_total, b->hist, b->scene_of,
+                                     b->d_slot_off, b->d_num, b->d_table, b->nslots, b->cell_bits, b->invalid_key,
+                                     b->passes);
+    k_bzero_int<<<1, 1, 0, st>>>(b->info_nb + kBatchFrozen);
+    sphk::launch_sort_reset(b->status, (size_t)b->passes * b->tiles_cap * 256, b->info_sort + sphk::kSortTiles, st);
+    uint32_t *kin = hkeys, *vin = hidx;
+    uint32_t *kout = (kin == b->keys_a) ? b->keys_b : b->keys_a, *vout = (vin == b->idx_a) ? b->idx_b : b->idx_a;
+    const int total_bits = b->scene_bits + b->cell_bits;
+    for (int ps = 0; ps < b->passes; ++ps) {
+        int bits = total_bits - 8 * ps;
+        bits = bits > 8 ? 8 : (bits < 1 ? 1 : bits);
+        sphk::launch_radix_pass(kin, vin, kout, vout, b->info_sort, b->hist + ps * 256,
+                                b->status + (size_t)ps * b->tiles_cap * 256, b->info_sort + sphk::kSortTiles + ps,
+                                b->info_sort + sphk::kError, 8 * ps, bits, b->nslots, st);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    const int cb = (b->nvalid + 255) / 256;
+    k_bcells<<<cb < 1 ? 1 : cb, 256, 0, st>>>(b->keys_a, b->idx_a, b->cell_start, b->cell_end, b->d_cbase, b->d_table,
+                                              b->pos_u, b->veleval_u, b->pos_s, b->veleval_s, b->info_nb, b->nvalid,
+                                              b->cell_bits);
+    const sphk::ManyScenes scenes = batch_scenes(b);
+    sphk::launch_density_batch(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, nullptr, b->mask,
+                               (size_t)b->nslots, b->cell_start, b->cell_end, b->info_nb, scenes, b->unit != 0,
+                               b->nvalid, st);
+    sphk::launch_force_batch(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->cell_start, b->cell_end,
+                             b->info_nb, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, scenes, b->unit != 0, dt,
+                             b->exact, b->nvalid, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return berr(b, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
+    return SPH_OK;
+}
+
+extern "C" {
+
+int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids, const GridParams* grids_scaled,
+                     const int* max_num, sph_batch** out) {
+    if (!out || !sphp || !grids || !max_num || nscenes <= 0 || nscenes > 65536)
+        return berr(nullptr, SPH_EINVAL, "sph_batch_create: bad arguments");
+    *out = nullptr;
+    sph_batch* b = new sph_batch();
+    b->nscenes = nscenes;
+    uint32_t maxc = 0;
+    size_t slots = 0, cells = 0;
+    for (int s = 0; s < nscenes; ++s) {
+        if (max_num[s] <= 0 || grids[s].nb_cells <= 0 || grids[s].nb_cells + 1 >= (1 << 24)) {
+            delete b;
+            return berr(nullptr, SPH_EINVAL, "scene %d: bad max_num or nb_cells", s);
+        }
+        b->sp.push_back(sphp[s]);
+        b->gp.push_back(grids[s]);
+        b->gps.push_back(grids_scaled ? grids_scaled[s] : sph_scaled_grid(grids[s], sphp[s].simulation_scale));
+        StepParams P;
+        std::string e;
+        if (sph_make_step_params(b->sp[s], b->gp[s], b->gps[s], P, e) != SPH_OK) {
+            delete b;
+            return berr(nullptr, SPH_EINVAL, "scene %d: %s", s, e.c_str());
+        }
+        if (!P.unit_scale) b->unit = 0;
+        b->P.push_back(P);
+        b->max_num.push_back(max_num[s]);
+        b->num.push_back(0);
+        b->slot_off.push_back((uint32_t)slots);
+        b->cbase.push_back((uint32_t)cells);
+        slots += (size_t)max_num[s];
+        cells += (size_t)grids[s].nb_cells + 1;
+        if ((uint32_t)grids[s].nb_cells > maxc) maxc = (uint32_t)grids[s].nb_cells;
+    }
+    if (slots >= (1u << 30)) {
+        delete b;
+        return berr(nullptr, SPH_EINVAL, "too many particle slots");
+    }
+    b->nslots = (int)slots;
+    b->ncells_total = cells;
+    b->cell_bits = bit_width_u(maxc + 1u);
+    b->scene_bits = bit_width_u((uint32_t)(nscenes - 1));
+    if (b->cell_bits + b->scene_bits > 32) {
+        delete b;
+        return berr(nullptr, SPH_EINVAL, "scene and cell bits exceed a 32-bit key");
+    }
+    b->invalid_key = (uint32_t)(((uint64_t)nscenes << b->cell_bits) - 1u);
+    b->passes = (b->scene_bits + b->cell_bits + 7) / 8;
+    b->tiles_cap = sphk::radix_tiles(b->nslots);
+    cudaGetDevice(&b->device);
+    const size_t N = slots;
+    int rc = SPH_OK;
+#define BALLOC(ptr, bytes)                                                                                   \
+    do {                                                                                                     \
+        if (rc == SPH_OK && cudaMalloc((void**)&(ptr), (bytes)) != cudaSuccess) {                            \
+            cudaGetLastError();                                                                              \
+            rc = berr(nullptr, SPH_ENOMEM, "cudaMalloc(%zu) failed", (size_t)(bytes));                       \
+        }                                                                                                    \
+    } while (0)
+    BALLOC(b->pos_u, N * 16);
+    BALLOC(b->vel_u, N * 16);
+    BALLOC(b->veleval_u, N * 16);
+    BALLOC(b->pos_s, N * 16);
+    BALLOC(b->veleval_s, N * 16);
+    BALLOC(b->rec_pd, N * 16);
+    BALLOC(b->rec_vi, N * 16);
+    BALLOC(b->density, N * 4);
+    BALLOC(b->mask, N * 4 * sphk::kMaskWords);
+    BALLOC(b->keys_a, N * 4);
+    BALLOC(b->idx_a, N * 4);
+    BALLOC(b->keys_b, N * 4);
+    BALLOC(b->idx_b, N * 4);
+    BALLOC(b->cell_start, cells * 4);
+    BALLOC(b->cell_end, cells * 4);
+    BALLOC(b->scene_of, N * 2);
+    BALLOC(b->d_slot_off, nscenes * 4);
+    BALLOC(b->d_cbase, nscenes * 4);
+    BALLOC(b->d_num, nscenes * 4);
+    BALLOC(b->d_table, nscenes * sizeof(StepParams));
+    BALLOC(b->info_sort, sizeof(int) * sphk::kInfoSlots);
+    BALLOC(b->info_nb, sizeof(int) * sphk::kInfoSlots);
+    BALLOC(b->hist, 4 * 256 * 4);
+    BALLOC(b->status, (size_t)b->passes * b->tiles_cap * 256 * 4);
+#undef BALLOC
+    if (rc == SPH_OK && cudaMallocHost((void**)&b->host_info, sizeof(int) * sphk::kInfoSlots) != cudaSuccess)
+        rc = berr(nullptr, SPH_ENOMEM, "cudaMallocHost failed");
+    if (rc == SPH_OK && cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        rc = berr(nullptr, SPH_ECUDA, "cudaStreamCreate failed");
+    if (rc != SPH_OK) {
+        batch_free(b);
+        delete b;
+        return rc;
+    }
+    b->stream = b->own_stream;
+    std::vector<uint16_t> sof(N);
+    for (int s = 0; s < nscenes; ++s)
+        for (int k = 0; k < max_num[s]; ++k) sof[b->slot_off[s] + k] = (uint16_t)s;
+    cudaStream_t st = b->stream;
+    cudaError_t e = cudaMemcpy(b->scene_of, sof.data(), N * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_slot_off, b->slot_off.data(), nscenes * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_cbase, b->cbase.data(), nscenes * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_table, b->P.data(), nscenes * sizeof(StepParams), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->d_num, 0, nscenes * 4);
+    if (e == cudaSuccess) e = cudaMemset(b->info_sort, 0, sizeof(int) * sphk::kInfoSlots);
+    if (e == cudaSuccess) e = cudaMemset(b->info_nb, 0, sizeof(int) * sphk::kInfoSlots);
+    const void* zero[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi};
+    for (const void* p : zero)
+        if (e == cudaSuccess) e = cudaMemset((void*)p, 0, N * 16);
+    if (e == cudaSuccess) e = cudaMemset(b->cell_start, 0xff, cells * 4);
+    if (e == cudaSuccess) e = cudaMemset(b->cell_end, 0, cells * 4);
+    if (e == cudaSuccess) {
+        k_bset<<<1, 1, 0, st>>>(b->info_sort + sphk::kNum, b->nslots);
+        k_bset<<<1, 1, 0, st>>>(b->info_sort + sphk::kOutStart, -1);
+        k_bset<<<1, 1, 0, st>>>(b->info_nb + sphk::kOutStart, -1);
+        e = cudaStreamSynchronize(st);
+    }
+    if (e != cudaSuccess) {
+        berr(nullptr, SPH_ECUDA, "batch init: %s", cudaGetErrorString(e));
+        batch_free(b);
+        delete b;
+        return SPH_ECUDA;
+    }
+    *out = b;
+    return SPH_OK;
+}
+
+int sph_batch_destroy(sph_batch* b) {
+    if (!b) return SPH_EINVAL;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    delete b;
+    return SPH_OK;
+}
+
+int sph_batch_set_stream(sph_batch* b, void* stream) {
+    if (!b) return SPH_EINVAL;
+    b->stream = stream ? (cudaStream_t)stream : b->own_stream;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return SPH_OK;
+}
+
+int sph_batch_set_exact(sph_batch* b, int exact) {
+    if (!b) return SPH_EINVAL;
+    b->exact = exact ? 1 : 0;
+    return SPH_OK;
+}
+
+int sph_batch_upload(sph_batch* b, int scene, const sph_float4* pos, const sph_float4* vel,
+                     const sph_float4* veleval, int n) {
+    if (!b || scene < 0 || scene >= b->nscenes || !pos || !vel || n < 0 || n > b->max_num[scene])
+        return berr(b, SPH_EINVAL, "sph_batch_upload: bad arguments");
+    cudaStream_t st = b->stream;
+    const size_t off = b->slot_off[scene], bytes = (size_t)n * 16;
+    if (n > 0) {
+        BCK(b, cudaMemcpyAsync(b->pos_u + off, pos, bytes, cudaMemcpyHostToDevice, st));
+        BCK(b, cudaMemcpyAsync(b->vel_u + off, vel, bytes, cudaMemcpyHostToDevice, st));
+        if (veleval)
+            BCK(b, cudaMemcpyAsync(b->veleval_u + off, veleval, bytes, cudaMemcpyHostToDevice, st));
+        else
+            BCK(b, cudaMemsetAsync(b->veleval_u + off, 0, bytes, st));
+    }
+    k_bset<<<1, 1, 0, st>>>(b->d_num + scene, n);
+    b->nvalid += n - b->num[scene];
+    b->num[scene] = n;
+    k_bset<<<1, 1, 0, st>>>(b->info_nb + sphk::kNum, b->nvalid);
+    BCK(b, cudaGetLastError());
+    BCK(b, cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
+int sph_batch_step(sph_batch* b, float dt, int nsteps) {
+    if (!b || nsteps < 0 || !std::isfinite(dt)) return berr(b, SPH_EINVAL, "sph_batch_step: bad arguments");
+    cudaSetDevice(b->device);
+    if (nsteps == 0 || b->nvalid == 0) return SPH_OK;
+    if (!b->graph || b->graph_dt != dt || b->graph_valid != b->nvalid || b->graph_exact != b->exact) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = batch_enqueue_step(b, dt);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (rc != SPH_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return berr(b, SPH_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->graph = nullptr;
+            return berr(b, SPH_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        }
+        b->graph_dt = dt;
+        b->graph_valid = b->nvalid;
+        b->graph_exact = b->exact;
+    }
+    for (int k = 0; k < nsteps; ++k) BCK(b, cudaGraphLaunch(b->graph, b->stream));
+    return SPH_OK;
+}
+
+int sph_batch_sync(sph_batch* b) {
+    if (!b) return SPH_EINVAL;
+    BCK(b, cudaMemcpyAsync(b->host_info, b->info_sort, sizeof(int) * sphk::kInfoSlots, cudaMemcpyDeviceToHost,
+                           b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    if (b->host_info[sphk::kError] & sphk::kErrLookbackTimeout)
+        return berr(b, SPH_ETIMEOUT, "radix sort look-back wait expired; the step result is invalid");
+    return SPH_OK;
+}
+
+int sph_batch_out_of_grid(sph_batch* b, int* count) {
+    if (!b || !count) return SPH_EINVAL;
+    int v = 0;
+    BCK(b, cudaMemcpyAsync(&v, b->info_nb + kBatchFrozen, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    *count = v;
+    return SPH_OK;
+}
+
+int sph_batch_download(sph_batch* b, int scene, int field, void* host, int n) {
+    if (!b || scene < 0 || scene >= b->nscenes || !host || n < 0 || n > b->max_num[scene])
+        return berr(b, SPH_EINVAL, "sph_batch_download: bad arguments");
+    const float4* src = nullptr;
+    switch (field) {
+        case SPH_FIELD_POS_U: src = b->pos_u; break;
+        case SPH_FIELD_VEL_U: src = b->vel_u; break;
+        case SPH_FIELD_VELEVAL_U: src = b->veleval_u; break;
+        default: return berr(b, SPH_EINVAL, "sph_batch_download: only pos_u, vel_u, veleval_u");
+    }
+    if (n > 0)
+        BCK(b, cudaMemcpyAsync(host, src + b->slot_off[scene], (size_t)n * 16, cudaMemcpyDeviceToHost, b->stream));
+    return sph_batch_sync(b);
+}
+
+int sph_batch_last_error(sph_batch* b, char* buf, int len) {
+    if (!buf || len <= 0) return SPH_EINVAL;
+    std::snprintf(buf, (size_t)len, "%s", (b ? b->err : g_batch_create_error).c_str());
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -20,16 +20,16 @@ namespace sphk {
 
 // When called from the fused step the kernel also does the out-of-grid
 // deletion bookkeeping (vel_s != nullptr).
-template <bool Unit, bool WantCount>
+template <bool Unit, bool WantCount, class Scenes>
 __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ veleval_s,
                                                  float* __restrict__ density, float4* __restrict__ rec_pd,
                                                  float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
                                                  uint32_t* __restrict__ mask, const size_t mstride,
-                                                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                                                 const uint32_t* __restrict__ cs0, const uint32_t* __restrict__ ce0,
                                                  int* __restrict__ info, const uint32_t* __restrict__ idx,
                                                  const float4* __restrict__ vel_u, float4* __restrict__ vel_s,
                                                  float4* __restrict__ del_pos, float4* __restrict__ del_vel,
-                                                 const StepParams P) {
+                                                 const Scenes R) {
     int n_old, out;
     const int n = effective_num(info, n_old, out);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -46,8 +46,18 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
         }
     }
     if (i >= n) return;
+    const StepParams& P = R.params(i);
+    const uint32_t* cs = cs0 + R.cell_base(i);
+    const uint32_t* ce = ce0 + R.cell_base(i);
     float4 pi = __ldg(pos_s + i);
     if (!Unit) pi = v4scale(pi, P.sc);
+    if (R.frozen(i)) {
+        density[i] = 0.f;
+        rec_pd[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
+        rec_vi[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (WantCount) nbr[i] = 0;
+        return;
+    }
     const float rc2 = P.rcut2, h2 = P.h2;
     float acc = 0.f;
     uint32_t cnt = 0;
@@ -97,24 +107,42 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
     if (WantCount) nbr[i] = cnt;
 }
 
-void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
-                    uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
-                    const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
-                    float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
-                    cudaStream_t st) {
+template <class Scenes>
+void launch_density_t(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
+                      uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
+                      const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
+                      float4* vel_s, float4* del_pos, float4* del_vel, const Scenes& R, bool unit, int grid_items,
+                      cudaStream_t st) {
     const int threads = 256;
     int blocks = (grid_items + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
-#define SPH_DENSITY_LAUNCH(U, W)                                                                              \
-    k_density<U, W><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, \
-                                                cell_start, cell_end, (int*)info, idx, vel_u, vel_s, del_pos,      \
-                                                del_vel, p)
-    if (p.unit_scale) {
+#define SPH_DENSITY_LAUNCH(U, W)                                                                                    \
+    k_density<U, W, Scenes><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask,      \
+                                                        mask_stride, cell_start, cell_end, (int*)info, idx, vel_u, \
+                                                        vel_s, del_pos, del_vel, R)
+    if (unit) {
         if (nbr) SPH_DENSITY_LAUNCH(true, true); else SPH_DENSITY_LAUNCH(true, false);
     } else {
         if (nbr) SPH_DENSITY_LAUNCH(false, true); else SPH_DENSITY_LAUNCH(false, false);
     }
 #undef SPH_DENSITY_LAUNCH
+}
+
+void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
+                    uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
+                    const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
+                    float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
+                    cudaStream_t st) {
+    launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
+                     idx, vel_u, vel_s, del_pos, del_vel, OneScene{p}, p.unit_scale != 0, grid_items, st);
+}
+
+void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
+                          float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
+                          const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                          const ManyScenes& scenes, bool unit, int grid_items, cudaStream_t st) {
+    launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
+                     nullptr, nullptr, nullptr, nullptr, nullptr, scenes, unit, grid_items, st);
 }
 
 }  // namespace sphk

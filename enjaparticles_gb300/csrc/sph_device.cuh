@@ -57,6 +57,34 @@ struct StepParams {
     int unit_scale;               // simulation_scale == 1.0f
 };
 
+// Scenes of the neighbour passes.
+//   OneScene: one particle system; the step parameters are the kernel
+//   argument and the cell arrays are the context's.
+//   ManyScenes: a batch of independent systems sorted together; the scene of
+//   sorted particle i is the high part of its key (key = scene << cell_bits |
+//   cell), each scene has its own parameter block and its own segment of the
+//   cell arrays.  A particle in its scene's out-of-grid cell is frozen: not
+//   walked, not integrated (a lone system would delete it).
+struct OneScene {
+    StepParams P;
+    __device__ __forceinline__ const StepParams& params(int) const { return P; }
+    __device__ __forceinline__ uint32_t cell_base(int) const { return 0u; }
+    __device__ __forceinline__ bool frozen(int) const { return false; }
+};
+struct ManyScenes {
+    const StepParams* table;
+    const uint32_t* cbase;
+    const uint32_t* keys;
+    int cell_bits;
+    __device__ __forceinline__ uint32_t scene(int i) const { return __ldg(keys + i) >> cell_bits; }
+    __device__ __forceinline__ const StepParams& params(int i) const { return table[scene(i)]; }
+    __device__ __forceinline__ uint32_t cell_base(int i) const { return __ldg(cbase + scene(i)); }
+    __device__ __forceinline__ bool frozen(int i) const {
+        const uint32_t k = __ldg(keys + i);
+        return (k & ((1u << cell_bits) - 1u)) == (uint32_t)table[k >> cell_bits].nb_cells;
+    }
+};
+
 // float -> int as the kernels' (int) cast, truncating toward zero; the
 // hardware conversion saturates and maps NaN to 0.
 __device__ __forceinline__ int f2i_rz(float v) { return __float2int_rz(v); }
@@ -114,6 +142,15 @@ void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_v
                   int* tile_ctr, int nsm, float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s,
                   float4* pos_u, float4* vel_u, float4* veleval_u, const StepParams& p, float dt, int fused,
                   int exact, int grid_items, cudaStream_t st);
+// Batch forms of the neighbour passes (fused force only).
+void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
+                          float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
+                          const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                          const ManyScenes& scenes, bool unit, int grid_items, cudaStream_t st);
+void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                        size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                        uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const ManyScenes& scenes,
+                        bool unit, float dt, int exact, int grid_items, cudaStream_t st);
 void launch_collision(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info,
                       const StepParams& p, int grid_items, cudaStream_t st);
 void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
@@ -127,3 +164,9 @@ void launch_permute_only(const uint32_t* idx, const float4* pos_u, const float4*
                          cudaStream_t st);
 
 }  // namespace sphk
+
+// Host helpers shared by the single-system and batch APIs (sph_api.cu).
+#include <string>
+int sph_make_step_params(const SPHParams& s, const GridParams& gp, const GridParams& gps, sphk::StepParams& P,
+                         std::string& err);
+GridParams sph_scaled_grid(const GridParams& g, float sc);

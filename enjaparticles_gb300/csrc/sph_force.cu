@@ -79,13 +79,13 @@ __device__ __forceinline__ void force_pair(ForceSums& a, const float4& pi, const
     }
 }
 
-template <bool Fused, bool Exact, bool Unit>
+template <bool Fused, bool Exact, bool Unit, class Scenes>
 __global__ void __launch_bounds__(kForceThreads) k_force(
     const float4* __restrict__ pos_s, const float4* __restrict__ rec_pd, const float4* __restrict__ rec_vi,
-    const uint32_t* __restrict__ mask, const size_t mstride, const uint32_t* __restrict__ cs,
-    const uint32_t* __restrict__ ce, const int* __restrict__ info, float4* __restrict__ force_s,
+    const uint32_t* __restrict__ mask, const size_t mstride, const uint32_t* __restrict__ cs0,
+    const uint32_t* __restrict__ ce0, const int* __restrict__ info, float4* __restrict__ force_s,
     float4* __restrict__ xsph_s, uint32_t* __restrict__ idx, const float4* __restrict__ vel_s,
-    float4* __restrict__ pos_u, float4* __restrict__ vel_u, float4* __restrict__ veleval_u, const StepParams P,
+    float4* __restrict__ pos_u, float4* __restrict__ vel_u, float4* __restrict__ veleval_u, const Scenes R,
     const float dt) {
     // Row table of each thread: sorted index of the run's first candidate and
     // walk-order offset of it; rows without candidates are left out.
@@ -95,8 +95,12 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     const int n = effective_num(info, n_old, out);
     const int t = threadIdx.x;
     const int i = blockIdx.x * kForceThreads + t;
-    const unsigned wmask = __ballot_sync(0xffffffffu, i < n);
-    if (i >= n) return;
+    const bool live = i < n && !R.frozen(i);
+    const unsigned wmask = __ballot_sync(0xffffffffu, live);
+    if (!live) return;
+    const StepParams& P = R.params(i);
+    const uint32_t* cs = cs0 + R.cell_base(i);
+    const uint32_t* ce = ce0 + R.cell_base(i);
 
     const float4 pi = __ldg(rec_pd + i);  // scaled position, rho_i
     const float4 vi = __ldg(rec_vi + i);  // veleval_i, 1/rho_i
@@ -211,32 +215,49 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     pos_u[orig] = po;
 }
 
+template <class Scenes>
+void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                    size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                    float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
+                    float4* veleval_u, const Scenes& R, bool unit, float dt, int fused, int exact, int grid_items,
+                    cudaStream_t st) {
+    int blocks = (grid_items + kForceThreads - 1) / kForceThreads;
+    if (blocks < 1) blocks = 1;
+#define SPH_FORCE_LAUNCH(F, E, U)                                                                                   \
+    k_force<F, E, U, Scenes><<<blocks, kForceThreads, 0, st>>>(pos_s, rec_pd, rec_vi, mask, mask_stride,           \
+                                                               cell_start, cell_end, info, force_s, xsph_s, idx,  \
+                                                               vel_s, pos_u, vel_u, veleval_u, R, dt)
+    if (fused) {
+        if (exact) {
+            if (unit) SPH_FORCE_LAUNCH(true, true, true); else SPH_FORCE_LAUNCH(true, true, false);
+        } else {
+            if (unit) SPH_FORCE_LAUNCH(true, false, true); else SPH_FORCE_LAUNCH(true, false, false);
+        }
+    } else {
+        if (exact) {
+            if (unit) SPH_FORCE_LAUNCH(false, true, true); else SPH_FORCE_LAUNCH(false, true, false);
+        } else {
+            if (unit) SPH_FORCE_LAUNCH(false, false, true); else SPH_FORCE_LAUNCH(false, false, false);
+        }
+    }
+#undef SPH_FORCE_LAUNCH
+}
+
 void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                   size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                   int* /*tile_ctr*/, int /*nsm*/, float4* force_s, float4* xsph_s, uint32_t* idx,
                   const float4* vel_s, float4* pos_u, float4* vel_u, float4* veleval_u, const StepParams& p,
                   float dt, int fused, int exact, int grid_items, cudaStream_t st) {
-    int blocks = (grid_items + kForceThreads - 1) / kForceThreads;
-    if (blocks < 1) blocks = 1;
-#define SPH_FORCE_LAUNCH(F, E, U)                                                                            \
-    k_force<F, E, U><<<blocks, kForceThreads, 0, st>>>(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, \
-                                                       cell_end, info, force_s, xsph_s, idx, vel_s, pos_u,   \
-                                                       vel_u, veleval_u, p, dt)
-    const bool u = p.unit_scale != 0;
-    if (fused) {
-        if (exact) {
-            if (u) SPH_FORCE_LAUNCH(true, true, true); else SPH_FORCE_LAUNCH(true, true, false);
-        } else {
-            if (u) SPH_FORCE_LAUNCH(true, false, true); else SPH_FORCE_LAUNCH(true, false, false);
-        }
-    } else {
-        if (exact) {
-            if (u) SPH_FORCE_LAUNCH(false, true, true); else SPH_FORCE_LAUNCH(false, true, false);
-        } else {
-            if (u) SPH_FORCE_LAUNCH(false, false, true); else SPH_FORCE_LAUNCH(false, false, false);
-        }
-    }
-#undef SPH_FORCE_LAUNCH
+    launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, cell_end, info, force_s, xsph_s, idx, vel_s,
+                   pos_u, vel_u, veleval_u, OneScene{p}, p.unit_scale != 0, dt, fused, exact, grid_items, st);
+}
+
+void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                        size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                        uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const ManyScenes& scenes,
+                        bool unit, float dt, int exact, int grid_items, cudaStream_t st) {
+    launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, cell_end, info, nullptr, nullptr, idx,
+                   nullptr, pos_u, vel_u, veleval_u, scenes, unit, dt, 1, exact, grid_items, st);
 }
 
 }  // namespace sphk

@@ -291,6 +291,36 @@ int sph_sync(sph_ctx* ctx);
  * sph_create when ctx is NULL) into buf. */
 int sph_last_error(sph_ctx* ctx, char* buf, int len);
 
+/* ---------------------------------------------------------------------------
+ * Batches: many independent systems ("scenes", each with its own SPHParams,
+ * grid and particle count) stepped together.  No counterpart in the
+ * reference, which steps one system per SPH object.  All scenes share one
+ * launch sequence per step (captured in one CUDA graph); every scene steps
+ * exactly as it would in its own context.  Particles that leave their
+ * scene's grid are frozen and counted (sph_batch_out_of_grid) instead of
+ * deleted.
+ * ------------------------------------------------------------------------- */
+typedef struct sph_batch sph_batch;
+
+/* nscenes scenes: sphp[s], grids[s] (grids_scaled may be NULL: derived from
+ * simulation_scale), capacity max_num[s].  Blocking. */
+int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids,
+                     const GridParams* grids_scaled, const int* max_num, sph_batch** out);
+int sph_batch_destroy(sph_batch* batch);
+int sph_batch_set_stream(sph_batch* batch, void* stream);
+int sph_batch_set_exact(sph_batch* batch, int exact);
+/* Replace scene `scene`'s particles (veleval NULL: zero).  Blocking. */
+int sph_batch_upload(sph_batch* batch, int scene, const sph_float4* pos, const sph_float4* vel,
+                     const sph_float4* veleval, int n);
+/* nsteps steps of every scene (hash ... force+collision+leapfrog).  Asynchronous. */
+int sph_batch_step(sph_batch* batch, float dt, int nsteps);
+/* Copy n elements of pos_u, vel_u or veleval_u of one scene.  Blocking. */
+int sph_batch_download(sph_batch* batch, int scene, int field, void* host, int n);
+/* Number of frozen (out-of-grid) particles in the last step.  Blocking. */
+int sph_batch_out_of_grid(sph_batch* batch, int* count);
+int sph_batch_sync(sph_batch* batch);
+int sph_batch_last_error(sph_batch* batch, char* buf, int len);
+
 /* Sort n (key, value) pairs held in caller-owned device memory, without
  * allocating any device memory.  No counterpart in the reference.
  *
