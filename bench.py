@@ -61,6 +61,10 @@ def parse():
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--serial-steps", type=int, default=10)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=65536)
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--adj-k", type=int, default=20)
     return ap.parse_args()
 
 
@@ -258,6 +262,58 @@ def bench_batched(args, torch):
             "note": "each scene of a batch steps bit-identically to the same scene in its own context"}
 
 
+def bench_adjoint(args, torch):
+    """The differentiable rollout: 65,536 particles of the dam-break lattice,
+    v0 ~ N(0, 0.1^2), 200 steps, checkpoint every 20 steps.
+      forward   200 plain steps (graph replays)
+      record    the same 200 steps keeping the checkpoints (sph_adjoint_record)
+      backward  segment recomputation + reverse kernels (sph_adjoint_backward,
+                one graph), for a loss gradient on the final positions
+    ratio = backward / forward (the adjoint step including its recomputation
+    against the plain forward step)."""
+    from enjaparticles_gb300 import abi, scenes
+    from enjaparticles_gb300.sph import SPH
+    import ctypes as C
+    n, steps, K = args.adj_n, args.adj_steps, args.adj_k
+    pos, vel, _, _ = scenes.rollout_case(n)
+    sp, g, gs = abi.dambreak_params(n, 0.01)
+    s = SPH(sp, g, n, gs)
+    stream = torch.cuda.current_stream()
+    abi.check(s.lib, s.ctx, s.lib.sph_set_stream(s.ctx, C.c_void_p(stream.cuda_stream)))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    s.upload(pos, vel)
+    s.step(DT, 10)
+    s.upload(pos, vel)
+    t_fwd = timed(lambda: s.step(DT, steps))
+    dpos = torch.full((n, 4), 1.0 / n, dtype=torch.float32, device="cuda")
+    dvel = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    s.upload(pos, vel)
+    s.adjoint_record(DT, steps, K)
+    t_build = timed(lambda: s.adjoint_backward(dpos=dpos.data_ptr(), out_vel=dvel.data_ptr()))
+    t_rec, t_bwd = [], []
+    for _ in range(3):
+        s.upload(pos, vel)
+        t_rec.append(timed(lambda: s.adjoint_record(DT, steps, K)))
+        t_bwd.append(timed(lambda: s.adjoint_backward(dpos=dpos.data_ptr(), out_vel=dvel.data_ptr())))
+    s.close()
+    t_rec, t_bwd = min(t_rec), min(t_bwd)
+    C1 = g.nb_cells + 1
+    return {"metric": "adjoint/forward time", "particles": n, "steps": steps, "checkpoint_every": K,
+            "forward_ms": 1e3 * t_fwd, "record_ms": 1e3 * t_rec, "backward_ms": 1e3 * t_bwd,
+            "value": t_bwd / t_fwd, "record_plus_backward_over_forward": (t_rec + t_bwd) / t_fwd,
+            "first_backward_ms_incl_graph_build": 1e3 * t_build,
+            "tape_bytes": K * (132 * n + 8 * C1), "checkpoint_bytes": (steps // K + 2) * 48 * n}
+
+
 def config_block(n, c):
     return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001, "
                         "1000-step rollout config" % n,
@@ -396,6 +452,8 @@ def main():
         line["clocks"] = clocks
     if rank == 0 and not args.no_batched:
         line["batched"] = bench_batched(args, torch)
+    if rank == 0 and not args.no_adjoint:
+        line["adjoint"] = bench_adjoint(args, torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(n, args.cpu_seconds)
     if rank == 0:

@@ -93,6 +93,9 @@ SIGNATURES = {
     "sph_profile_kernel_name": (C.c_char_p, [_P, _I]),
     "sph_sync": (_I, [_P]),
     "sph_last_error": (_I, [_P, C.c_char_p, _I]),
+    "sph_adjoint_record": (_I, [_P, _F, _I, _I]),
+    "sph_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
+    "sph_adjoint_rollout": (_I, [_P, _I, _I, _P, _P, C.POINTER(_F)]),
     "sph_batch_create": (_I, [_I, _P, _P, _P, _P, C.POINTER(_P)]),
     "sph_batch_destroy": (_I, [_P]),
     "sph_batch_set_stream": (_I, [_P, _P]),

@@ -16,7 +16,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librtps_sph.so")
 
 SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cells.cu", "sph_density.cu", "sph_force.cu", "sph_integrate.cu",
-           "sph_batch.cu", "sph_noalloc.cu", "sph_params.cpp"]
+           "sph_batch.cu", "sph_noalloc.cu", "sph_adjoint.cu", "sph_params.cpp"]
 # Per-file flags: the density pass relies on every multiply and add being
 # rounded on its own.
 EXTRA = {"sph_density.cu": ["-fmad=false"]}

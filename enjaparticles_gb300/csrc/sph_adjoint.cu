@@ -1,0 +1,657 @@
+// sph_adjoint.cu — the differentiable rollout: reverse-mode gradients of a
+// loss of the final particle state with respect to the initial state and the
+// viscosity coefficient, through hand-written adjoints of the step's density,
+// force, wall collision and leapfrog stages.
+//
+// Forward step (one fused step, sorted index i, o = sort_indices[i]; the
+// reference formulas of density.cl:44-126, force.cl:43-186,
+// collision_wall.cl:31-118 and leapfrog.cl:30-121):
+//   rho_i = Dc * sum_{j in N(i) + i} w(q_ij),   w(q) = (h^2 - q)^3, q = |p_i - p_j|^2
+//   F_i = sum_j d_ij phi(q) (P_i + P_j) / rho_j,   phi = (h - r)^2 / r,  P = K (rho - rho0)
+//   V_i = sum_j (e_j - e_i) (h - r) / rho_j
+//   X_i = sum_j w(q) (e_j - e_i) / (rho_i + rho_j)
+//   f_i = (m / rho_i) (cb F_i + mu cv V_i) + walls(p_i, v_i),   xs_i = cd X_i
+//   g = clamp(f_i + gravity),  vn = v_i + dt g + xf xs_i,  e' = (v_i + vn) / 2,  p' = p_i + dt vn
+// with p the scaled position, e the veleval velocity, mu the viscosity.
+// Sorting and hashing are piecewise constant and are not differentiated:
+// each reverse step reuses the forward step's permutation, cell ranges,
+// neighbour bitmask and per-particle records.
+//
+// Reverse step, three kernels:
+//   A  per particle: leapfrog, acceleration clamp and walls; gives the
+//      adjoint of the step's input velocity, a_i = (m / rho_i) * fbar_i (the
+//      force adjoint seen by the pair sums), the XSPH sum adjoint and the
+//      density adjoint of the m / rho_i factor.
+//   B  neighbour gather: pressure, viscosity and XSPH pair terms.  Each
+//      thread accumulates both its own (i-side) terms and the terms its
+//      neighbours' sums contribute to it (j-side), so nothing is scattered:
+//      no atomics.  Gives the veleval adjoint, the complete density adjoint
+//      and the viscosity gradient.
+//   C  neighbour gather: the density sum's position terms, with both
+//      particles' density adjoints; completes the position adjoint.
+//
+// Memory: the state (pos, vel, veleval) is checkpointed every K steps during
+// the recorded forward run.  The backward pass recomputes one segment of K
+// steps at a time from its checkpoint with the unchanged forward kernels,
+// which write their per-step records straight into a K-slot tape, then
+// reverses the segment.  Tape per step: sort_indices, cell start/end, the
+// (position, rho) and (veleval, 1/rho) records, the neighbour bitmask, the
+// pre-wall force and the input velocity: 132 B per particle + 8 B per cell.
+// The whole backward pass is one CUDA graph.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "sph_ctx.cuh"
+#include "sph_walk.cuh"
+
+using sphk::StepParams;
+
+namespace {
+
+constexpr int kAdjThreads = 128;
+
+struct TapeStep {
+    const uint32_t* idx;
+    const uint32_t* cs;
+    const uint32_t* ce;
+    const float4* rec_pd;  // (scaled position, rho)
+    const float4* rec_vi;  // (veleval, 1/rho)
+    const uint32_t* mask;
+    const float4* fsph;    // SPH force before the walls
+    const float4* vin;     // velocity the step integrated
+};
+
+__device__ __forceinline__ float3 xyz(const float4& v) { return make_float3(v.x, v.y, v.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// ---------------------------------------------------------------------------
+// A: leapfrog, clamp and walls, per sorted particle.
+//
+// Walls: for an active wall with normal n (diff > EPSILON) the repulsion
+// n (k diff - c n.v) has d/dp = -k n n^T and d/dv = -c n n^T; the "friction"
+// -v_t = -v + v (n.v), taken when mean(v_t) > 0, has d/dv = (n.v - 1) I + v n^T.
+// The branch tests repeat the forward arithmetic operation by operation.
+__device__ __forceinline__ void wall_adjoint(float diff, float4 n, float4 v, float3 fb, const StepParams& P,
+                                             float3& pb, float3& vb) {
+    if (!(diff > P.eps)) return;
+    const float3 nn = xyz(n);
+    const float nf = dot(nn, fb);
+    pb = pb - (P.kwall * nf) * nn;
+    vb = vb - (P.cwall * nf) * nn;
+    float4 vv = v;
+    vv.w = 0.f;
+    const float s = sphk::v4dot(n, vv);
+    const float4 vt = sphk::v4sub(vv, sphk::v4scale(vv, s));
+    const float mean = __fdiv_rn(__fadd_rn(__fadd_rn(vt.x, vt.y), vt.z), 3.0f);
+    if (mean > 0.f) vb = vb + (s - 1.f) * fb + dot(xyz(vv), fb) * nn;
+}
+
+__global__ void __launch_bounds__(256) k_adj_integrate(int n, StepParams P, float dt, TapeStep T,
+                                                       const float4* __restrict__ xb_out,
+                                                       const float4* __restrict__ vb_out,
+                                                       const float4* __restrict__ eb_out, float4* __restrict__ vb_in,
+                                                       float4* __restrict__ adj_a, float4* __restrict__ adj_x,
+                                                       float4* __restrict__ pbar) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = __ldg(T.idx + i);
+    const float isc = P.unit_scale ? 1.f : 1.f / P.sc;
+    const float3 pbn = isc * xyz(__ldg(xb_out + o));  // adjoint of p' = p + dt vn
+    const float3 vbo = xyz(__ldg(vb_out + o));
+    const float3 ebo = xyz(__ldg(eb_out + o));
+    const float3 vnb = vbo + dt * pbn + 0.5f * ebo;  // adjoint of vn
+    float3 pb = pbn;
+    float3 vb = 0.5f * ebo + vnb;
+    float3 gb = dt * vnb;
+    const float4 pd = __ldg(T.rec_pd + i);
+    const float4 p4 = make_float4(pd.x, pd.y, pd.z, pd.w);
+    const float4 v = __ldg(T.vin + i);
+    const float4 fs = __ldg(T.fsph + i);
+    // the forward's total force, bit for bit, for the clamp test
+    float4 g = sphk::collide_walls(p4, v, fs, P);
+    g = sphk::v4add(g, P.gravity);
+    g.w = 0.f;
+    const float speed = __fsqrt_rn(sphk::v4dot(g, g));
+    if (speed > P.vlimit) {
+        // g' = L g / |g|:  dg'/dg = (L / |g|) (I - u u^T), u = g / |g|
+        const float3 u = (1.f / speed) * xyz(g);
+        gb = (P.vlimit / speed) * (gb - dot(u, gb) * u);
+    }
+    const float3 fb = gb;
+    wall_adjoint(__fsub_rn(P.bound, __fsub_rn(p4.z, P.gs_bnd_min.z)), make_float4(0.f, 0.f, 1.f, 0.f), v, fb, P, pb,
+                 vb);
+    wall_adjoint(__fsub_rn(P.bound, __fsub_rn(P.gs_bnd_max.z, p4.z)), make_float4(0.f, 0.f, -1.f, 0.f), v, fb, P, pb,
+                 vb);
+    wall_adjoint(__fsub_rn(P.bound, __fsub_rn(p4.y, P.gs_bnd_min.y)), make_float4(0.f, 1.f, 0.f, 0.f), v, fb, P, pb,
+                 vb);
+    wall_adjoint(__fsub_rn(P.bound, __fsub_rn(P.gs_bnd_max.y, p4.y)), make_float4(0.f, -1.f, 0.f, 0.f), v, fb, P, pb,
+                 vb);
+    wall_adjoint(__fsub_rn(P.bound, __fsub_rn(p4.x, P.gs_bnd_min.x)), make_float4(1.f, 0.f, 0.f, 0.f), v, fb, P, pb,
+                 vb);
+    wall_adjoint(__fsub_rn(P.bound, __fsub_rn(P.gs_bnd_max.x, p4.x)), make_float4(-1.f, 0.f, 0.f, 0.f), v, fb, P, pb,
+                 vb);
+    const float rho = pd.w;
+    const float A = P.mass * __ldg(T.rec_vi + i).w;
+    // f_sph = A * (...):  rho enters through A = m / rho
+    const float rhob_a = -dot(fb, xyz(fs)) / rho;
+    const float3 a = A * fb;
+    const float3 xb = (P.coef_d * P.xsph_factor) * vnb;
+    adj_a[i] = make_float4(a.x, a.y, a.z, rhob_a);
+    adj_x[i] = make_float4(xb.x, xb.y, xb.z, 0.f);
+    pbar[i] = make_float4(pb.x, pb.y, pb.z, 0.f);
+    vb_in[o] = make_float4(vb.x, vb.y, vb.z, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// Neighbours of sorted particle i as the forward density pass recorded them:
+// the bitmask over the first kMaskBits candidates in walk order, the rest
+// tested again.  Lanes advance in lock step, one neighbour each per
+// iteration (the forward force pass's scheme); fn(j) runs for each j != i.
+// Particles outside the integer-hash range walk the 27 cells directly.
+template <class Fn>
+__device__ __forceinline__ void for_each_neighbour(const StepParams& P, const TapeStep& T, size_t mstride, int i,
+                                                   const float4& pi, unsigned wmask, uint32_t (*s_rs)[kAdjThreads],
+                                                   uint32_t (*s_off)[kAdjThreads], Fn&& fn) {
+    const int t = threadIdx.x;
+    const float rc2 = P.rcut2;
+    int nrows = 0;
+    uint32_t M = 0;
+    const int3 c = sphk::grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
+    if (sphk::cell_fast(P, c)) {
+        sphk::walk_rows_fast(P, T.cs, T.ce, c, [&](uint32_t rs, uint32_t re) {
+            s_rs[nrows][t] = rs;
+            s_off[nrows][t] = M;
+            M += re - rs;
+            ++nrows;
+        });
+    } else {
+        sphk::walk_rows_slow(P, T.cs, T.ce, c, [&](uint32_t rs, uint32_t re) {
+            for (uint32_t j = rs; j < re; ++j) {
+                const float4 pj = __ldg(T.rec_pd + j);
+                const float r2 = sphk::dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
+                if (r2 <= rc2 && j != (uint32_t)i) fn(j);
+            }
+        });
+    }
+    s_off[nrows][t] = M;
+    const uint32_t* mrow = T.mask + i;
+    const uint32_t mbits = M < (uint32_t)sphk::kMaskBits ? M : (uint32_t)sphk::kMaskBits;
+    uint32_t w = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
+    uint32_t q = (uint32_t)sphk::kMaskBits;
+    int r = 0;
+    for (;;) {
+        bool have = false;
+        uint32_t p = 0;
+        while (m == 0 && (w + 1) * 32u < mbits) {
+            ++w;
+            m = __ldg(mrow + (size_t)w * mstride);
+        }
+        if (m != 0) {
+            p = w * 32u + (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+            have = true;
+        } else {
+            while (q < M) {
+                const uint32_t pp = q++;
+                while (pp >= s_off[r + 1][t]) ++r;
+                const uint32_t j = s_rs[r][t] + (pp - s_off[r][t]);
+                const float4 pj = __ldg(T.rec_pd + j);
+                const float r2 = sphk::dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
+                if (r2 <= rc2 && j != (uint32_t)i) {
+                    p = pp;
+                    have = true;
+                    break;
+                }
+            }
+        }
+        if (!__any_sync(wmask, have)) break;
+        if (have) {
+            while (p >= s_off[r + 1][t]) ++r;
+            fn(s_rs[r][t] + (p - s_off[r][t]));
+        }
+    }
+}
+
+// Sum over the warp, added once per warp to a double accumulator.
+__device__ __forceinline__ void warp_add_double(double* acc, float v) {
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+    if ((threadIdx.x & 31) == 0 && v != 0.f) atomicAdd(acc, (double)v);
+}
+
+// ---------------------------------------------------------------------------
+// B: pressure, viscosity and XSPH pair terms.  Thread k, neighbour j,
+// d = p_k - p_j, r = max(|d|, EPSILON):
+//   d phi / d d = psi d,   psi = -(h - r)(h + r) / r^3   (0 when clamped)
+//   d r / d d   = d / r                                  (0 when clamped)
+//   d w / d d   = -6 (h^2 - q)^2 d
+// i-side: the derivatives of k's own sums F_k, V_k, X_k (adjoints cb a_k,
+// mu cv a_k, xbar_k) with respect to p_k, e_k and rho_k; j-side: those of
+// j's sums with respect to the same variables of k.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_force(int n, StepParams P, TapeStep T, size_t mstride,
+                                                           const float4* __restrict__ adj_a,
+                                                           const float4* __restrict__ adj_x,
+                                                           float4* __restrict__ pbar, float* __restrict__ rhob_out,
+                                                           float4* __restrict__ eb_in, double* __restrict__ visc_acc) {
+    __shared__ uint32_t s_rs[9][kAdjThreads];
+    __shared__ uint32_t s_off[10][kAdjThreads];
+    const int k = blockIdx.x * kAdjThreads + threadIdx.x;
+    const bool live = k < n;
+    const unsigned wmask = __ballot_sync(0xffffffffu, live);
+    float visc_part = 0.f;
+    if (live) {
+        const float4 pk = __ldg(T.rec_pd + k);
+        const float4 vk = __ldg(T.rec_vi + k);
+        const float4 ak4 = __ldg(adj_a + k);
+        const float3 ak = xyz(ak4), xk = xyz(__ldg(adj_x + k)), ek = xyz(vk);
+        const float dk = pk.w, idk = vk.w;
+        const float Pk = P.K * (dk - P.rho0);
+        const float cb = P.coef_b, cs = P.coef_s;
+        float3 pb = make_float3(0.f, 0.f, 0.f), eb = pb, Vs = pb;
+        float rhob = 0.f;
+        for_each_neighbour(P, T, mstride, k, pk, wmask, s_rs, s_off, [&](uint32_t j) {
+            const float4 pj = __ldg(T.rec_pd + j);
+            const float4 vj = __ldg(T.rec_vi + j);
+            const float3 aj = xyz(__ldg(adj_a + j)), xj = xyz(__ldg(adj_x + j));
+            const float3 d = make_float3(pk.x - pj.x, pk.y - pj.y, pk.z - pj.z);
+            const float q = dot(d, d);
+            const float rt = sqrtf(q);
+            const bool clamped = !(rt >= P.eps);
+            const float rr = clamped ? P.eps : rt;
+            const float ir = 1.f / rr;
+            const float hr = P.h - rr;
+            const float hq = P.h2 - q;
+            const float w = hq * hq * hq;
+            const float wd = -6.f * hq * hq;
+            const float phi = hr * hr * ir;
+            const float psi = clamped ? 0.f : -hr * (P.h + rr) * ir * ir * ir;
+            const float gr = clamped ? 0.f : ir;
+            const float dj = pj.w, idj = vj.w;
+            const float Pj = P.K * (dj - P.rho0);
+            const float isum = 1.f / (dk + dj);
+            const float3 de = xyz(vj) - ek;
+            const float skj = (Pk + Pj) * idj, sjk = (Pj + Pk) * idk;
+            const float cFk = cb * dot(ak, d), cFj = cb * dot(aj, d);
+            const float cVk = cs * dot(ak, de), cVj = cs * dot(aj, de);
+            const float cXk = dot(xk, de), cXj = dot(xj, de);
+            // positions
+            const float sd = psi * (skj * cFk - sjk * cFj) + gr * (cVj * idk - cVk * idj) + wd * isum * (cXk - cXj);
+            pb = pb + sd * d + (phi * cb) * (skj * ak - sjk * aj);
+            // veleval
+            eb = eb + (hr * idk * cs) * aj - (hr * idj * cs) * ak + (w * isum) * (xj - xk);
+            // density
+            rhob += P.K * phi * idj * cFk + phi * cFj * idk * ((Pj + Pk) * idk - P.K) + hr * cVj * idk * idk +
+                    w * isum * isum * (cXj - cXk);
+            Vs = Vs + (hr * idj) * de;
+        });
+        const float4 p0 = pbar[k];
+        pbar[k] = make_float4(p0.x + pb.x, p0.y + pb.y, p0.z + pb.z, 0.f);
+        rhob_out[k] = ak4.w + rhob;
+        eb_in[__ldg(T.idx + k)] = make_float4(eb.x, eb.y, eb.z, 0.f);
+        visc_part = P.wvisc_dd * dot(ak, Vs);
+    }
+    warp_add_double(visc_acc, visc_part);
+}
+
+// ---------------------------------------------------------------------------
+// C: density position terms.  rho_k and rho_j both hold w(|p_k - p_j|^2):
+// pbar_k += Dc * (-6 (h^2 - q)^2) * (rhobar_k + rhobar_j) * d.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_density(int n, StepParams P, TapeStep T, size_t mstride,
+                                                             const float* __restrict__ rhob,
+                                                             const float4* __restrict__ pbar,
+                                                             float4* __restrict__ xb_in) {
+    __shared__ uint32_t s_rs[9][kAdjThreads];
+    __shared__ uint32_t s_off[10][kAdjThreads];
+    const int k = blockIdx.x * kAdjThreads + threadIdx.x;
+    const bool live = k < n;
+    const unsigned wmask = __ballot_sync(0xffffffffu, live);
+    if (!live) return;
+    const float4 pk = __ldg(T.rec_pd + k);
+    const float rk = __ldg(rhob + k);
+    float3 pb = make_float3(0.f, 0.f, 0.f);
+    for_each_neighbour(P, T, mstride, k, pk, wmask, s_rs, s_off, [&](uint32_t j) {
+        const float4 pj = __ldg(T.rec_pd + j);
+        const float3 d = make_float3(pk.x - pj.x, pk.y - pj.y, pk.z - pj.z);
+        const float hq = P.h2 - dot(d, d);
+        pb = pb + (-6.f * hq * hq * (rk + __ldg(rhob + j))) * d;
+    });
+    const float4 p0 = pbar[k];
+    const float s = P.unit_scale ? 1.f : P.sc;
+    const float3 x = s * (xyz(p0) + P.dens_coef * pb);
+    xb_in[__ldg(T.idx + k)] = make_float4(x.x, x.y, x.z, 0.f);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct sph_adjoint {
+    // recorded rollout
+    int recorded = 0;
+    int nsteps = 0, K = 0, n = 0, exact = 0;
+    float dt = 0.f;
+    unsigned params_version = 0;
+    // capacity
+    int cap_K = 0, cap_ckpt = 0;
+    float4* ckpt = nullptr;  // [cap_ckpt][3][max_num]: pos, vel, veleval at steps 0, K, 2K, ..., then the final state
+    // tape [cap_K] slots
+    uint32_t* t_idx = nullptr;
+    uint32_t* t_cs = nullptr;
+    uint32_t* t_ce = nullptr;
+    float4* t_pd = nullptr;
+    float4* t_vi = nullptr;
+    uint32_t* t_mask = nullptr;
+    float4* t_f = nullptr;
+    float4* t_v = nullptr;
+    // adjoint state, original order (ping-pong) and per sorted particle
+    float4* xb[2] = {nullptr, nullptr};
+    float4* vb[2] = {nullptr, nullptr};
+    float4* eb[2] = {nullptr, nullptr};
+    float4* adj_a = nullptr;
+    float4* adj_x = nullptr;
+    float4* pbar = nullptr;
+    float* rhob = nullptr;
+    double* visc_acc = nullptr;
+    double* host_visc = nullptr;
+    // backward graph and the configuration it was captured for
+    cudaGraphExec_t graph = nullptr;
+    int g_nsteps = -1, g_K = -1, g_n = -1, g_exact = -1;
+    float g_dt = 0.f;
+    unsigned g_version = 0;
+    cudaStream_t g_stream = nullptr;
+};
+
+namespace {
+
+void free_tape(sph_adjoint* a) {
+    void* ptrs[] = {a->t_idx, a->t_cs, a->t_ce, a->t_pd, a->t_vi, a->t_mask, a->t_f, a->t_v};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    a->t_idx = a->t_cs = a->t_ce = a->t_mask = nullptr;
+    a->t_pd = a->t_vi = a->t_f = a->t_v = nullptr;
+    a->cap_K = 0;
+}
+
+void drop_graph(sph_adjoint* a) {
+    if (a->graph) cudaGraphExecDestroy(a->graph);
+    a->graph = nullptr;
+}
+
+int ensure_buffers(sph_ctx* c, int K, int nckpt) {
+    sph_adjoint* a = c->adj;
+    const size_t N = (size_t)c->max_num, C1 = (size_t)c->gp.nb_cells + 1;
+    if (!a->xb[0]) {
+        for (int s = 0; s < 2; ++s) {
+            CK(c, cudaMalloc((void**)&a->xb[s], N * 16));
+            CK(c, cudaMalloc((void**)&a->vb[s], N * 16));
+            CK(c, cudaMalloc((void**)&a->eb[s], N * 16));
+        }
+        CK(c, cudaMalloc((void**)&a->adj_a, N * 16));
+        CK(c, cudaMalloc((void**)&a->adj_x, N * 16));
+        CK(c, cudaMalloc((void**)&a->pbar, N * 16));
+        CK(c, cudaMalloc((void**)&a->rhob, N * 4));
+        CK(c, cudaMalloc((void**)&a->visc_acc, sizeof(double)));
+        CK(c, cudaMallocHost((void**)&a->host_visc, sizeof(double)));
+    }
+    if (nckpt > a->cap_ckpt) {
+        drop_graph(a);
+        if (a->ckpt) cudaFree(a->ckpt);
+        a->ckpt = nullptr;
+        a->cap_ckpt = 0;
+        CK(c, cudaMalloc((void**)&a->ckpt, (size_t)nckpt * 3 * N * 16));
+        a->cap_ckpt = nckpt;
+    }
+    if (K > a->cap_K) {
+        drop_graph(a);
+        free_tape(a);
+        const size_t k = (size_t)K;
+        CK(c, cudaMalloc((void**)&a->t_idx, k * N * 4));
+        CK(c, cudaMalloc((void**)&a->t_cs, k * C1 * 4));
+        CK(c, cudaMalloc((void**)&a->t_ce, k * C1 * 4));
+        CK(c, cudaMalloc((void**)&a->t_pd, k * N * 16));
+        CK(c, cudaMalloc((void**)&a->t_vi, k * N * 16));
+        CK(c, cudaMalloc((void**)&a->t_mask, k * N * 4 * sphk::kMaskWords));
+        CK(c, cudaMalloc((void**)&a->t_f, k * N * 16));
+        CK(c, cudaMalloc((void**)&a->t_v, k * N * 16));
+        a->cap_K = K;
+    }
+    return SPH_OK;
+}
+
+float4* ckpt_slot(sph_ctx* c, int slot, int field) {
+    return c->adj->ckpt + ((size_t)slot * 3 + field) * (size_t)c->max_num;
+}
+
+int copy_state(sph_ctx* c, int slot, bool save) {
+    const size_t b = (size_t)c->adj->n * 16;
+    float4* st[3] = {c->pos_u, c->vel_u, c->veleval_u};
+    for (int f = 0; f < 3; ++f) {
+        float4* ck = ckpt_slot(c, slot, f);
+        CK(c, cudaMemcpyAsync(save ? ck : st[f], save ? st[f] : ck, b, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return SPH_OK;
+}
+
+TapeStep tape_step(sph_ctx* c, int slot) {
+    sph_adjoint* a = c->adj;
+    const size_t N = (size_t)c->max_num, C1 = (size_t)c->gp.nb_cells + 1, s = (size_t)slot;
+    TapeStep T;
+    T.idx = a->t_idx + s * N;
+    T.cs = a->t_cs + s * C1;
+    T.ce = a->t_ce + s * C1;
+    T.rec_pd = a->t_pd + s * N;
+    T.rec_vi = a->t_vi + s * N;
+    T.mask = a->t_mask + s * N * sphk::kMaskWords;
+    T.fsph = a->t_f + s * N;
+    T.vin = a->t_v + s * N;
+    return T;
+}
+
+// One forward step whose records land in tape slot `slot`: the context's
+// record buffers are pointed at the slot for the enqueue and restored after.
+int enqueue_taped_step(sph_ctx* c, int slot) {
+    const TapeStep T = tape_step(c, slot);
+    float4 *rec_pd = c->rec_pd, *rec_vi = c->rec_vi;
+    uint32_t *mask = c->mask, *cs = c->cell_start, *ce = c->cell_end, *idx_a = c->idx_a;
+    c->rec_pd = const_cast<float4*>(T.rec_pd);
+    c->rec_vi = const_cast<float4*>(T.rec_vi);
+    c->mask = const_cast<uint32_t*>(T.mask);
+    c->cell_start = const_cast<uint32_t*>(T.cs);
+    c->cell_end = const_cast<uint32_t*>(T.ce);
+    c->idx_a = const_cast<uint32_t*>(T.idx);
+    c->keep_f = const_cast<float4*>(T.fsph);
+    c->keep_v = const_cast<float4*>(T.vin);
+    const int rc = enqueue_fused_step(c, c->adj->dt);
+    c->rec_pd = rec_pd;
+    c->rec_vi = rec_vi;
+    c->mask = mask;
+    c->cell_start = cs;
+    c->cell_end = ce;
+    c->idx_a = idx_a;
+    c->keys_cur = c->keys_a;
+    c->idx_cur = idx_a;
+    c->keep_f = nullptr;
+    c->keep_v = nullptr;
+    return rc;
+}
+
+// The reverse of one step: adjoints of the step's outputs in buffers `src`,
+// of its inputs into 1 - src.
+int enqueue_reverse_step(sph_ctx* c, int slot, int src) {
+    sph_adjoint* a = c->adj;
+    const TapeStep T = tape_step(c, slot);
+    const int n = a->n, dst = 1 - src;
+    const size_t mstride = (size_t)c->max_num;
+    const int b256 = (n + 255) / 256, b128 = (n + kAdjThreads - 1) / kAdjThreads;
+    k_adj_integrate<<<b256, 256, 0, c->stream>>>(n, c->P, a->dt, T, a->xb[src], a->vb[src], a->eb[src], a->vb[dst],
+                                                 a->adj_a, a->adj_x, a->pbar);
+    k_adj_force<<<b128, kAdjThreads, 0, c->stream>>>(n, c->P, T, mstride, a->adj_a, a->adj_x, a->pbar, a->rhob,
+                                                     a->eb[dst], a->visc_acc);
+    k_adj_density<<<b128, kAdjThreads, 0, c->stream>>>(n, c->P, T, mstride, a->rhob, a->pbar, a->xb[dst]);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+// The whole backward pass: for each segment, last first, restore its
+// checkpoint, recompute it into the tape, reverse it; then restore the final
+// state.  Starts from the adjoints in buffers 0; ends in buffers nsteps % 2.
+int enqueue_backward(sph_ctx* c) {
+    sph_adjoint* a = c->adj;
+    const int T = a->nsteps, K = a->K;
+    const int nseg = (T + K - 1) / K;
+    int src = 0, rc;
+    for (int s = nseg - 1; s >= 0; --s) {
+        const int t0 = s * K, t1 = (t0 + K < T) ? t0 + K : T;
+        if ((rc = copy_state(c, s, false))) return rc;
+        for (int t = t0; t < t1; ++t)
+            if ((rc = enqueue_taped_step(c, t - t0))) return rc;
+        for (int t = t1 - 1; t >= t0; --t) {
+            if ((rc = enqueue_reverse_step(c, t - t0, src))) return rc;
+            src = 1 - src;
+        }
+    }
+    return copy_state(c, nseg, false);
+}
+
+int adj_check(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->adj || !c->adj->recorded)
+        return set_err(c, SPH_ESTATE, "no recorded rollout: call sph_adjoint_record first");
+    if (c->adj->params_version != c->params_version || c->adj->exact != c->exact)
+        return set_err(c, SPH_ESTATE, "parameters changed since the rollout was recorded");
+    return SPH_OK;
+}
+
+}  // namespace
+
+void sph_adjoint_release(sph_ctx* c) {
+    sph_adjoint* a = c ? c->adj : nullptr;
+    if (!a) return;
+    drop_graph(a);
+    free_tape(a);
+    void* ptrs[] = {a->ckpt, a->xb[0], a->xb[1], a->vb[0], a->vb[1], a->eb[0], a->eb[1], a->adj_a, a->adj_x,
+                    a->pbar, a->rhob, a->visc_acc};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (a->host_visc) cudaFreeHost(a->host_visc);
+    delete a;
+    c->adj = nullptr;
+}
+
+extern "C" {
+
+int sph_adjoint_record(sph_ctx* c, float dt, int nsteps, int K) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (nsteps <= 0 || K <= 0 || !std::isfinite(dt))
+        return set_err(c, SPH_EINVAL, "sph_adjoint_record: bad arguments (nsteps=%d, K=%d)", nsteps, K);
+    if (!c->adj) c->adj = new sph_adjoint();
+    sph_adjoint* a = c->adj;
+    a->recorded = 0;
+    if ((rc = read_info(c))) return rc;
+    if (c->host_info[sphk::kOutStart] >= 0)
+        return set_err(c, SPH_ESTATE, "an out-of-grid deletion is pending; step once before recording");
+    const int n = c->host_info[sphk::kNum];
+    if (n <= 0) return set_err(c, SPH_ESTATE, "no particles to record");
+    if (K > nsteps) K = nsteps;
+    const int nseg = (nsteps + K - 1) / K;
+    if ((rc = ensure_buffers(c, K, nseg + 1))) return rc;
+    a->n = n;
+    a->dt = dt;
+    a->nsteps = nsteps;
+    a->K = K;
+    a->exact = c->exact;
+    a->params_version = c->params_version;
+    for (int s = 0; s < nseg; ++s) {
+        if ((rc = copy_state(c, s, true))) return rc;
+        const int steps = (s + 1) * K <= nsteps ? K : nsteps - s * K;
+        if ((rc = sph_step(c, dt, steps))) return rc;
+    }
+    if ((rc = copy_state(c, nseg, true))) return rc;
+    if ((rc = read_info(c))) return rc;
+    const int out = c->host_info[sphk::kOutStart], now = c->host_info[sphk::kNum];
+    if (now != n || out >= 0)
+        return set_err(c, SPH_EOOB, "particles left the grid during the rollout; its gradient is not defined");
+    a->recorded = 1;
+    return SPH_OK;
+}
+
+int sph_adjoint_backward(sph_ctx* c, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
+                         const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0,
+                         sph_float4* dL_dveleval0, double* dL_dvisc) {
+    int rc = adj_check(c);
+    if (rc) return rc;
+    sph_adjoint* a = c->adj;
+    const size_t b = (size_t)a->n * 16;
+    if (dL_dpos)
+        CK(c, cudaMemcpyAsync(a->xb[0], dL_dpos, b, cudaMemcpyDeviceToDevice, c->stream));
+    else
+        CK(c, cudaMemsetAsync(a->xb[0], 0, b, c->stream));
+    if (dL_dvel)
+        CK(c, cudaMemcpyAsync(a->vb[0], dL_dvel, b, cudaMemcpyDeviceToDevice, c->stream));
+    else
+        CK(c, cudaMemsetAsync(a->vb[0], 0, b, c->stream));
+    if (dL_dveleval)
+        CK(c, cudaMemcpyAsync(a->eb[0], dL_dveleval, b, cudaMemcpyDeviceToDevice, c->stream));
+    else
+        CK(c, cudaMemsetAsync(a->eb[0], 0, b, c->stream));
+    CK(c, cudaMemsetAsync(a->visc_acc, 0, sizeof(double), c->stream));
+    const bool stale = !a->graph || a->g_nsteps != a->nsteps || a->g_K != a->K || a->g_n != a->n ||
+                       a->g_exact != a->exact || a->g_dt != a->dt || a->g_version != a->params_version ||
+                       a->g_stream != c->stream;
+    if (stale) {
+        drop_graph(a);
+        cudaGraph_t g = nullptr;
+        CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        rc = enqueue_backward(c);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return set_err(c, SPH_ECUDA, "backward graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&a->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            a->graph = nullptr;
+            return set_err(c, SPH_ECUDA, "backward graph instantiate: %s", cudaGetErrorString(e));
+        }
+        a->g_nsteps = a->nsteps;
+        a->g_K = a->K;
+        a->g_n = a->n;
+        a->g_exact = a->exact;
+        a->g_dt = a->dt;
+        a->g_version = a->params_version;
+        a->g_stream = c->stream;
+    }
+    CK(c, cudaGraphLaunch(a->graph, c->stream));
+    const int fin = a->nsteps & 1;
+    if (dL_dpos0) CK(c, cudaMemcpyAsync(dL_dpos0, a->xb[fin], b, cudaMemcpyDeviceToDevice, c->stream));
+    if (dL_dvel0) CK(c, cudaMemcpyAsync(dL_dvel0, a->vb[fin], b, cudaMemcpyDeviceToDevice, c->stream));
+    if (dL_dveleval0) CK(c, cudaMemcpyAsync(dL_dveleval0, a->eb[fin], b, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(a->host_visc, a->visc_acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if ((rc = read_info(c))) return rc;
+    if (dL_dvisc) *dL_dvisc = *a->host_visc;
+    return SPH_OK;
+}
+
+int sph_adjoint_rollout(sph_ctx* c, int nsteps, int K, const sph_float4* dL_dpos_final, sph_float4* dL_dvel0,
+                        float* dL_dvisc) {
+    int rc = adj_check(c);
+    if (rc) return rc;
+    const int k_eff = K > c->adj->nsteps ? c->adj->nsteps : K;
+    if (nsteps != c->adj->nsteps || k_eff != c->adj->K)
+        return set_err(c, SPH_EINVAL, "sph_adjoint_rollout: (nsteps=%d, K=%d) differ from the recorded (%d, %d)",
+                       nsteps, K, c->adj->nsteps, c->adj->K);
+    double v = 0.0;
+    rc = sph_adjoint_backward(c, dL_dpos_final, nullptr, nullptr, nullptr, dL_dvel0, nullptr, &v);
+    if (rc == SPH_OK && dL_dvisc) *dL_dvisc = (float)v;
+    return rc;
+}
+
+}  // extern "C"

@@ -9,54 +9,13 @@
 #include <cstring>
 #include <string>
 
-#include "sph_device.cuh"
+#include "sph_ctx.cuh"
 
 using sphk::StepParams;
 
-struct sph_ctx {
-    int device = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    SPHParams sp;
-    GridParams gp, gps;
-    StepParams P;
-    int max_num = 0;
-    int num_hint = 0;  // host upper bound of the particle count (grid sizing)
-    int passes = 1;
-    int exact = 0;
-    // device state
-    float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr;
-    float4 *pos_s = nullptr, *vel_s = nullptr, *veleval_s = nullptr, *force_s = nullptr, *xsph_s = nullptr;
-    float4 *del_pos = nullptr, *del_vel = nullptr;
-    float* density = nullptr;
-    float4* rec_pd = nullptr;    // (scaled pos, rho) per sorted particle
-    float4* rec_vi = nullptr;    // (veleval, 1/rho) per sorted particle
-    int* fctr = nullptr;         // force tile counters [nsm + 1]
-    int nsm = 1;
-    uint32_t* nbr = nullptr;
-    uint32_t* mask = nullptr;    // neighbour bitmask [kMaskWords][max_num]
-    uint32_t *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
-    uint32_t *keys_cur = nullptr, *idx_cur = nullptr;  // what SORT_HASHES / SORT_INDICES show
-    uint32_t *cell_start = nullptr, *cell_end = nullptr;
-    int* info = nullptr;
-    uint32_t* scratch = nullptr;
-    size_t scratch_words = 0;
-    uint32_t* hist = nullptr;    // [4][256]
-    uint32_t* status = nullptr;  // [passes][tiles][256]
-    int tiles_cap = 0;
-    int* host_info = nullptr;  // pinned
-    // graph of one fused step
-    cudaGraphExec_t graph = nullptr;
-    float graph_dt = 0.f;
-    int graph_num = -1;
-    int graph_exact = -1;
-    unsigned params_version = 1, graph_version = 0;
-    std::string err;
-};
-
 static std::string g_create_error;
 
-static int set_err(sph_ctx* c, int code, const char* fmt, ...) {
+int set_err(sph_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -68,18 +27,6 @@ static int set_err(sph_ctx* c, int code, const char* fmt, ...) {
         g_create_error = buf;
     return code;
 }
-
-#define CK(ctx, call)                                                                                 \
-    do {                                                                                              \
-        cudaError_t e_ = (call);                                                                      \
-        if (e_ != cudaSuccess) return set_err(ctx, SPH_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
-    } while (0)
-
-#define CK_LAUNCH(ctx)                                                                                       \
-    do {                                                                                                     \
-        cudaError_t e_ = cudaGetLastError();                                                                 \
-        if (e_ != cudaSuccess) return set_err(ctx, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
-    } while (0)
 
 namespace {
 
@@ -259,9 +206,10 @@ int field_capacity(sph_ctx* c, int field) {
 }
 
 void free_all(sph_ctx* c) {
+    sph_adjoint_release(c);
     if (c->graph) cudaGraphExecDestroy(c->graph);
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
-                    c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->fctr, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
+                    c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
                     c->cell_start, c->cell_end, c->info, c->scratch};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -319,9 +267,12 @@ void density_launch(sph_ctx* c, const uint32_t* idx, bool with_deletion, cudaStr
 
 void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {
     sphk::launch_force(c->pos_s, c->rec_pd, c->rec_vi, c->mask, (size_t)c->max_num, c->cell_start, c->cell_end,
-                       c->info, c->fctr, c->nsm, c->force_s, c->xsph_s, idx, c->vel_s, c->pos_u, c->vel_u,
-                       c->veleval_u, c->P, dt, fused ? 1 : 0, c->exact, c->num_hint, st);
+                       c->info, c->force_s, c->xsph_s, idx, c->vel_s, c->pos_u, c->vel_u, c->veleval_u,
+                       fused ? c->keep_f : nullptr, fused ? c->keep_v : nullptr, c->P, dt, fused ? 1 : 0, c->exact,
+                       c->num_hint, st);
 }
+
+}  // namespace
 
 int enqueue_fused_step(sph_ctx* c, float dt) {
     int rc = enqueue_hash(c);
@@ -352,7 +303,6 @@ int check_ctx(sph_ctx* c) {
     return SPH_OK;
 }
 
-}  // namespace
 
 extern "C" {
 
@@ -391,9 +341,6 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
         delete c;
         return set_err(nullptr, SPH_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     }
-    int nsm = 1;
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm < 1) nsm = 1;
-    c->nsm = nsm > 1000 ? 1000 : nsm;
     const int total_bits = bit_width((uint32_t)c->gp.nb_cells);
     c->passes = (total_bits + 7) / 8;
     if (c->passes < 1) c->passes = 1;
@@ -424,7 +371,6 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->nbr, N * 4);
     ALLOC(c->rec_pd, N * 16);
     ALLOC(c->rec_vi, N * 16);
-    ALLOC(c->fctr, sizeof(int) * 1024);
     ALLOC(c->mask, N * 4 * sphk::kMaskWords);
     ALLOC(c->keys_a, N * 4);
     ALLOC(c->idx_a, N * 4);
@@ -461,7 +407,6 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     cudaMemsetAsync(c->nbr, 0, N * 4, st);
     cudaMemsetAsync(c->rec_pd, 0, N * 16, st);
     cudaMemsetAsync(c->rec_vi, 0, N * 16, st);
-    cudaMemsetAsync(c->fctr, 0, sizeof(int) * 1024, st);
     cudaMemsetAsync(c->mask, 0, N * 4 * sphk::kMaskWords, st);
     fill_u32(c->keys_a, N, 0x7fffffffu, st);
     fill_u32(c->idx_a, N, 0x7fffffffu, st);

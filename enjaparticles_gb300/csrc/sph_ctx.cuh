@@ -1,0 +1,79 @@
+// sph_ctx.cuh — the single-system context behind the sph_ctx* handle of
+// include/rtps_sph.h, shared by the translation units that drive it
+// (sph_api.cu: buffers, stages and the step graph; sph_adjoint.cu: the
+// differentiable rollout).
+#pragma once
+
+#include <string>
+
+#include "sph_device.cuh"
+
+struct sph_adjoint;  // recorded rollout and its buffers (sph_adjoint.cu)
+
+struct sph_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    SPHParams sp;
+    GridParams gp, gps;
+    sphk::StepParams P;
+    int max_num = 0;
+    int num_hint = 0;  // host upper bound of the particle count (grid sizing)
+    int passes = 1;
+    int exact = 0;
+    // device state
+    float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr;
+    float4 *pos_s = nullptr, *vel_s = nullptr, *veleval_s = nullptr, *force_s = nullptr, *xsph_s = nullptr;
+    float4 *del_pos = nullptr, *del_vel = nullptr;
+    float* density = nullptr;
+    float4* rec_pd = nullptr;    // (scaled pos, rho) per sorted particle
+    float4* rec_vi = nullptr;    // (veleval, 1/rho) per sorted particle
+    uint32_t* nbr = nullptr;
+    uint32_t* mask = nullptr;    // neighbour bitmask [kMaskWords][max_num]
+    uint32_t *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
+    uint32_t *keys_cur = nullptr, *idx_cur = nullptr;  // what SORT_HASHES / SORT_INDICES show
+    uint32_t *cell_start = nullptr, *cell_end = nullptr;
+    int* info = nullptr;
+    uint32_t* scratch = nullptr;
+    size_t scratch_words = 0;
+    uint32_t* hist = nullptr;    // [4][256]
+    uint32_t* status = nullptr;  // [passes][tiles][256]
+    int tiles_cap = 0;
+    int* host_info = nullptr;  // pinned
+    // When set, the fused step also stores, per sorted particle, the SPH
+    // force before the walls (keep_f) and the step's input velocity (keep_v):
+    // the tape of the differentiable rollout.
+    float4 *keep_f = nullptr, *keep_v = nullptr;
+    // graph of one fused step
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.f;
+    int graph_num = -1;
+    int graph_exact = -1;
+    unsigned params_version = 1, graph_version = 0;
+    sph_adjoint* adj = nullptr;
+    std::string err;
+};
+
+// Records the message (on the context, or as the last creation error when c
+// is null) and returns code.
+int set_err(sph_ctx* c, int code, const char* fmt, ...);
+// Makes the context's device current.
+int check_ctx(sph_ctx* c);
+// Enqueues one fused step (hash .. leapfrog) on c->stream.
+int enqueue_fused_step(sph_ctx* c, float dt);
+// Reads the device counters into c->host_info (synchronises the stream).
+int read_info(sph_ctx* c);
+// Frees the differentiable-rollout state of c (no-op when there is none).
+void sph_adjoint_release(sph_ctx* c);
+
+#define CK(ctx, call)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return set_err(ctx, SPH_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CK_LAUNCH(ctx)                                                                                       \
+    do {                                                                                                     \
+        cudaError_t e_ = cudaGetLastError();                                                                 \
+        if (e_ != cudaSuccess) return set_err(ctx, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+    } while (0)

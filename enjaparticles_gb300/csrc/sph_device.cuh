@@ -136,11 +136,12 @@ void launch_density(const float4* pos_s, const float4* veleval_s, float* density
                     const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
                     float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
                     cudaStream_t st);
-// tile_ctr: nsm + 1 ints, zero before the first launch; the kernel leaves them zero.
+// keep_f / keep_v (fused only, nullable): per sorted particle, the SPH force
+// before the walls and the velocity the step integrates.
 void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                   size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                  int* tile_ctr, int nsm, float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s,
-                  float4* pos_u, float4* vel_u, float4* veleval_u, const StepParams& p, float dt, int fused,
+                  float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
+                  float4* veleval_u, float4* keep_f, float4* keep_v, const StepParams& p, float dt, int fused,
                   int exact, int grid_items, cudaStream_t st);
 // Batch forms of the neighbour passes (fused force only).
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,

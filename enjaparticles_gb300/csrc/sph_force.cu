@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     const uint32_t* __restrict__ mask, const size_t mstride, const uint32_t* __restrict__ cs0,
     const uint32_t* __restrict__ ce0, const int* __restrict__ info, float4* __restrict__ force_s,
     float4* __restrict__ xsph_s, uint32_t* __restrict__ idx, const float4* __restrict__ vel_s,
-    float4* __restrict__ pos_u, float4* __restrict__ vel_u, float4* __restrict__ veleval_u, const Scenes R,
-    const float dt) {
+    float4* __restrict__ pos_u, float4* __restrict__ vel_u, float4* __restrict__ veleval_u,
+    float4* __restrict__ keep_f, float4* __restrict__ keep_v, const Scenes R, const float dt) {
     // Row table of each thread: sorted index of the run's first candidate and
     // walk-order offset of it; rows without candidates are left out.
     __shared__ uint32_t s_rs[9][kForceThreads];
@@ -205,6 +205,10 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
         orig = __ldg(idx + i);
         v = vel_u[orig];
     }
+    if (keep_f != nullptr) {
+        keep_f[i] = f;
+        keep_v[i] = v;
+    }
     const float4 pp = __ldg(pos_s + i);
     const float4 psc = Unit ? pp : v4scale(pp, P.sc);
     f = collide_walls(psc, v, f, P);
@@ -219,14 +223,15 @@ template <class Scenes>
 void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                     size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                     float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
-                    float4* veleval_u, const Scenes& R, bool unit, float dt, int fused, int exact, int grid_items,
-                    cudaStream_t st) {
+                    float4* veleval_u, float4* keep_f, float4* keep_v, const Scenes& R, bool unit, float dt, int fused,
+                    int exact, int grid_items, cudaStream_t st) {
     int blocks = (grid_items + kForceThreads - 1) / kForceThreads;
     if (blocks < 1) blocks = 1;
 #define SPH_FORCE_LAUNCH(F, E, U)                                                                                   \
     k_force<F, E, U, Scenes><<<blocks, kForceThreads, 0, st>>>(pos_s, rec_pd, rec_vi, mask, mask_stride,           \
                                                                cell_start, cell_end, info, force_s, xsph_s, idx,  \
-                                                               vel_s, pos_u, vel_u, veleval_u, R, dt)
+                                                               vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, \
+                                                               R, dt)
     if (fused) {
         if (exact) {
             if (unit) SPH_FORCE_LAUNCH(true, true, true); else SPH_FORCE_LAUNCH(true, true, false);
@@ -245,11 +250,12 @@ void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec
 
 void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                   size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                  int* /*tile_ctr*/, int /*nsm*/, float4* force_s, float4* xsph_s, uint32_t* idx,
-                  const float4* vel_s, float4* pos_u, float4* vel_u, float4* veleval_u, const StepParams& p,
-                  float dt, int fused, int exact, int grid_items, cudaStream_t st) {
+                  float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
+                  float4* veleval_u, float4* keep_f, float4* keep_v, const StepParams& p, float dt, int fused,
+                  int exact, int grid_items, cudaStream_t st) {
     launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, cell_end, info, force_s, xsph_s, idx, vel_s,
-                   pos_u, vel_u, veleval_u, OneScene{p}, p.unit_scale != 0, dt, fused, exact, grid_items, st);
+                   pos_u, vel_u, veleval_u, keep_f, keep_v, OneScene{p}, p.unit_scale != 0, dt, fused, exact,
+                   grid_items, st);
 }
 
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
@@ -257,7 +263,7 @@ void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4*
                         uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const ManyScenes& scenes,
                         bool unit, float dt, int exact, int grid_items, cudaStream_t st) {
     launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, cell_end, info, nullptr, nullptr, idx,
-                   nullptr, pos_u, vel_u, veleval_u, scenes, unit, dt, 1, exact, grid_items, st);
+                   nullptr, pos_u, vel_u, veleval_u, nullptr, nullptr, scenes, unit, dt, 1, exact, grid_items, st);
 }
 
 }  // namespace sphk

@@ -68,3 +68,32 @@ def dambreak(n, scene=0, velocity_sigma=0.0, velocity_seed=11):
     if velocity_sigma > 0:
         vel[:, :3] = normal(velocity_seed, 3 * n, velocity_sigma).reshape(n, 3).astype(np.float32)
     return pos, vel
+
+
+def rollout_case(n=65536, velocity_sigma=0.1, target_sigma=0.05, target_viscosity=0.03):
+    """The differentiable-rollout scene: the dam-break lattice of n particles
+    with initial velocities N(0, velocity_sigma^2) per component (seed 11), and
+    the initial velocities of its target run, those plus N(0, target_sigma^2)
+    (seed 12), to be rolled out with viscosity target_viscosity.
+
+    Returns (pos, vel0, vel0_target, target_viscosity), float32 (n, 4) arrays.
+    """
+    pos, vel = dambreak(n, scene=0, velocity_sigma=velocity_sigma, velocity_seed=11)
+    vt = vel.copy()
+    vt[:, :3] += normal(12, 3 * n, target_sigma).reshape(n, 3).astype(np.float32)
+    return pos, vel, vt, float(target_viscosity)
+
+
+def sample_coordinates(n, count, seed=13, offset=0):
+    """`count` distinct (particle, axis) pairs drawn uniformly (seeded)."""
+    out, k = [], offset
+    seen = set()
+    while len(out) < count:
+        u = uniform(seed, 1, offset=k)[0]
+        k += 1
+        c = int(u * 3 * n)
+        if c in seen:
+            continue
+        seen.add(c)
+        out.append((c // 3, c % 3))
+    return out, k

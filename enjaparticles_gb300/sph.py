@@ -156,6 +156,22 @@ class SPH:
     def sync(self):
         self._ck(self.lib.sph_sync(self.ctx))
 
+    # -- differentiable rollout ----------------------------------------------
+    def adjoint_record(self, dt, nsteps, K):
+        """Run nsteps steps keeping a checkpoint every K steps (sph_adjoint_record)."""
+        self._ck(self.lib.sph_adjoint_record(self.ctx, float(dt), int(nsteps), int(K)))
+
+    def adjoint_backward(self, dpos=None, dvel=None, dveleval=None, out_pos=None, out_vel=None, out_veleval=None):
+        """Backward pass of the recorded rollout (sph_adjoint_backward).
+
+        Arguments are DEVICE addresses (ints, e.g. torch's data_ptr()) of num
+        float4 in original particle order, or None.  Returns dL/dviscosity.
+        """
+        v = C.c_double()
+        self._ck(self.lib.sph_adjoint_backward(self.ctx, dpos, dvel, dveleval, out_pos, out_vel, out_veleval,
+                                               C.byref(v)))
+        return v.value
+
 
 def dambreak_system(n, viscosity=0.01, max_num=None, exact=False, velocity_sigma=0.0, scene=0):
     """An SPH system holding the dam-break scene of n particles."""

@@ -292,6 +292,40 @@ int sph_sync(sph_ctx* ctx);
 int sph_last_error(sph_ctx* ctx, char* buf, int len);
 
 /* ---------------------------------------------------------------------------
+ * Differentiable rollout.  No counterpart in the reference.  Reverse-mode
+ * gradients of a loss of the final state of an nsteps-step rollout with
+ * respect to its initial state and the viscosity coefficient, through
+ * adjoints of density, force, wall collision and leapfrog; sorting and
+ * hashing are piecewise constant and not differentiated.  The wall and
+ * friction tests and the acceleration clamp are taken as the forward run
+ * took them (the gradient of the branch the trajectory is on).
+ * ------------------------------------------------------------------------- */
+
+/* Run nsteps fused steps from the current state (as sph_step), keeping the
+ * state every K steps (checkpoints).  Leaves the final state in the context.
+ * Needs a fixed particle set: SPH_EOOB when a particle leaves the grid during
+ * the rollout, SPH_ESTATE when a deletion is pending.  Blocking. */
+int sph_adjoint_record(sph_ctx* ctx, float dt, int nsteps, int K);
+
+/* Backward pass of the recorded rollout.  Inputs: the loss gradient with
+ * respect to the final pos_u / vel_u / veleval_u (NULL: zero); outputs: the
+ * gradient with respect to the initial ones (NULL: not wanted) and to
+ * SPHParams.viscosity (FP64 sum; NULL: not wanted).  All arrays are DEVICE
+ * pointers of num float4 in original particle order (w lanes ignored / 0).
+ * Recomputes each K-step segment from its checkpoint (tape memory: K *
+ * (132 * max_num + 8 * nb_cells) bytes) and leaves the context's state as
+ * the rollout's final state; the sort scratch buffers (SORT_HASHES) hold
+ * recomputation leftovers afterwards.  Blocking. */
+int sph_adjoint_backward(sph_ctx* ctx, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
+                         const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0,
+                         sph_float4* dL_dveleval0, double* dL_dvisc);
+
+/* The backward pass for a loss of the final positions only: dL_dvel0 (device,
+ * num float4) and *dL_dvisc (host).  nsteps and K must be those recorded. */
+int sph_adjoint_rollout(sph_ctx* ctx, int nsteps, int K, const sph_float4* dL_dpos_final,
+                        sph_float4* dL_dvel0, float* dL_dvisc);
+
+/* ---------------------------------------------------------------------------
  * Batches: many independent systems ("scenes", each with its own SPHParams,
  * grid and particle count) stepped together.  No counterpart in the
  * reference, which steps one system per SPH object.  All scenes share one

@@ -59,6 +59,9 @@ def oracle():
             "oracle_sim_last_nc": (_I, [_P]),
             "oracle_sim_get": (_I, [_P, _I, _P, _I]),
             "oracle_sim_deleted": (_I, [_P, _P, _P, _I]),
+            "oracle_rollout64": (_I, [_P, _P, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+            "oracle_rollout64_jvp": (_I, [_P, _P, C.c_double, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P,
+                                          _P, _P, _P]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -155,3 +158,45 @@ class OracleSim:
             out = np.empty((n, 4), np.float32)
         assert self.lib.oracle_sim_get(self.h, FIELD_IDS[field], ptr(out), n) == 0
         return out
+
+
+def rollout64(sphp, grid_scaled, pos, vel, dt, nsteps, viscosity=None, veleval=None, want_vel=False):
+    """FP64 rollout (state in double) from (n,3) or (n,4) arrays.
+
+    Returns (final positions (n,3) float64, final velocities or None,
+    branch signature, neighbour signature).  Raises if a particle left the grid.
+    """
+    lib = oracle()
+    p = np.ascontiguousarray(np.asarray(pos, np.float64)[:, :3])
+    v = np.ascontiguousarray(np.asarray(vel, np.float64)[:, :3])
+    e = None if veleval is None else np.ascontiguousarray(np.asarray(veleval, np.float64)[:, :3])
+    n = p.shape[0]
+    po = np.empty((n, 3), np.float64)
+    vo = np.empty((n, 3), np.float64) if want_vel else None
+    sb, sn = C.c_uint64(), C.c_uint64()
+    mu = float(sphp.viscosity) if viscosity is None else float(viscosity)
+    rc = lib.oracle_rollout64(C.addressof(sphp), C.addressof(grid_scaled), mu, float(dt), int(nsteps), n,
+                              ptr(p), ptr(v), ptr(e), ptr(po), ptr(vo), C.addressof(sb), C.addressof(sn))
+    if rc != 0:
+        raise RuntimeError("oracle_rollout64 failed (a particle left the grid?)")
+    return po, vo, sb.value, sn.value
+
+
+def rollout64_jvp(sphp, grid_scaled, pos, vel, dt, nsteps, dpos=None, dvel=None, dveleval=None, dvisc=0.0,
+                  viscosity=None, veleval=None):
+    """FP64 rollout on dual numbers: (final positions, their derivative along
+    the input direction (dpos, dvel, dveleval, dvisc)), both (n, 3) float64."""
+    lib = oracle()
+    c3 = lambda a: None if a is None else np.ascontiguousarray(np.asarray(a, np.float64)[:, :3])
+    p, v, e = c3(pos), c3(vel), c3(veleval)
+    dp, dv, de = c3(dpos), c3(dvel), c3(dveleval)
+    n = p.shape[0]
+    po = np.empty((n, 3), np.float64)
+    dpo = np.empty((n, 3), np.float64)
+    mu = float(sphp.viscosity) if viscosity is None else float(viscosity)
+    rc = lib.oracle_rollout64_jvp(C.addressof(sphp), C.addressof(grid_scaled), mu, float(dvisc), float(dt),
+                                  int(nsteps), n, ptr(p), ptr(v), ptr(e), ptr(dp), ptr(dv), ptr(de), ptr(po),
+                                  ptr(dpo))
+    if rc != 0:
+        raise RuntimeError("oracle_rollout64_jvp failed (a particle left the grid?)")
+    return po, dpo
