@@ -62,6 +62,11 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--serial-steps", type=int, default=10)
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-calibration", action="store_true")
+    ap.add_argument("--cal-scenes", type=int, default=64)
+    ap.add_argument("--cal-iters", type=int, default=50)
+    ap.add_argument("--cal-steps", type=int, default=100)
+    ap.add_argument("--cal-k", type=int, default=10)
     ap.add_argument("--adj-n", type=int, default=65536)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-k", type=int, default=20)
@@ -314,6 +319,53 @@ def bench_adjoint(args, torch):
             "tape_bytes": K * (132 * n + 8 * C1), "checkpoint_bytes": (steps // K + 2) * 48 * n}
 
 
+def bench_calibration(args, torch):
+    """Batched differentiable calibration: 64 dam-break scenes, N_s ~
+    U{8192..65536} (seed 21), hidden viscosities mu_s ~ U[0.005, 0.05]
+    (seed 22); targets = the final positions of 100-step runs with the hidden
+    viscosities; 50 batched gradient iterations on every mu_s from 0.02, each
+    a 100-step recorded rollout (checkpoint every 10 steps), the per-scene
+    loss and one batched backward pass.  value = scenes * iterations / s over
+    the whole loop."""
+    import time
+    import numpy as np
+    from enjaparticles_gb300 import abi, scenes
+    from enjaparticles_gb300.batch import Batch, dambreak_batch_scenes
+    from enjaparticles_gb300.calibrate import calibrate_viscosity
+    S, steps = args.cal_scenes, args.cal_steps
+    ns, _ = dambreak_batch_scenes(S, seed_n=21, n_lo=8192, n_hi=65536)
+    hidden = [float(np.float32(0.005 + u * 0.045)) for u in scenes.uniform(22, S)]
+    params = [abi.dambreak_params(n, mu) for n, mu in zip(ns, hidden)]
+    data = [scenes.dambreak(n, scene=k) for k, n in enumerate(ns)]
+    b = Batch(params, ns)
+    b.set_stream(torch.cuda.current_stream().cuda_stream)
+    for k, (pos, vel) in enumerate(data):
+        b.upload(k, pos, vel)
+    b.step(DT, steps)
+    tgt = np.zeros((b.nslots, 4), np.float32)
+    for k, off in enumerate(b.slot_offsets()):
+        tgt[off:off + ns[k]] = b.get(k, "pos_u")
+    target = torch.from_numpy(tgt).cuda()
+    for k, (pos, vel) in enumerate(data):
+        b.upload(k, pos, vel)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mu, hist = calibrate_viscosity(b, target.data_ptr(), [0.02] * S, iterations=args.cal_iters, nsteps=steps,
+                                   K=args.cal_k, dt=DT)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    b.close()
+    hidden = np.asarray(hidden)
+    err = np.abs(mu - hidden)
+    return {"metric": "scenes*iterations/s", "value": S * args.cal_iters / el, "scenes": S,
+            "particles": int(sum(ns)), "iterations": args.cal_iters, "steps": steps, "checkpoint_every": args.cal_k,
+            "seconds": el, "mu_abs_err_mean": float(err.mean()), "mu_abs_err_max": float(err.max()),
+            "mu_rel_err_median": float(np.median(err / hidden)), "mu_rel_err_max": float((err / hidden).max()),
+            "loss_first_median": float(np.median(hist[0][0])), "loss_last_median": float(np.median(hist[-1][0])),
+            "start_mu": 0.02,
+            "note": "host wall clock around the whole loop (rollouts, losses, backward passes, Adam on log mu)"}
+
+
 def config_block(n, c):
     return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001, "
                         "1000-step rollout config" % n,
@@ -454,6 +506,8 @@ def main():
         line["batched"] = bench_batched(args, torch)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = bench_adjoint(args, torch)
+    if rank == 0 and not args.no_calibration:
+        line["calibration"] = bench_calibration(args, torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(n, args.cpu_seconds)
     if rank == 0:

@@ -106,6 +106,16 @@ SIGNATURES = {
     "sph_batch_out_of_grid": (_I, [_P, C.POINTER(_I)]),
     "sph_batch_sync": (_I, [_P]),
     "sph_batch_last_error": (_I, [_P, C.c_char_p, _I]),
+    "sph_batch_set_params": (_I, [_P, _I, _P]),
+    "sph_batch_get_params": (_I, [_P, _I, _P]),
+    "sph_batch_get_device_ptr": (_I, [_P, _I, C.POINTER(_P)]),
+    "sph_batch_slot_offset": (_I, [_P, _I, C.POINTER(_I)]),
+    "sph_batch_adjoint_record": (_I, [_P, _F, _I, _I]),
+    "sph_batch_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "sph_batch_adjoint_rewind": (_I, [_P]),
+    "sph_batch_loss_mse": (_I, [_P, _P, _P, _P]),
+    "sph_adjoint_rewind": (_I, [_P]),
+    "sph_loss_mse": (_I, [_P, _P, _P, C.POINTER(C.c_double)]),
     "sph_sort_pairs_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P]),
     "sph_build_info": (C.c_char_p, []),
 }

@@ -25,6 +25,8 @@ class Batch:
             raise abi.SPHError(rc, buf.value.decode())
         self.nscenes = n
         self.num = [0] * n
+        self.max_num = [int(m) for m in max_num]
+        self.nslots = sum(self.max_num)
         if exact:
             self._ck(self.lib.sph_batch_set_exact(self.h, 1))
 
@@ -71,6 +73,54 @@ class Batch:
         c = C.c_int()
         self._ck(self.lib.sph_batch_out_of_grid(self.h, C.byref(c)))
         return c.value
+
+    # -- parameters and device views ------------------------------------------
+    def params(self, scene):
+        sp = abi.SPHParams()
+        self._ck(self.lib.sph_batch_get_params(self.h, int(scene), C.byref(sp)))
+        return sp
+
+    def set_params(self, scene, sp):
+        self._ck(self.lib.sph_batch_set_params(self.h, int(scene), C.byref(sp)))
+
+    def set_viscosity(self, scene, mu):
+        sp = self.params(scene)
+        sp.viscosity = float(mu)
+        self.set_params(scene, sp)
+
+    def device_ptr(self, field):
+        p = C.c_void_p()
+        self._ck(self.lib.sph_batch_get_device_ptr(self.h, abi.FIELDS[field], C.byref(p)))
+        return p.value
+
+    def slot_offsets(self):
+        out = []
+        for s in range(self.nscenes):
+            o = C.c_int()
+            self._ck(self.lib.sph_batch_slot_offset(self.h, s, C.byref(o)))
+            out.append(o.value)
+        return out
+
+    # -- differentiable rollout (device addresses in slot layout) ---------------
+    def adjoint_record(self, dt, nsteps, K):
+        self._ck(self.lib.sph_batch_adjoint_record(self.h, float(dt), int(nsteps), int(K)))
+
+    def adjoint_backward(self, dpos=None, dvel=None, dveleval=None, out_pos=None, out_vel=None, out_veleval=None):
+        """Returns dL/dviscosity per scene (list of floats)."""
+        g = (C.c_double * self.nscenes)()
+        self._ck(self.lib.sph_batch_adjoint_backward(self.h, dpos, dvel, dveleval, out_pos, out_vel, out_veleval,
+                                                     C.cast(g, C.c_void_p)))
+        return list(g)
+
+    def adjoint_rewind(self):
+        self._ck(self.lib.sph_batch_adjoint_rewind(self.h))
+
+    def loss_mse(self, target, grad):
+        """Per-scene mean squared distance of pos_u to target (device address,
+        slot layout); writes its gradient to grad (device address)."""
+        out = (C.c_double * self.nscenes)()
+        self._ck(self.lib.sph_batch_loss_mse(self.h, target, grad, C.cast(out, C.c_void_p)))
+        return list(out)
 
 
 def dambreak_batch_scenes(nscenes, seed_n=7, seed_mu=None, n_lo=2048, n_hi=32768, mu_lo=0.005, mu_hi=0.05):

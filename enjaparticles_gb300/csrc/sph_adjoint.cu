@@ -38,11 +38,16 @@
 // (position, rho) and (veleval, 1/rho) records, the neighbour bitmask, the
 // pre-wall force and the input velocity: 132 B per particle + 8 B per cell.
 // The whole backward pass is one CUDA graph.
+//
+// Batches (sph_batch_adjoint_*) run the same kernels over every scene of a
+// batch at once: the scene of a sorted particle comes from its tape key, the
+// viscosity gradient is accumulated per scene.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
 
+#include "sph_batch.cuh"
 #include "sph_ctx.cuh"
 #include "sph_walk.cuh"
 
@@ -54,6 +59,7 @@ constexpr int kAdjThreads = 128;
 
 struct TapeStep {
     const uint32_t* idx;
+    const uint32_t* keys;  // sort keys (batches: the scene of each sorted particle)
     const uint32_t* cs;
     const uint32_t* ce;
     const float4* rec_pd;  // (scaled position, rho)
@@ -91,7 +97,8 @@ __device__ __forceinline__ void wall_adjoint(float diff, float4 n, float4 v, flo
     if (mean > 0.f) vb = vb + (s - 1.f) * fb + dot(xyz(vv), fb) * nn;
 }
 
-__global__ void __launch_bounds__(256) k_adj_integrate(int n, StepParams P, float dt, TapeStep T,
+template <class Scenes>
+__global__ void __launch_bounds__(256) k_adj_integrate(int n, const Scenes R, float dt, TapeStep T,
                                                        const float4* __restrict__ xb_out,
                                                        const float4* __restrict__ vb_out,
                                                        const float4* __restrict__ eb_out, float4* __restrict__ vb_in,
@@ -99,6 +106,7 @@ __global__ void __launch_bounds__(256) k_adj_integrate(int n, StepParams P, floa
                                                        float4* __restrict__ pbar) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const StepParams& P = R.params(i);
     const uint32_t o = __ldg(T.idx + i);
     const float isc = P.unit_scale ? 1.f : 1.f / P.sc;
     const float3 pbn = isc * xyz(__ldg(xb_out + o));  // adjoint of p' = p + dt vn
@@ -154,8 +162,9 @@ __global__ void __launch_bounds__(256) k_adj_integrate(int n, StepParams P, floa
 // iteration (the forward force pass's scheme); fn(j) runs for each j != i.
 // Particles outside the integer-hash range walk the 27 cells directly.
 template <class Fn>
-__device__ __forceinline__ void for_each_neighbour(const StepParams& P, const TapeStep& T, size_t mstride, int i,
-                                                   const float4& pi, unsigned wmask, uint32_t (*s_rs)[kAdjThreads],
+__device__ __forceinline__ void for_each_neighbour(const StepParams& P, const uint32_t* cs, const uint32_t* ce,
+                                                   const TapeStep& T, size_t mstride, int i, const float4& pi,
+                                                   unsigned wmask, uint32_t (*s_rs)[kAdjThreads],
                                                    uint32_t (*s_off)[kAdjThreads], Fn&& fn) {
     const int t = threadIdx.x;
     const float rc2 = P.rcut2;
@@ -163,14 +172,14 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const Ta
     uint32_t M = 0;
     const int3 c = sphk::grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
     if (sphk::cell_fast(P, c)) {
-        sphk::walk_rows_fast(P, T.cs, T.ce, c, [&](uint32_t rs, uint32_t re) {
+        sphk::walk_rows_fast(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {
             s_rs[nrows][t] = rs;
             s_off[nrows][t] = M;
             M += re - rs;
             ++nrows;
         });
     } else {
-        sphk::walk_rows_slow(P, T.cs, T.ce, c, [&](uint32_t rs, uint32_t re) {
+        sphk::walk_rows_slow(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {
             for (uint32_t j = rs; j < re; ++j) {
                 const float4 pj = __ldg(T.rec_pd + j);
                 const float r2 = sphk::dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
@@ -217,11 +226,21 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const Ta
     }
 }
 
-// Sum over the warp, added once per warp to a double accumulator.
-__device__ __forceinline__ void warp_add_double(double* acc, float v) {
+// acc[scene] += v over the warp: one atomic per warp when all its lanes
+// belong to one scene, one per lane otherwise (warps at scene boundaries).
+// Every lane of the warp calls it; lanes without a value pass scene ~0u.
+// The warp sum is formed in double, so that the result does not depend on
+// how a scene's particles fall onto warps beyond double rounding.
+__device__ __forceinline__ void warp_add_double(double* acc, uint32_t scene, float v) {
+    const unsigned peers = __match_any_sync(0xffffffffu, scene);
+    if (peers == 0xffffffffu) {
+        double d = (double)v;
 #pragma unroll
-    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-    if ((threadIdx.x & 31) == 0 && v != 0.f) atomicAdd(acc, (double)v);
+        for (int s = 16; s > 0; s >>= 1) d += __shfl_xor_sync(0xffffffffu, d, s);
+        if ((threadIdx.x & 31) == 0 && d != 0.0 && scene != ~0u) atomicAdd(acc + scene, d);
+    } else if (scene != ~0u && v != 0.f) {
+        atomicAdd(acc + scene, (double)v);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -233,7 +252,8 @@ __device__ __forceinline__ void warp_add_double(double* acc, float v) {
 // i-side: the derivatives of k's own sums F_k, V_k, X_k (adjoints cb a_k,
 // mu cv a_k, xbar_k) with respect to p_k, e_k and rho_k; j-side: those of
 // j's sums with respect to the same variables of k.
-__global__ void __launch_bounds__(kAdjThreads) k_adj_force(int n, StepParams P, TapeStep T, size_t mstride,
+template <class Scenes>
+__global__ void __launch_bounds__(kAdjThreads) k_adj_force(int n, const Scenes R, TapeStep T, size_t mstride,
                                                            const float4* __restrict__ adj_a,
                                                            const float4* __restrict__ adj_x,
                                                            float4* __restrict__ pbar, float* __restrict__ rhob_out,
@@ -244,7 +264,12 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_force(int n, StepParams P, 
     const bool live = k < n;
     const unsigned wmask = __ballot_sync(0xffffffffu, live);
     float visc_part = 0.f;
+    uint32_t scene = ~0u;
     if (live) {
+        const StepParams& P = R.params(k);
+        scene = R.scene(k);
+        const uint32_t* cell_s = T.cs + R.cell_base(k);
+        const uint32_t* cell_e = T.ce + R.cell_base(k);
         const float4 pk = __ldg(T.rec_pd + k);
         const float4 vk = __ldg(T.rec_vi + k);
         const float4 ak4 = __ldg(adj_a + k);
@@ -254,7 +279,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_force(int n, StepParams P, 
         const float cb = P.coef_b, cs = P.coef_s;
         float3 pb = make_float3(0.f, 0.f, 0.f), eb = pb, Vs = pb;
         float rhob = 0.f;
-        for_each_neighbour(P, T, mstride, k, pk, wmask, s_rs, s_off, [&](uint32_t j) {
+        for_each_neighbour(P, cell_s, cell_e, T, mstride, k, pk, wmask, s_rs, s_off, [&](uint32_t j) {
             const float4 pj = __ldg(T.rec_pd + j);
             const float4 vj = __ldg(T.rec_vi + j);
             const float3 aj = xyz(__ldg(adj_a + j)), xj = xyz(__ldg(adj_x + j));
@@ -295,13 +320,14 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_force(int n, StepParams P, 
         eb_in[__ldg(T.idx + k)] = make_float4(eb.x, eb.y, eb.z, 0.f);
         visc_part = P.wvisc_dd * dot(ak, Vs);
     }
-    warp_add_double(visc_acc, visc_part);
+    warp_add_double(visc_acc, scene, visc_part);
 }
 
 // ---------------------------------------------------------------------------
 // C: density position terms.  rho_k and rho_j both hold w(|p_k - p_j|^2):
 // pbar_k += Dc * (-6 (h^2 - q)^2) * (rhobar_k + rhobar_j) * d.
-__global__ void __launch_bounds__(kAdjThreads) k_adj_density(int n, StepParams P, TapeStep T, size_t mstride,
+template <class Scenes>
+__global__ void __launch_bounds__(kAdjThreads) k_adj_density(int n, const Scenes R, TapeStep T, size_t mstride,
                                                              const float* __restrict__ rhob,
                                                              const float4* __restrict__ pbar,
                                                              float4* __restrict__ xb_in) {
@@ -311,10 +337,13 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_density(int n, StepParams P
     const bool live = k < n;
     const unsigned wmask = __ballot_sync(0xffffffffu, live);
     if (!live) return;
+    const StepParams& P = R.params(k);
+    const uint32_t* cs = T.cs + R.cell_base(k);
+    const uint32_t* ce = T.ce + R.cell_base(k);
     const float4 pk = __ldg(T.rec_pd + k);
     const float rk = __ldg(rhob + k);
     float3 pb = make_float3(0.f, 0.f, 0.f);
-    for_each_neighbour(P, T, mstride, k, pk, wmask, s_rs, s_off, [&](uint32_t j) {
+    for_each_neighbour(P, cs, ce, T, mstride, k, pk, wmask, s_rs, s_off, [&](uint32_t j) {
         const float4 pj = __ldg(T.rec_pd + j);
         const float3 d = make_float3(pk.x - pj.x, pk.y - pj.y, pk.z - pj.z);
         const float hq = P.h2 - dot(d, d);
@@ -326,121 +355,159 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_density(int n, StepParams P
     xb_in[__ldg(T.idx + k)] = make_float4(x.x, x.y, x.z, 0.f);
 }
 
+// ---------------------------------------------------------------------------
+// Mean-squared-distance loss of the final positions, per scene, in FP64:
+//   L_s = (1/N_s) sum_{i in s} |x_i - x*_i|^2,   dL_s/dx_i = 2 (x_i - x*_i) / N_s.
+// Slots past a scene's particle count get a zero gradient.
+__global__ void __launch_bounds__(256) k_loss_mse(const float4* __restrict__ pos, const float4* __restrict__ target,
+                                                  float4* __restrict__ grad, int nslots,
+                                                  const uint16_t* __restrict__ scene_of,
+                                                  const uint32_t* __restrict__ slot_off,
+                                                  const int* __restrict__ num, int n_single,
+                                                  double* __restrict__ loss) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t scene = ~0u;
+    float v = 0.f;
+    if (t < nslots) {
+        const uint32_t s = scene_of ? scene_of[t] : 0u;
+        const int cnt = scene_of ? num[s] : n_single;
+        const bool valid = scene_of ? (int)(t - slot_off[s]) < cnt : t < n_single;
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) {
+            const float4 x = __ldg(pos + t), y = __ldg(target + t);
+            const float dx = x.x - y.x, dy = x.y - y.y, dz = x.z - y.z;
+            const float inv = 1.f / (float)cnt;
+            g = make_float4(2.f * inv * dx, 2.f * inv * dy, 2.f * inv * dz, 0.f);
+            scene = s;
+            // the per-particle term rounded once; the sum is in double
+            v = (float)(((double)dx * dx + (double)dy * dy + (double)dz * dz) / (double)cnt);
+        }
+        grad[t] = g;
+    }
+    warp_add_double(loss, scene, v);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
-struct sph_adjoint {
-    // recorded rollout
+// Recorded rollout and adjoint buffers of a context or a batch.
+struct AdjState {
     int recorded = 0;
     int nsteps = 0, K = 0, n = 0, exact = 0;
     float dt = 0.f;
     unsigned params_version = 0;
-    // capacity
+    size_t N = 0, C1 = 0, state_elems = 0;  // slot capacity, cell entries, state elements checkpointed
+    int nscenes = 1;
+    bool tape_keys = false;
     int cap_K = 0, cap_ckpt = 0;
-    float4* ckpt = nullptr;  // [cap_ckpt][3][max_num]: pos, vel, veleval at steps 0, K, 2K, ..., then the final state
-    // tape [cap_K] slots
-    uint32_t* t_idx = nullptr;
-    uint32_t* t_cs = nullptr;
-    uint32_t* t_ce = nullptr;
-    float4* t_pd = nullptr;
-    float4* t_vi = nullptr;
-    uint32_t* t_mask = nullptr;
-    float4* t_f = nullptr;
-    float4* t_v = nullptr;
-    // adjoint state, original order (ping-pong) and per sorted particle
+    float4* ckpt = nullptr;  // [cap_ckpt][3][N]: pos, vel, veleval at steps 0, K, 2K, ..., then the final state
+    uint32_t *t_idx = nullptr, *t_keys = nullptr, *t_cs = nullptr, *t_ce = nullptr, *t_mask = nullptr;
+    float4 *t_pd = nullptr, *t_vi = nullptr, *t_f = nullptr, *t_v = nullptr;
     float4* xb[2] = {nullptr, nullptr};
     float4* vb[2] = {nullptr, nullptr};
     float4* eb[2] = {nullptr, nullptr};
-    float4* adj_a = nullptr;
-    float4* adj_x = nullptr;
-    float4* pbar = nullptr;
+    float4 *adj_a = nullptr, *adj_x = nullptr, *pbar = nullptr;
     float* rhob = nullptr;
-    double* visc_acc = nullptr;
-    double* host_visc = nullptr;
-    // backward graph and the configuration it was captured for
+    double* visc_acc = nullptr;   // [nscenes]
+    double* host_visc = nullptr;  // [nscenes], pinned
     cudaGraphExec_t graph = nullptr;
     int g_nsteps = -1, g_K = -1, g_n = -1, g_exact = -1;
     float g_dt = 0.f;
     unsigned g_version = 0;
     cudaStream_t g_stream = nullptr;
 };
+struct sph_adjoint : AdjState {};
+struct sph_batch_adjoint : AdjState {};
 
 namespace {
 
-void free_tape(sph_adjoint* a) {
-    void* ptrs[] = {a->t_idx, a->t_cs, a->t_ce, a->t_pd, a->t_vi, a->t_mask, a->t_f, a->t_v};
+void free_tape(AdjState* a) {
+    void* ptrs[] = {a->t_idx, a->t_keys, a->t_cs, a->t_ce, a->t_pd, a->t_vi, a->t_mask, a->t_f, a->t_v};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    a->t_idx = a->t_cs = a->t_ce = a->t_mask = nullptr;
+    a->t_idx = a->t_keys = a->t_cs = a->t_ce = a->t_mask = nullptr;
     a->t_pd = a->t_vi = a->t_f = a->t_v = nullptr;
     a->cap_K = 0;
 }
 
-void drop_graph(sph_adjoint* a) {
+void drop_graph(AdjState* a) {
     if (a->graph) cudaGraphExecDestroy(a->graph);
     a->graph = nullptr;
 }
 
-int ensure_buffers(sph_ctx* c, int K, int nckpt) {
-    sph_adjoint* a = c->adj;
-    const size_t N = (size_t)c->max_num, C1 = (size_t)c->gp.nb_cells + 1;
+void free_state(AdjState* a) {
+    drop_graph(a);
+    free_tape(a);
+    void* ptrs[] = {a->ckpt, a->xb[0], a->xb[1], a->vb[0], a->vb[1], a->eb[0], a->eb[1], a->adj_a, a->adj_x,
+                    a->pbar, a->rhob, a->visc_acc};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (a->host_visc) cudaFreeHost(a->host_visc);
+}
+
+// Allocation of the adjoint buffers (once), the checkpoints (nckpt slots)
+// and the tape (K slots); returns a cudaError_t.
+cudaError_t ensure_buffers(AdjState* a, int K, int nckpt) {
+    const size_t N = a->N, C1 = a->C1;
+    cudaError_t e = cudaSuccess;
+#define AL(ptr, bytes) \
+    if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes))
     if (!a->xb[0]) {
         for (int s = 0; s < 2; ++s) {
-            CK(c, cudaMalloc((void**)&a->xb[s], N * 16));
-            CK(c, cudaMalloc((void**)&a->vb[s], N * 16));
-            CK(c, cudaMalloc((void**)&a->eb[s], N * 16));
+            AL(a->xb[s], N * 16);
+            AL(a->vb[s], N * 16);
+            AL(a->eb[s], N * 16);
         }
-        CK(c, cudaMalloc((void**)&a->adj_a, N * 16));
-        CK(c, cudaMalloc((void**)&a->adj_x, N * 16));
-        CK(c, cudaMalloc((void**)&a->pbar, N * 16));
-        CK(c, cudaMalloc((void**)&a->rhob, N * 4));
-        CK(c, cudaMalloc((void**)&a->visc_acc, sizeof(double)));
-        CK(c, cudaMallocHost((void**)&a->host_visc, sizeof(double)));
+        AL(a->adj_a, N * 16);
+        AL(a->adj_x, N * 16);
+        AL(a->pbar, N * 16);
+        AL(a->rhob, N * 4);
+        AL(a->visc_acc, sizeof(double) * a->nscenes);
+        if (e == cudaSuccess) e = cudaMallocHost((void**)&a->host_visc, sizeof(double) * a->nscenes);
+        for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
+            e = cudaMemset(a->xb[s], 0, N * 16);
+            if (e == cudaSuccess) e = cudaMemset(a->vb[s], 0, N * 16);
+            if (e == cudaSuccess) e = cudaMemset(a->eb[s], 0, N * 16);
+        }
+        if (e != cudaSuccess) return e;
     }
     if (nckpt > a->cap_ckpt) {
         drop_graph(a);
         if (a->ckpt) cudaFree(a->ckpt);
         a->ckpt = nullptr;
         a->cap_ckpt = 0;
-        CK(c, cudaMalloc((void**)&a->ckpt, (size_t)nckpt * 3 * N * 16));
+        AL(a->ckpt, (size_t)nckpt * 3 * N * 16);
+        if (e != cudaSuccess) return e;
         a->cap_ckpt = nckpt;
     }
     if (K > a->cap_K) {
         drop_graph(a);
         free_tape(a);
         const size_t k = (size_t)K;
-        CK(c, cudaMalloc((void**)&a->t_idx, k * N * 4));
-        CK(c, cudaMalloc((void**)&a->t_cs, k * C1 * 4));
-        CK(c, cudaMalloc((void**)&a->t_ce, k * C1 * 4));
-        CK(c, cudaMalloc((void**)&a->t_pd, k * N * 16));
-        CK(c, cudaMalloc((void**)&a->t_vi, k * N * 16));
-        CK(c, cudaMalloc((void**)&a->t_mask, k * N * 4 * sphk::kMaskWords));
-        CK(c, cudaMalloc((void**)&a->t_f, k * N * 16));
-        CK(c, cudaMalloc((void**)&a->t_v, k * N * 16));
+        AL(a->t_idx, k * N * 4);
+        if (a->tape_keys) AL(a->t_keys, k * N * 4);
+        AL(a->t_cs, k * C1 * 4);
+        AL(a->t_ce, k * C1 * 4);
+        AL(a->t_pd, k * N * 16);
+        AL(a->t_vi, k * N * 16);
+        AL(a->t_mask, k * N * 4 * sphk::kMaskWords);
+        AL(a->t_f, k * N * 16);
+        AL(a->t_v, k * N * 16);
+        if (e != cudaSuccess) {
+            free_tape(a);
+            return e;
+        }
         a->cap_K = K;
     }
-    return SPH_OK;
+#undef AL
+    return cudaSuccess;
 }
 
-float4* ckpt_slot(sph_ctx* c, int slot, int field) {
-    return c->adj->ckpt + ((size_t)slot * 3 + field) * (size_t)c->max_num;
-}
-
-int copy_state(sph_ctx* c, int slot, bool save) {
-    const size_t b = (size_t)c->adj->n * 16;
-    float4* st[3] = {c->pos_u, c->vel_u, c->veleval_u};
-    for (int f = 0; f < 3; ++f) {
-        float4* ck = ckpt_slot(c, slot, f);
-        CK(c, cudaMemcpyAsync(save ? ck : st[f], save ? st[f] : ck, b, cudaMemcpyDeviceToDevice, c->stream));
-    }
-    return SPH_OK;
-}
-
-TapeStep tape_step(sph_ctx* c, int slot) {
-    sph_adjoint* a = c->adj;
-    const size_t N = (size_t)c->max_num, C1 = (size_t)c->gp.nb_cells + 1, s = (size_t)slot;
+TapeStep tape_step(const AdjState* a, int slot) {
+    const size_t N = a->N, C1 = a->C1, s = (size_t)slot;
     TapeStep T;
     T.idx = a->t_idx + s * N;
+    T.keys = a->t_keys ? a->t_keys + s * N : nullptr;
     T.cs = a->t_cs + s * C1;
     T.ce = a->t_ce + s * C1;
     T.rec_pd = a->t_pd + s * N;
@@ -451,10 +518,46 @@ TapeStep tape_step(sph_ctx* c, int slot) {
     return T;
 }
 
+float4* ckpt_slot(const AdjState* a, int slot, int field) {
+    return a->ckpt + ((size_t)slot * 3 + field) * a->N;
+}
+
+// Checkpoint `slot` <-> the state arrays (pos, vel, veleval).
+cudaError_t copy_state(const AdjState* a, float4* const st[3], int slot, bool save, cudaStream_t stream) {
+    const size_t b = a->state_elems * 16;
+    for (int f = 0; f < 3; ++f) {
+        float4* ck = ckpt_slot(a, slot, f);
+        const cudaError_t e =
+            cudaMemcpyAsync(save ? ck : st[f], save ? st[f] : ck, b, cudaMemcpyDeviceToDevice, stream);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+template <class Scenes>
+void launch_reverse(const AdjState* a, const Scenes& R, const TapeStep& T, int src, cudaStream_t st) {
+    const int n = a->n, dst = 1 - src;
+    const size_t mstride = a->N;
+    const int b256 = (n + 255) / 256, b128 = (n + kAdjThreads - 1) / kAdjThreads;
+    k_adj_integrate<Scenes><<<b256, 256, 0, st>>>(n, R, a->dt, T, a->xb[src], a->vb[src], a->eb[src], a->vb[dst],
+                                                  a->adj_a, a->adj_x, a->pbar);
+    k_adj_force<Scenes><<<b128, kAdjThreads, 0, st>>>(n, R, T, mstride, a->adj_a, a->adj_x, a->pbar, a->rhob,
+                                                      a->eb[dst], a->visc_acc);
+    k_adj_density<Scenes><<<b128, kAdjThreads, 0, st>>>(n, R, T, mstride, a->rhob, a->pbar, a->xb[dst]);
+}
+
+// --- contexts ----------------------------------------------------------------
+float4* const* ctx_state(sph_ctx* c, float4* st[3]) {
+    st[0] = c->pos_u;
+    st[1] = c->vel_u;
+    st[2] = c->veleval_u;
+    return st;
+}
+
 // One forward step whose records land in tape slot `slot`: the context's
 // record buffers are pointed at the slot for the enqueue and restored after.
-int enqueue_taped_step(sph_ctx* c, int slot) {
-    const TapeStep T = tape_step(c, slot);
+int ctx_taped_step(sph_ctx* c, int slot) {
+    const TapeStep T = tape_step(c->adj, slot);
     float4 *rec_pd = c->rec_pd, *rec_vi = c->rec_vi;
     uint32_t *mask = c->mask, *cs = c->cell_start, *ce = c->cell_end, *idx_a = c->idx_a;
     c->rec_pd = const_cast<float4*>(T.rec_pd);
@@ -479,45 +582,118 @@ int enqueue_taped_step(sph_ctx* c, int slot) {
     return rc;
 }
 
-// The reverse of one step: adjoints of the step's outputs in buffers `src`,
-// of its inputs into 1 - src.
-int enqueue_reverse_step(sph_ctx* c, int slot, int src) {
-    sph_adjoint* a = c->adj;
-    const TapeStep T = tape_step(c, slot);
-    const int n = a->n, dst = 1 - src;
-    const size_t mstride = (size_t)c->max_num;
-    const int b256 = (n + 255) / 256, b128 = (n + kAdjThreads - 1) / kAdjThreads;
-    k_adj_integrate<<<b256, 256, 0, c->stream>>>(n, c->P, a->dt, T, a->xb[src], a->vb[src], a->eb[src], a->vb[dst],
-                                                 a->adj_a, a->adj_x, a->pbar);
-    k_adj_force<<<b128, kAdjThreads, 0, c->stream>>>(n, c->P, T, mstride, a->adj_a, a->adj_x, a->pbar, a->rhob,
-                                                     a->eb[dst], a->visc_acc);
-    k_adj_density<<<b128, kAdjThreads, 0, c->stream>>>(n, c->P, T, mstride, a->rhob, a->pbar, a->xb[dst]);
-    CK_LAUNCH(c);
-    return SPH_OK;
+// --- batches -----------------------------------------------------------------
+float4* const* batch_state(sph_batch* b, float4* st[3]) {
+    st[0] = b->pos_u;
+    st[1] = b->vel_u;
+    st[2] = b->veleval_u;
+    return st;
+}
+
+int batch_taped_step(sph_batch* b, int slot, float dt) {
+    const TapeStep T = tape_step(b->adj, slot);
+    float4 *rec_pd = b->rec_pd, *rec_vi = b->rec_vi;
+    uint32_t *mask = b->mask, *cs = b->cell_start, *ce = b->cell_end, *idx_a = b->idx_a, *keys_a = b->keys_a;
+    b->rec_pd = const_cast<float4*>(T.rec_pd);
+    b->rec_vi = const_cast<float4*>(T.rec_vi);
+    b->mask = const_cast<uint32_t*>(T.mask);
+    b->cell_start = const_cast<uint32_t*>(T.cs);
+    b->cell_end = const_cast<uint32_t*>(T.ce);
+    b->idx_a = const_cast<uint32_t*>(T.idx);
+    b->keys_a = const_cast<uint32_t*>(T.keys);
+    b->keep_f = const_cast<float4*>(T.fsph);
+    b->keep_v = const_cast<float4*>(T.vin);
+    const int rc = batch_enqueue_step(b, dt);
+    b->rec_pd = rec_pd;
+    b->rec_vi = rec_vi;
+    b->mask = mask;
+    b->cell_start = cs;
+    b->cell_end = ce;
+    b->idx_a = idx_a;
+    b->keys_a = keys_a;
+    b->keep_f = nullptr;
+    b->keep_v = nullptr;
+    return rc;
 }
 
 // The whole backward pass: for each segment, last first, restore its
 // checkpoint, recompute it into the tape, reverse it; then restore the final
 // state.  Starts from the adjoints in buffers 0; ends in buffers nsteps % 2.
-int enqueue_backward(sph_ctx* c) {
-    sph_adjoint* a = c->adj;
+// Returns SPH_OK or the error of the first failing enqueue (set on the owner).
+template <class Owner, class TapedStep, class Reverse>
+int enqueue_backward(Owner* o, AdjState* a, float4* const st[3], cudaStream_t stream, TapedStep&& taped,
+                     Reverse&& reverse, int (*fail)(Owner*, const char*, cudaError_t)) {
     const int T = a->nsteps, K = a->K;
     const int nseg = (T + K - 1) / K;
     int src = 0, rc;
+    cudaError_t e;
     for (int s = nseg - 1; s >= 0; --s) {
         const int t0 = s * K, t1 = (t0 + K < T) ? t0 + K : T;
-        if ((rc = copy_state(c, s, false))) return rc;
+        if ((e = copy_state(a, st, s, false, stream)) != cudaSuccess) return fail(o, "checkpoint restore", e);
         for (int t = t0; t < t1; ++t)
-            if ((rc = enqueue_taped_step(c, t - t0))) return rc;
+            if ((rc = taped(t - t0))) return rc;
         for (int t = t1 - 1; t >= t0; --t) {
-            if ((rc = enqueue_reverse_step(c, t - t0, src))) return rc;
+            reverse(tape_step(a, t - t0), src);
             src = 1 - src;
         }
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(o, "reverse kernels", e);
     }
-    return copy_state(c, nseg, false);
+    if ((e = copy_state(a, st, nseg, false, stream)) != cudaSuccess) return fail(o, "state restore", e);
+    return SPH_OK;
 }
 
-int adj_check(sph_ctx* c) {
+int ctx_fail(sph_ctx* c, const char* what, cudaError_t e) {
+    return set_err(c, SPH_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+int batch_fail(sph_batch* b, const char* what, cudaError_t e) {
+    return berr(b, SPH_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+bool graph_stale(const AdjState* a, cudaStream_t stream) {
+    return !a->graph || a->g_nsteps != a->nsteps || a->g_K != a->K || a->g_n != a->n || a->g_exact != a->exact ||
+           a->g_dt != a->dt || a->g_version != a->params_version || a->g_stream != stream;
+}
+
+void graph_key(AdjState* a, cudaStream_t stream) {
+    a->g_nsteps = a->nsteps;
+    a->g_K = a->K;
+    a->g_n = a->n;
+    a->g_exact = a->exact;
+    a->g_dt = a->dt;
+    a->g_version = a->params_version;
+    a->g_stream = stream;
+}
+
+// Loads the final-state adjoints (NULL: zero) into buffers 0 and clears the
+// viscosity accumulators.
+cudaError_t load_seeds(AdjState* a, const sph_float4* dpos, const sph_float4* dvel, const sph_float4* dveleval,
+                       cudaStream_t st) {
+    const size_t b = a->state_elems * 16;
+    const sph_float4* src[3] = {dpos, dvel, dveleval};
+    float4* dst[3] = {a->xb[0], a->vb[0], a->eb[0]};
+    for (int f = 0; f < 3; ++f) {
+        const cudaError_t e = src[f] ? cudaMemcpyAsync(dst[f], src[f], b, cudaMemcpyDeviceToDevice, st)
+                                     : cudaMemsetAsync(dst[f], 0, b, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaMemsetAsync(a->visc_acc, 0, sizeof(double) * a->nscenes, st);
+}
+
+cudaError_t store_results(AdjState* a, sph_float4* dpos0, sph_float4* dvel0, sph_float4* dveleval0,
+                          cudaStream_t st) {
+    const size_t b = a->state_elems * 16;
+    const int fin = a->nsteps & 1;
+    sph_float4* dst[3] = {dpos0, dvel0, dveleval0};
+    const float4* src[3] = {a->xb[fin], a->vb[fin], a->eb[fin]};
+    for (int f = 0; f < 3; ++f) {
+        if (!dst[f]) continue;
+        const cudaError_t e = cudaMemcpyAsync(dst[f], src[f], b, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaMemcpyAsync(a->host_visc, a->visc_acc, sizeof(double) * a->nscenes, cudaMemcpyDeviceToHost, st);
+}
+
+int ctx_adj_check(sph_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
     if (!c->adj || !c->adj->recorded)
@@ -527,20 +703,42 @@ int adj_check(sph_ctx* c) {
     return SPH_OK;
 }
 
+int batch_adj_check(sph_batch* b) {
+    if (!b) return SPH_EINVAL;
+    cudaSetDevice(b->device);
+    if (!b->adj || !b->adj->recorded)
+        return berr(b, SPH_ESTATE, "no recorded rollout: call sph_batch_adjoint_record first");
+    if (b->adj->params_version != b->params_version || b->adj->exact != b->exact ||
+        b->adj->n != b->nvalid)
+        return berr(b, SPH_ESTATE, "parameters or particles changed since the rollout was recorded");
+    return SPH_OK;
+}
+
+// The neighbour-pass counters into b->host_info, after sph_batch_sync has
+// checked the sort's device error word.
+int batch_read_info(sph_batch* b) {
+    const int rc = sph_batch_sync(b);
+    if (rc) return rc;
+    BCK(b, cudaMemcpyAsync(b->host_info, b->info_nb, sizeof(int) * sphk::kInfoSlots, cudaMemcpyDeviceToHost,
+                           b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    return SPH_OK;
+}
+
 }  // namespace
 
 void sph_adjoint_release(sph_ctx* c) {
-    sph_adjoint* a = c ? c->adj : nullptr;
-    if (!a) return;
-    drop_graph(a);
-    free_tape(a);
-    void* ptrs[] = {a->ckpt, a->xb[0], a->xb[1], a->vb[0], a->vb[1], a->eb[0], a->eb[1], a->adj_a, a->adj_x,
-                    a->pbar, a->rhob, a->visc_acc};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
-    if (a->host_visc) cudaFreeHost(a->host_visc);
-    delete a;
+    if (!c || !c->adj) return;
+    free_state(c->adj);
+    delete c->adj;
     c->adj = nullptr;
+}
+
+void sph_batch_adjoint_release(sph_batch* b) {
+    if (!b || !b->adj) return;
+    free_state(b->adj);
+    delete b->adj;
+    b->adj = nullptr;
 }
 
 extern "C" {
@@ -550,7 +748,11 @@ int sph_adjoint_record(sph_ctx* c, float dt, int nsteps, int K) {
     if (rc) return rc;
     if (nsteps <= 0 || K <= 0 || !std::isfinite(dt))
         return set_err(c, SPH_EINVAL, "sph_adjoint_record: bad arguments (nsteps=%d, K=%d)", nsteps, K);
-    if (!c->adj) c->adj = new sph_adjoint();
+    if (!c->adj) {
+        c->adj = new sph_adjoint();
+        c->adj->N = (size_t)c->max_num;
+        c->adj->C1 = (size_t)c->gp.nb_cells + 1;
+    }
     sph_adjoint* a = c->adj;
     a->recorded = 0;
     if ((rc = read_info(c))) return rc;
@@ -560,19 +762,27 @@ int sph_adjoint_record(sph_ctx* c, float dt, int nsteps, int K) {
     if (n <= 0) return set_err(c, SPH_ESTATE, "no particles to record");
     if (K > nsteps) K = nsteps;
     const int nseg = (nsteps + K - 1) / K;
-    if ((rc = ensure_buffers(c, K, nseg + 1))) return rc;
+    const cudaError_t e = ensure_buffers(a, K, nseg + 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(c, SPH_ENOMEM, "adjoint buffers (K=%d, %d checkpoints): %s", K, nseg + 1,
+                       cudaGetErrorString(e));
+    }
     a->n = n;
+    a->state_elems = (size_t)n;
     a->dt = dt;
     a->nsteps = nsteps;
     a->K = K;
     a->exact = c->exact;
     a->params_version = c->params_version;
+    float4* st[3];
+    ctx_state(c, st);
     for (int s = 0; s < nseg; ++s) {
-        if ((rc = copy_state(c, s, true))) return rc;
+        CK(c, copy_state(a, st, s, true, c->stream));
         const int steps = (s + 1) * K <= nsteps ? K : nsteps - s * K;
         if ((rc = sph_step(c, dt, steps))) return rc;
     }
-    if ((rc = copy_state(c, nseg, true))) return rc;
+    CK(c, copy_state(a, st, nseg, true, c->stream));
     if ((rc = read_info(c))) return rc;
     const int out = c->host_info[sphk::kOutStart], now = c->host_info[sphk::kNum];
     if (now != n || out >= 0)
@@ -584,31 +794,20 @@ int sph_adjoint_record(sph_ctx* c, float dt, int nsteps, int K) {
 int sph_adjoint_backward(sph_ctx* c, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
                          const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0,
                          sph_float4* dL_dveleval0, double* dL_dvisc) {
-    int rc = adj_check(c);
+    int rc = ctx_adj_check(c);
     if (rc) return rc;
     sph_adjoint* a = c->adj;
-    const size_t b = (size_t)a->n * 16;
-    if (dL_dpos)
-        CK(c, cudaMemcpyAsync(a->xb[0], dL_dpos, b, cudaMemcpyDeviceToDevice, c->stream));
-    else
-        CK(c, cudaMemsetAsync(a->xb[0], 0, b, c->stream));
-    if (dL_dvel)
-        CK(c, cudaMemcpyAsync(a->vb[0], dL_dvel, b, cudaMemcpyDeviceToDevice, c->stream));
-    else
-        CK(c, cudaMemsetAsync(a->vb[0], 0, b, c->stream));
-    if (dL_dveleval)
-        CK(c, cudaMemcpyAsync(a->eb[0], dL_dveleval, b, cudaMemcpyDeviceToDevice, c->stream));
-    else
-        CK(c, cudaMemsetAsync(a->eb[0], 0, b, c->stream));
-    CK(c, cudaMemsetAsync(a->visc_acc, 0, sizeof(double), c->stream));
-    const bool stale = !a->graph || a->g_nsteps != a->nsteps || a->g_K != a->K || a->g_n != a->n ||
-                       a->g_exact != a->exact || a->g_dt != a->dt || a->g_version != a->params_version ||
-                       a->g_stream != c->stream;
-    if (stale) {
+    CK(c, load_seeds(a, dL_dpos, dL_dvel, dL_dveleval, c->stream));
+    if (graph_stale(a, c->stream)) {
         drop_graph(a);
+        float4* st[3];
+        ctx_state(c, st);
         cudaGraph_t g = nullptr;
         CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        rc = enqueue_backward(c);
+        const sphk::OneScene R{c->P};
+        rc = enqueue_backward(
+            c, a, st, c->stream, [&](int slot) { return ctx_taped_step(c, slot); },
+            [&](const TapeStep& T, int src) { launch_reverse(a, R, T, src, c->stream); }, ctx_fail);
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
@@ -621,28 +820,18 @@ int sph_adjoint_backward(sph_ctx* c, const sph_float4* dL_dpos, const sph_float4
             a->graph = nullptr;
             return set_err(c, SPH_ECUDA, "backward graph instantiate: %s", cudaGetErrorString(e));
         }
-        a->g_nsteps = a->nsteps;
-        a->g_K = a->K;
-        a->g_n = a->n;
-        a->g_exact = a->exact;
-        a->g_dt = a->dt;
-        a->g_version = a->params_version;
-        a->g_stream = c->stream;
+        graph_key(a, c->stream);
     }
     CK(c, cudaGraphLaunch(a->graph, c->stream));
-    const int fin = a->nsteps & 1;
-    if (dL_dpos0) CK(c, cudaMemcpyAsync(dL_dpos0, a->xb[fin], b, cudaMemcpyDeviceToDevice, c->stream));
-    if (dL_dvel0) CK(c, cudaMemcpyAsync(dL_dvel0, a->vb[fin], b, cudaMemcpyDeviceToDevice, c->stream));
-    if (dL_dveleval0) CK(c, cudaMemcpyAsync(dL_dveleval0, a->eb[fin], b, cudaMemcpyDeviceToDevice, c->stream));
-    CK(c, cudaMemcpyAsync(a->host_visc, a->visc_acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, store_results(a, dL_dpos0, dL_dvel0, dL_dveleval0, c->stream));
     if ((rc = read_info(c))) return rc;
-    if (dL_dvisc) *dL_dvisc = *a->host_visc;
+    if (dL_dvisc) *dL_dvisc = a->host_visc[0];
     return SPH_OK;
 }
 
 int sph_adjoint_rollout(sph_ctx* c, int nsteps, int K, const sph_float4* dL_dpos_final, sph_float4* dL_dvel0,
                         float* dL_dvisc) {
-    int rc = adj_check(c);
+    int rc = ctx_adj_check(c);
     if (rc) return rc;
     const int k_eff = K > c->adj->nsteps ? c->adj->nsteps : K;
     if (nsteps != c->adj->nsteps || k_eff != c->adj->K)
@@ -652,6 +841,168 @@ int sph_adjoint_rollout(sph_ctx* c, int nsteps, int K, const sph_float4* dL_dpos
     rc = sph_adjoint_backward(c, dL_dpos_final, nullptr, nullptr, nullptr, dL_dvel0, nullptr, &v);
     if (rc == SPH_OK && dL_dvisc) *dL_dvisc = (float)v;
     return rc;
+}
+
+int sph_adjoint_rewind(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!c->adj || !c->adj->recorded) return set_err(c, SPH_ESTATE, "no recorded rollout to rewind");
+    float4* st[3];
+    CK(c, copy_state(c->adj, ctx_state(c, st), 0, false, c->stream));
+    return read_info(c);
+}
+
+int sph_loss_mse(sph_ctx* c, const sph_float4* target, sph_float4* dL_dpos, double* loss) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!target || !dL_dpos) return set_err(c, SPH_EINVAL, "sph_loss_mse: null array");
+    if (!c->adj) {
+        c->adj = new sph_adjoint();
+        c->adj->N = (size_t)c->max_num;
+        c->adj->C1 = (size_t)c->gp.nb_cells + 1;
+    }
+    const cudaError_t e = ensure_buffers(c->adj, 0, 0);
+    if (e != cudaSuccess) return set_err(c, SPH_ENOMEM, "sph_loss_mse: %s", cudaGetErrorString(e));
+    if ((rc = read_info(c))) return rc;
+    const int n = c->host_info[sphk::kNum];
+    CK(c, cudaMemsetAsync(c->adj->visc_acc, 0, sizeof(double), c->stream));
+    const int blocks = (n + 255) / 256;
+    if (n > 0)
+        k_loss_mse<<<blocks, 256, 0, c->stream>>>(c->pos_u, reinterpret_cast<const float4*>(target),
+                                                  reinterpret_cast<float4*>(dL_dpos), n, nullptr, nullptr, nullptr, n,
+                                                  c->adj->visc_acc);
+    CK_LAUNCH(c);
+    CK(c, cudaMemcpyAsync(c->adj->host_visc, c->adj->visc_acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if ((rc = read_info(c))) return rc;
+    if (loss) *loss = c->adj->host_visc[0];
+    return SPH_OK;
+}
+
+// --- batches -----------------------------------------------------------------
+int sph_batch_adjoint_record(sph_batch* b, float dt, int nsteps, int K) {
+    if (!b || nsteps <= 0 || K <= 0 || !std::isfinite(dt))
+        return berr(b, SPH_EINVAL, "sph_batch_adjoint_record: bad arguments (nsteps=%d, K=%d)", nsteps, K);
+    cudaSetDevice(b->device);
+    if (!b->adj) {
+        b->adj = new sph_batch_adjoint();
+        b->adj->N = (size_t)b->nslots;
+        b->adj->C1 = b->ncells_total;
+        b->adj->nscenes = b->nscenes;
+        b->adj->tape_keys = true;
+        b->adj->state_elems = (size_t)b->nslots;
+    }
+    sph_batch_adjoint* a = b->adj;
+    a->recorded = 0;
+    if (b->nvalid <= 0) return berr(b, SPH_ESTATE, "no particles to record");
+    if (K > nsteps) K = nsteps;
+    const int nseg = (nsteps + K - 1) / K;
+    const cudaError_t e = ensure_buffers(a, K, nseg + 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return berr(b, SPH_ENOMEM, "adjoint buffers (K=%d, %d checkpoints): %s", K, nseg + 1, cudaGetErrorString(e));
+    }
+    a->n = b->nvalid;
+    a->dt = dt;
+    a->nsteps = nsteps;
+    a->K = K;
+    a->exact = b->exact;
+    a->params_version = b->params_version;
+    BCK(b, cudaMemsetAsync(b->info_nb + kBatchFrozenTotal, 0, sizeof(int), b->stream));
+    float4* st[3];
+    batch_state(b, st);
+    int rc;
+    for (int s = 0; s < nseg; ++s) {
+        BCK(b, copy_state(a, st, s, true, b->stream));
+        const int steps = (s + 1) * K <= nsteps ? K : nsteps - s * K;
+        if ((rc = sph_batch_step(b, dt, steps))) return rc;
+    }
+    BCK(b, copy_state(a, st, nseg, true, b->stream));
+    if ((rc = batch_read_info(b))) return rc;
+    if (b->host_info[kBatchFrozenTotal] != 0)
+        return berr(b, SPH_EOOB, "particles left their scene's grid during the rollout; its gradient is not defined");
+    a->recorded = 1;
+    return SPH_OK;
+}
+
+int sph_batch_adjoint_backward(sph_batch* b, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
+                               const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0,
+                               sph_float4* dL_dveleval0, double* dL_dvisc) {
+    int rc = batch_adj_check(b);
+    if (rc) return rc;
+    sph_batch_adjoint* a = b->adj;
+    BCK(b, load_seeds(a, dL_dpos, dL_dvel, dL_dveleval, b->stream));
+    if (graph_stale(a, b->stream)) {
+        drop_graph(a);
+        float4* st[3];
+        batch_state(b, st);
+        cudaGraph_t g = nullptr;
+        BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const float dt = a->dt;
+        rc = enqueue_backward(
+            b, a, st, b->stream, [&](int slot) { return batch_taped_step(b, slot, dt); },
+            [&](const TapeStep& T, int src) {
+                const sphk::ManyScenes R{b->d_table, b->d_cbase, T.keys, b->cell_bits};
+                launch_reverse(a, R, T, src, b->stream);
+            },
+            batch_fail);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return berr(b, SPH_ECUDA, "backward graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&a->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            a->graph = nullptr;
+            return berr(b, SPH_ECUDA, "backward graph instantiate: %s", cudaGetErrorString(e));
+        }
+        graph_key(a, b->stream);
+    }
+    BCK(b, cudaGraphLaunch(a->graph, b->stream));
+    BCK(b, store_results(a, dL_dpos0, dL_dvel0, dL_dveleval0, b->stream));
+    if ((rc = sph_batch_sync(b))) return rc;
+    if (dL_dvisc)
+        for (int s = 0; s < b->nscenes; ++s) dL_dvisc[s] = a->host_visc[s];
+    return SPH_OK;
+}
+
+int sph_batch_adjoint_rewind(sph_batch* b) {
+    if (!b) return SPH_EINVAL;
+    cudaSetDevice(b->device);
+    if (!b->adj || !b->adj->recorded) return berr(b, SPH_ESTATE, "no recorded rollout to rewind");
+    float4* st[3];
+    BCK(b, copy_state(b->adj, batch_state(b, st), 0, false, b->stream));
+    return sph_batch_sync(b);
+}
+
+int sph_batch_loss_mse(sph_batch* b, const sph_float4* target, sph_float4* dL_dpos, double* loss) {
+    if (!b || !target || !dL_dpos) return berr(b, SPH_EINVAL, "sph_batch_loss_mse: null argument");
+    cudaSetDevice(b->device);
+    if (!b->adj) {
+        b->adj = new sph_batch_adjoint();
+        b->adj->N = (size_t)b->nslots;
+        b->adj->C1 = b->ncells_total;
+        b->adj->nscenes = b->nscenes;
+        b->adj->tape_keys = true;
+        b->adj->state_elems = (size_t)b->nslots;
+    }
+    sph_batch_adjoint* a = b->adj;
+    const cudaError_t e = ensure_buffers(a, 0, 0);
+    if (e != cudaSuccess) return berr(b, SPH_ENOMEM, "sph_batch_loss_mse: %s", cudaGetErrorString(e));
+    BCK(b, cudaMemsetAsync(a->visc_acc, 0, sizeof(double) * b->nscenes, b->stream));
+    const int blocks = (b->nslots + 255) / 256;
+    k_loss_mse<<<blocks, 256, 0, b->stream>>>(b->pos_u, reinterpret_cast<const float4*>(target),
+                                              reinterpret_cast<float4*>(dL_dpos), b->nslots, b->scene_of,
+                                              b->d_slot_off, b->d_num, 0, a->visc_acc);
+    BCK(b, cudaGetLastError());
+    BCK(b, cudaMemcpyAsync(a->host_visc, a->visc_acc, sizeof(double) * b->nscenes, cudaMemcpyDeviceToHost,
+                           b->stream));
+    const int rc = sph_batch_sync(b);
+    if (rc) return rc;
+    if (loss)
+        for (int s = 0; s < b->nscenes; ++s) loss[s] = a->host_visc[s];
+    return SPH_OK;
 }
 
 }  // extern "C"

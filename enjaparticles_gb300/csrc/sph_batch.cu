@@ -25,13 +25,11 @@
 #include <string>
 #include <vector>
 
-#include "sph_device.cuh"
+#include "sph_batch.cuh"
 
 using sphk::StepParams;
 
 namespace {
-
-constexpr int kBatchFrozen = 5;  // info slot: frozen particles seen by the last step
 
 __global__ void __launch_bounds__(256) k_bhash(const float4* __restrict__ pos_u, uint32_t* __restrict__ keys,
                                                uint32_t* __restrict__ idx, uint32_t* __restrict__ cell_start,
@@ -102,7 +100,10 @@ __global__ void __launch_bounds__(256) k_bcells(const uint32_t* __restrict__ key
         cell_end[cbase[prev >> cell_bits] + (prev & cmask)] = (uint32_t)i;
     }
     if (i == nvalid - 1) cell_end[g] = (uint32_t)nvalid;
-    if (cell == (uint32_t)table[s].nb_cells) atomicAdd(info + kBatchFrozen, 1);
+    if (cell == (uint32_t)table[s].nb_cells) {
+        atomicAdd(info + kBatchFrozen, 1);
+        atomicAdd(info + kBatchFrozenTotal, 1);
+    }
     const uint32_t o = __ldg(idx + i);
     pos_s[i] = __ldg(pos_u + o);
     veleval_s[i] = __ldg(veleval_u + o);
@@ -122,39 +123,9 @@ int bit_width_u(uint32_t v) {
 
 }  // namespace
 
-struct sph_batch {
-    int device = 0, nscenes = 0, exact = 0;
-    cudaStream_t own_stream = nullptr, stream = nullptr;
-    std::vector<SPHParams> sp;
-    std::vector<GridParams> gp, gps;
-    std::vector<StepParams> P;
-    std::vector<int> max_num, num;
-    std::vector<uint32_t> slot_off, cbase;
-    int nslots = 0, nvalid = 0, cell_bits = 0, scene_bits = 0, passes = 1, tiles_cap = 0, unit = 1;
-    size_t ncells_total = 0;
-    uint32_t invalid_key = 0;
-    // device
-    float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr, *pos_s = nullptr, *veleval_s = nullptr;
-    float4 *rec_pd = nullptr, *rec_vi = nullptr;
-    float* density = nullptr;
-    uint32_t *mask = nullptr, *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
-    uint32_t *cell_start = nullptr, *cell_end = nullptr;
-    uint16_t* scene_of = nullptr;
-    uint32_t *d_slot_off = nullptr, *d_cbase = nullptr;
-    int* d_num = nullptr;
-    StepParams* d_table = nullptr;
-    int *info_sort = nullptr, *info_nb = nullptr;
-    uint32_t *hist = nullptr, *status = nullptr;
-    int* host_info = nullptr;
-    cudaGraphExec_t graph = nullptr;
-    float graph_dt = 0.f;
-    int graph_valid = -1, graph_exact = -1;
-    std::string err;
-};
-
 static std::string g_batch_create_error;
 
-static int berr(sph_batch* b, int code, const char* fmt, ...) {
+int berr(sph_batch* b, int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
     va_start(ap, fmt);
@@ -164,13 +135,8 @@ static int berr(sph_batch* b, int code, const char* fmt, ...) {
     return code;
 }
 
-#define BCK(b, call)                                                                                  \
-    do {                                                                                              \
-        cudaError_t e_ = (call);                                                                      \
-        if (e_ != cudaSuccess) return berr(b, SPH_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));    \
-    } while (0)
-
 static void batch_free(sph_batch* b) {
+    sph_batch_adjoint_release(b);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     void* ptrs[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi, b->density,
                     b->mask, b->keys_a, b->idx_a, b->keys_b, b->idx_b, b->cell_start, b->cell_end, b->scene_of,
@@ -181,11 +147,11 @@ static void batch_free(sph_batch* b) {
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
 }
 
-static sphk::ManyScenes batch_scenes(const sph_batch* b) {
+sphk::ManyScenes batch_scenes(const sph_batch* b) {
     return sphk::ManyScenes{b->d_table, b->d_cbase, b->keys_a, b->cell_bits};
 }
 
-static int batch_enqueue_step(sph_batch* b, float dt) {
+int batch_enqueue_step(sph_batch* b, float dt) {
     cudaStream_t st = b->stream;
     uint32_t* hkeys = (b->passes & 1) ? b->keys_b : b->keys_a;
     uint32_t* hidx = (b->passes & 1) ? b->idx_b : b->idx_a;
@@ -218,8 +184,8 @@ static int batch_enqueue_step(sph_batch* b, float dt) {
                                (size_t)b->nslots, b->cell_start, b->cell_end, b->info_nb, scenes, b->unit != 0,
                                b->nvalid, st);
     sphk::launch_force_batch(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->cell_start, b->cell_end,
-                             b->info_nb, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, scenes, b->unit != 0, dt,
-                             b->exact, b->nvalid, st);
+                             b->info_nb, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, b->keep_f, b->keep_v, scenes,
+                             b->unit != 0, dt, b->exact, b->nvalid, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return berr(b, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
     return SPH_OK;
@@ -368,6 +334,48 @@ int sph_batch_set_stream(sph_batch* b, void* stream) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
+    return SPH_OK;
+}
+
+int sph_batch_set_params(sph_batch* b, int scene, const SPHParams* sphp) {
+    if (!b || !sphp || scene < 0 || scene >= b->nscenes) return berr(b, SPH_EINVAL, "sph_batch_set_params: bad arguments");
+    if (sphp->simulation_scale != b->sp[scene].simulation_scale)
+        return berr(b, SPH_EINVAL, "sph_batch_set_params: simulation_scale cannot change (it sets the grid)");
+    cudaSetDevice(b->device);
+    SPHParams sp = *sphp;
+    sp.max_num = b->max_num[scene];
+    sp.num = b->num[scene];
+    StepParams P;
+    std::string e;
+    if (sph_make_step_params(sp, b->gp[scene], b->gps[scene], P, e) != SPH_OK)
+        return berr(b, SPH_EINVAL, "scene %d: %s", scene, e.c_str());
+    b->sp[scene] = sp;
+    b->P[scene] = P;
+    BCK(b, cudaMemcpyAsync(b->d_table + scene, &b->P[scene], sizeof(StepParams), cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    b->params_version++;
+    return SPH_OK;
+}
+
+int sph_batch_get_params(sph_batch* b, int scene, SPHParams* sphp) {
+    if (!b || !sphp || scene < 0 || scene >= b->nscenes) return berr(b, SPH_EINVAL, "sph_batch_get_params: bad arguments");
+    *sphp = b->sp[scene];
+    return SPH_OK;
+}
+
+int sph_batch_get_device_ptr(sph_batch* b, int field, void** dptr) {
+    if (!b || !dptr) return SPH_EINVAL;
+    switch (field) {
+        case SPH_FIELD_POS_U: *dptr = b->pos_u; return SPH_OK;
+        case SPH_FIELD_VEL_U: *dptr = b->vel_u; return SPH_OK;
+        case SPH_FIELD_VELEVAL_U: *dptr = b->veleval_u; return SPH_OK;
+        default: return berr(b, SPH_EINVAL, "sph_batch_get_device_ptr: only pos_u, vel_u, veleval_u");
+    }
+}
+
+int sph_batch_slot_offset(sph_batch* b, int scene, int* offset) {
+    if (!b || !offset || scene < 0 || scene >= b->nscenes) return SPH_EINVAL;
+    *offset = (int)b->slot_off[scene];
     return SPH_OK;
 }
 

@@ -1,0 +1,59 @@
+// sph_batch.cuh — the batch behind the sph_batch* handle of
+// include/rtps_sph.h, shared by sph_batch.cu (buffers, the batched step) and
+// sph_adjoint.cu (the batched differentiable rollout).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "sph_device.cuh"
+
+constexpr int kBatchFrozen = 5;       // info slot: frozen particles seen by the last step
+constexpr int kBatchFrozenTotal = 6;  // info slot: frozen particle-steps since the last reset
+
+struct sph_batch_adjoint;  // recorded batched rollout (sph_adjoint.cu)
+
+struct sph_batch {
+    int device = 0, nscenes = 0, exact = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    std::vector<SPHParams> sp;
+    std::vector<GridParams> gp, gps;
+    std::vector<sphk::StepParams> P;
+    std::vector<int> max_num, num;
+    std::vector<uint32_t> slot_off, cbase;
+    int nslots = 0, nvalid = 0, cell_bits = 0, scene_bits = 0, passes = 1, tiles_cap = 0, unit = 1;
+    size_t ncells_total = 0;
+    uint32_t invalid_key = 0;
+    unsigned params_version = 1;
+    // device
+    float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr, *pos_s = nullptr, *veleval_s = nullptr;
+    float4 *rec_pd = nullptr, *rec_vi = nullptr;
+    float* density = nullptr;
+    uint32_t *mask = nullptr, *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
+    uint32_t *cell_start = nullptr, *cell_end = nullptr;
+    uint16_t* scene_of = nullptr;
+    uint32_t *d_slot_off = nullptr, *d_cbase = nullptr;
+    int* d_num = nullptr;
+    sphk::StepParams* d_table = nullptr;
+    int *info_sort = nullptr, *info_nb = nullptr;
+    uint32_t *hist = nullptr, *status = nullptr;
+    int* host_info = nullptr;
+    // tape outputs of the fused force pass (see sph_ctx::keep_f)
+    float4 *keep_f = nullptr, *keep_v = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    float graph_dt = 0.f;
+    int graph_valid = -1, graph_exact = -1;
+    sph_batch_adjoint* adj = nullptr;
+    std::string err;
+};
+
+int berr(sph_batch* b, int code, const char* fmt, ...);
+sphk::ManyScenes batch_scenes(const sph_batch* b);
+int batch_enqueue_step(sph_batch* b, float dt);
+void sph_batch_adjoint_release(sph_batch* b);
+
+#define BCK(b, call)                                                                                  \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return berr(b, SPH_ECUDA, "%s: %s", #call, cudaGetErrorString(e_));    \
+    } while (0)

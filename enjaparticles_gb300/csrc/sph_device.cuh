@@ -70,6 +70,7 @@ struct OneScene {
     __device__ __forceinline__ const StepParams& params(int) const { return P; }
     __device__ __forceinline__ uint32_t cell_base(int) const { return 0u; }
     __device__ __forceinline__ bool frozen(int) const { return false; }
+    __device__ __forceinline__ uint32_t scene(int) const { return 0u; }
 };
 struct ManyScenes {
     const StepParams* table;
@@ -150,8 +151,9 @@ void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* d
                           const ManyScenes& scenes, bool unit, int grid_items, cudaStream_t st);
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                         size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                        uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const ManyScenes& scenes,
-                        bool unit, float dt, int exact, int grid_items, cudaStream_t st);
+                        uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,
+                        float4* keep_v, const ManyScenes& scenes, bool unit, float dt, int exact, int grid_items,
+                        cudaStream_t st);
 void launch_collision(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info,
                       const StepParams& p, int grid_items, cudaStream_t st);
 void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,

@@ -260,10 +260,11 @@ void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_v
 
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                         size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                        uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const ManyScenes& scenes,
-                        bool unit, float dt, int exact, int grid_items, cudaStream_t st) {
+                        uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,
+                        float4* keep_v, const ManyScenes& scenes, bool unit, float dt, int exact, int grid_items,
+                        cudaStream_t st) {
     launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, cell_end, info, nullptr, nullptr, idx,
-                   nullptr, pos_u, vel_u, veleval_u, nullptr, nullptr, scenes, unit, dt, 1, exact, grid_items, st);
+                   nullptr, pos_u, vel_u, veleval_u, keep_f, keep_v, scenes, unit, dt, 1, exact, grid_items, st);
 }
 
 }  // namespace sphk

@@ -325,6 +325,15 @@ int sph_adjoint_backward(sph_ctx* ctx, const sph_float4* dL_dpos, const sph_floa
 int sph_adjoint_rollout(sph_ctx* ctx, int nsteps, int K, const sph_float4* dL_dpos_final,
                         sph_float4* dL_dvel0, float* dL_dvisc);
 
+/* Put the recorded rollout's initial state back into the context (for the
+ * next iteration of an optimisation loop).  Blocking. */
+int sph_adjoint_rewind(sph_ctx* ctx);
+
+/* Mean squared distance of the current positions to target (device, num
+ * float4, original order): *loss = (1/num) sum |x_i - x*_i|^2 (FP64 sum) and
+ * dL_dpos (device, num float4) = 2 (x_i - x*_i) / num.  Blocking. */
+int sph_loss_mse(sph_ctx* ctx, const sph_float4* target, sph_float4* dL_dpos, double* loss);
+
 /* ---------------------------------------------------------------------------
  * Batches: many independent systems ("scenes", each with its own SPHParams,
  * grid and particle count) stepped together.  No counterpart in the
@@ -354,6 +363,32 @@ int sph_batch_download(sph_batch* batch, int scene, int field, void* host, int n
 int sph_batch_out_of_grid(sph_batch* batch, int* count);
 int sph_batch_sync(sph_batch* batch);
 int sph_batch_last_error(sph_batch* batch, char* buf, int len);
+/* Replace scene `scene`'s SPHParams (same simulation_scale; the grid stays).
+ * Blocking. */
+int sph_batch_set_params(sph_batch* batch, int scene, const SPHParams* sphp);
+int sph_batch_get_params(sph_batch* batch, int scene, SPHParams* sphp);
+/* Device address of pos_u / vel_u / veleval_u of the whole batch: one float4
+ * per particle slot, scene s's particles at slots [offset_s, offset_s + num_s)
+ * (sph_batch_slot_offset). */
+int sph_batch_get_device_ptr(sph_batch* batch, int field, void** dptr);
+int sph_batch_slot_offset(sph_batch* batch, int scene, int* offset);
+
+/* Differentiable rollout of every scene at once (see sph_adjoint_record):
+ * one launch sequence per step and per reverse step for all scenes, the
+ * viscosity gradient per scene.  Arrays are DEVICE pointers in slot layout
+ * (one float4 per particle slot; unused slots are ignored on input and
+ * unspecified on output); dL_dvisc is a host array of nscenes doubles.
+ * Needs every particle to stay inside its scene's grid (SPH_EOOB).
+ * Blocking. */
+int sph_batch_adjoint_record(sph_batch* batch, float dt, int nsteps, int K);
+int sph_batch_adjoint_backward(sph_batch* batch, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
+                               const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0,
+                               sph_float4* dL_dveleval0, double* dL_dvisc);
+int sph_batch_adjoint_rewind(sph_batch* batch);
+/* Per-scene mean squared distance to target (device, slot layout): loss (host,
+ * nscenes doubles) and its gradient dL_dpos (device, slot layout; zero in
+ * unused slots).  Blocking. */
+int sph_batch_loss_mse(sph_batch* batch, const sph_float4* target, sph_float4* dL_dpos, double* loss);
 
 /* Sort n (key, value) pairs held in caller-owned device memory, without
  * allocating any device memory.  No counterpart in the reference.

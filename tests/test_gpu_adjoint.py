@@ -179,7 +179,7 @@ def test_adjoint_rollout_case_matches_fd64():
     (sp, gs, pos, vel, ve, target), (gp, gv, ge, gmu, pT, loss) = _rollout_case_grads(n, steps, K)
     assert np.isfinite(gv).all() and np.isfinite(gmu)
     scale = np.abs(gv[:, :3]).max()
-    checked, offset, errs = 0, 0, []
+    checked, offset, errs, detail = 0, 0, [], []
     while checked < 32:
         coords, offset = sample_coordinates(n, 1, seed=13, offset=offset)
         (i, a), = coords
@@ -187,7 +187,11 @@ def test_adjoint_rollout_case_matches_fd64():
         if not same_branches:
             continue
         errs.append(_check("vel[%d,%d]" % (i, a), float(gv[i, a]), fd, 1e-3 * scale))
+        detail.append((errs[-1], i, a, float(gv[i, a]), fd))
         checked += 1
+    for e, i, a, got, want in sorted(detail, reverse=True)[:4]:
+        print("  vel[%d,%d]: adjoint %.6e FD %.6e rel %.2e (|FD|/max|grad| %.2e)" % (i, a, got, want, e,
+                                                                                     abs(want) / scale))
     # the viscosity moves every particle: shrink eps until no branch flips
     for eps in (1e-4, 1e-5, 1e-6, 1e-7):
         fd, same_branches, _ = fd_gradient(sp, gs, pos, vel, ve, DT, steps, "visc", None, eps, target=target)
