@@ -323,15 +323,16 @@ def bench_calibration(args, torch):
     """Batched differentiable calibration: 64 dam-break scenes, N_s ~
     U{8192..65536} (seed 21), hidden viscosities mu_s ~ U[0.005, 0.05]
     (seed 22); targets = the final positions of 100-step runs with the hidden
-    viscosities; 50 batched gradient iterations on every mu_s from 0.02, each
-    a 100-step recorded rollout (checkpoint every 10 steps), the per-scene
-    loss and one batched backward pass.  value = scenes * iterations / s over
-    the whole loop."""
+    viscosities, kept at the checkpoint times; 50 batched gradient iterations
+    on every mu_s from 0.02, each a 100-step recorded rollout (checkpoint every
+    10 steps), the per-scene trajectory loss (mean squared distance at the 10
+    checkpoint times) and one batched backward pass.  value = scenes *
+    iterations / s over the whole loop."""
     import time
     import numpy as np
     from enjaparticles_gb300 import abi, scenes
     from enjaparticles_gb300.batch import Batch, dambreak_batch_scenes
-    from enjaparticles_gb300.calibrate import calibrate_viscosity
+    from enjaparticles_gb300.calibrate import calibrate_viscosity, record_targets
     S, steps = args.cal_scenes, args.cal_steps
     ns, _ = dambreak_batch_scenes(S, seed_n=21, n_lo=8192, n_hi=65536)
     hidden = [float(np.float32(0.005 + u * 0.045)) for u in scenes.uniform(22, S)]
@@ -341,17 +342,11 @@ def bench_calibration(args, torch):
     b.set_stream(torch.cuda.current_stream().cuda_stream)
     for k, (pos, vel) in enumerate(data):
         b.upload(k, pos, vel)
-    b.step(DT, steps)
-    tgt = np.zeros((b.nslots, 4), np.float32)
-    for k, off in enumerate(b.slot_offsets()):
-        tgt[off:off + ns[k]] = b.get(k, "pos_u")
-    target = torch.from_numpy(tgt).cuda()
-    for k, (pos, vel) in enumerate(data):
-        b.upload(k, pos, vel)
+    targets = record_targets(b, hidden, steps, args.cal_k, DT, torch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    mu, hist = calibrate_viscosity(b, target.data_ptr(), [0.02] * S, iterations=args.cal_iters, nsteps=steps,
-                                   K=args.cal_k, dt=DT)
+    mu, hist = calibrate_viscosity(b, targets, [0.02] * S, iterations=args.cal_iters, nsteps=steps, K=args.cal_k,
+                                   dt=DT)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
     b.close()
@@ -363,7 +358,7 @@ def bench_calibration(args, torch):
             "mu_rel_err_median": float(np.median(err / hidden)), "mu_rel_err_max": float((err / hidden).max()),
             "loss_first_median": float(np.median(hist[0][0])), "loss_last_median": float(np.median(hist[-1][0])),
             "start_mu": 0.02,
-            "note": "host wall clock around the whole loop (rollouts, losses, backward passes, Adam on log mu)"}
+            "note": "host wall clock around the whole loop (rollouts, losses, backward passes, iRprop- steps on log mu)"}
 
 
 def config_block(n, c):

@@ -114,6 +114,9 @@ SIGNATURES = {
     "sph_batch_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "sph_batch_adjoint_rewind": (_I, [_P]),
     "sph_batch_loss_mse": (_I, [_P, _P, _P, _P]),
+    "sph_batch_trajectory": (_I, [_P, _P]),
+    "sph_batch_loss_traj": (_I, [_P, _P, _P, _F, _P]),
+    "sph_batch_adjoint_backward_traj": (_I, [_P, _P, _P, _P, _P, _P]),
     "sph_adjoint_rewind": (_I, [_P]),
     "sph_loss_mse": (_I, [_P, _P, _P, C.POINTER(C.c_double)]),
     "sph_sort_pairs_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P]),

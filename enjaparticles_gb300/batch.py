@@ -115,6 +115,24 @@ class Batch:
     def adjoint_rewind(self):
         self._ck(self.lib.sph_batch_adjoint_rewind(self.h))
 
+    def trajectory(self, out):
+        """Positions at the recorded rollout's checkpoint times into out (device
+        address of nck * nslots float4)."""
+        self._ck(self.lib.sph_batch_trajectory(self.h, out))
+
+    def loss_traj(self, targets, grads, huber=0.0):
+        """Per-scene trajectory loss (sph_batch_loss_traj); huber = 0: mean
+        squared distance, else Huber with delta = huber * h."""
+        out = (C.c_double * self.nscenes)()
+        self._ck(self.lib.sph_batch_loss_traj(self.h, targets, grads, float(huber), C.cast(out, C.c_void_p)))
+        return list(out)
+
+    def adjoint_backward_traj(self, grads, out_pos=None, out_vel=None, out_veleval=None):
+        g = (C.c_double * self.nscenes)()
+        self._ck(self.lib.sph_batch_adjoint_backward_traj(self.h, grads, out_pos, out_vel, out_veleval,
+                                                          C.cast(g, C.c_void_p)))
+        return list(g)
+
     def loss_mse(self, target, grad):
         """Per-scene mean squared distance of pos_u to target (device address,
         slot layout); writes its gradient to grad (device address)."""

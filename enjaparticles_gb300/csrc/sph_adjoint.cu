@@ -356,14 +356,18 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_density(int n, const Scenes
 }
 
 // ---------------------------------------------------------------------------
-// Mean-squared-distance loss of the final positions, per scene, in FP64:
-//   L_s = (1/N_s) sum_{i in s} |x_i - x*_i|^2,   dL_s/dx_i = 2 (x_i - x*_i) / N_s.
-// Slots past a scene's particle count get a zero gradient.
+// Distance loss of positions against targets, per scene, summed in FP64:
+//   L_s = (w/N_s) sum_{i in s} rho(|x_i - x*_i|)
+// with rho(d) = d^2 (mean squared distance, delta = 0) or the Huber function
+// rho(d) = d^2 for d <= delta, 2 delta d - delta^2 beyond, delta = huber * h_s
+// (h_s the scene's smoothing distance).  The gradient goes to grad; slots past
+// a scene's particle count get a zero gradient.
 __global__ void __launch_bounds__(256) k_loss_mse(const float4* __restrict__ pos, const float4* __restrict__ target,
                                                   float4* __restrict__ grad, int nslots,
                                                   const uint16_t* __restrict__ scene_of,
                                                   const uint32_t* __restrict__ slot_off,
-                                                  const int* __restrict__ num, int n_single,
+                                                  const int* __restrict__ num, int n_single, float weight,
+                                                  const StepParams* __restrict__ table, float huber,
                                                   double* __restrict__ loss) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t scene = ~0u;
@@ -376,15 +380,32 @@ __global__ void __launch_bounds__(256) k_loss_mse(const float4* __restrict__ pos
         if (valid) {
             const float4 x = __ldg(pos + t), y = __ldg(target + t);
             const float dx = x.x - y.x, dy = x.y - y.y, dz = x.z - y.z;
-            const float inv = 1.f / (float)cnt;
-            g = make_float4(2.f * inv * dx, 2.f * inv * dy, 2.f * inv * dz, 0.f);
+            const float inv = weight / (float)cnt;
+            const double d2 = (double)dx * dx + (double)dy * dy + (double)dz * dz;
+            const float delta = huber > 0.f ? huber * table[s].h : 0.f;
+            float gs = 2.f * inv;  // d rho / d x = gs * (x - x*)
+            double r = d2;
+            if (delta > 0.f && d2 > (double)delta * delta) {
+                const double d = sqrt(d2);
+                r = 2.0 * delta * d - (double)delta * delta;
+                gs = (float)(2.0 * delta / d) * inv;
+            }
+            g = make_float4(gs * dx, gs * dy, gs * dz, 0.f);
             scene = s;
             // the per-particle term rounded once; the sum is in double
-            v = (float)(((double)dx * dx + (double)dy * dy + (double)dz * dz) / (double)cnt);
+            v = (float)(r * (double)weight / (double)cnt);
         }
         grad[t] = g;
     }
     warp_add_double(loss, scene, v);
+}
+
+// x += seed (the loss gradient at an intermediate time), xyz lanes.
+__global__ void __launch_bounds__(256) k_add_seed(float4* __restrict__ x, const float4* __restrict__ seed, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = x[i], b = __ldg(seed + i);
+    x[i] = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, 0.f);
 }
 
 }  // namespace
@@ -401,6 +422,8 @@ struct AdjState {
     bool tape_keys = false;
     int cap_K = 0, cap_ckpt = 0;
     float4* ckpt = nullptr;  // [cap_ckpt][3][N]: pos, vel, veleval at steps 0, K, 2K, ..., then the final state
+    float4* seeds = nullptr; // [cap_seeds][N]: position-loss gradients at the checkpoint times
+    int cap_seeds = 0;
     uint32_t *t_idx = nullptr, *t_keys = nullptr, *t_cs = nullptr, *t_ce = nullptr, *t_mask = nullptr;
     float4 *t_pd = nullptr, *t_vi = nullptr, *t_f = nullptr, *t_v = nullptr;
     float4* xb[2] = {nullptr, nullptr};
@@ -415,6 +438,7 @@ struct AdjState {
     float g_dt = 0.f;
     unsigned g_version = 0;
     cudaStream_t g_stream = nullptr;
+    int g_seeded = -1;
 };
 struct sph_adjoint : AdjState {};
 struct sph_batch_adjoint : AdjState {};
@@ -439,7 +463,7 @@ void free_state(AdjState* a) {
     drop_graph(a);
     free_tape(a);
     void* ptrs[] = {a->ckpt, a->xb[0], a->xb[1], a->vb[0], a->vb[1], a->eb[0], a->eb[1], a->adj_a, a->adj_x,
-                    a->pbar, a->rhob, a->visc_acc};
+                    a->pbar, a->rhob, a->visc_acc, a->seeds};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (a->host_visc) cudaFreeHost(a->host_visc);
@@ -621,7 +645,7 @@ int batch_taped_step(sph_batch* b, int slot, float dt) {
 // state.  Starts from the adjoints in buffers 0; ends in buffers nsteps % 2.
 // Returns SPH_OK or the error of the first failing enqueue (set on the owner).
 template <class Owner, class TapedStep, class Reverse>
-int enqueue_backward(Owner* o, AdjState* a, float4* const st[3], cudaStream_t stream, TapedStep&& taped,
+int enqueue_backward(Owner* o, AdjState* a, float4* const st[3], cudaStream_t stream, bool seeded, TapedStep&& taped,
                      Reverse&& reverse, int (*fail)(Owner*, const char*, cudaError_t)) {
     const int T = a->nsteps, K = a->K;
     const int nseg = (T + K - 1) / K;
@@ -636,6 +660,11 @@ int enqueue_backward(Owner* o, AdjState* a, float4* const st[3], cudaStream_t st
             reverse(tape_step(a, t - t0), src);
             src = 1 - src;
         }
+        if (seeded) {
+            // the loss gradient with respect to the positions at time t0
+            const int n = (int)a->state_elems;
+            k_add_seed<<<(n + 255) / 256, 256, 0, stream>>>(a->xb[src], a->seeds + (size_t)s * a->N, n);
+        }
         if ((e = cudaGetLastError()) != cudaSuccess) return fail(o, "reverse kernels", e);
     }
     if ((e = copy_state(a, st, nseg, false, stream)) != cudaSuccess) return fail(o, "state restore", e);
@@ -649,12 +678,12 @@ int batch_fail(sph_batch* b, const char* what, cudaError_t e) {
     return berr(b, SPH_ECUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-bool graph_stale(const AdjState* a, cudaStream_t stream) {
+bool graph_stale(const AdjState* a, cudaStream_t stream, int seeded) {
     return !a->graph || a->g_nsteps != a->nsteps || a->g_K != a->K || a->g_n != a->n || a->g_exact != a->exact ||
-           a->g_dt != a->dt || a->g_version != a->params_version || a->g_stream != stream;
+           a->g_dt != a->dt || a->g_version != a->params_version || a->g_stream != stream || a->g_seeded != seeded;
 }
 
-void graph_key(AdjState* a, cudaStream_t stream) {
+void graph_key(AdjState* a, cudaStream_t stream, int seeded) {
     a->g_nsteps = a->nsteps;
     a->g_K = a->K;
     a->g_n = a->n;
@@ -662,6 +691,7 @@ void graph_key(AdjState* a, cudaStream_t stream) {
     a->g_dt = a->dt;
     a->g_version = a->params_version;
     a->g_stream = stream;
+    a->g_seeded = seeded;
 }
 
 // Loads the final-state adjoints (NULL: zero) into buffers 0 and clears the
@@ -798,7 +828,7 @@ int sph_adjoint_backward(sph_ctx* c, const sph_float4* dL_dpos, const sph_float4
     if (rc) return rc;
     sph_adjoint* a = c->adj;
     CK(c, load_seeds(a, dL_dpos, dL_dvel, dL_dveleval, c->stream));
-    if (graph_stale(a, c->stream)) {
+    if (graph_stale(a, c->stream, 0)) {
         drop_graph(a);
         float4* st[3];
         ctx_state(c, st);
@@ -806,7 +836,7 @@ int sph_adjoint_backward(sph_ctx* c, const sph_float4* dL_dpos, const sph_float4
         CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         const sphk::OneScene R{c->P};
         rc = enqueue_backward(
-            c, a, st, c->stream, [&](int slot) { return ctx_taped_step(c, slot); },
+            c, a, st, c->stream, false, [&](int slot) { return ctx_taped_step(c, slot); },
             [&](const TapeStep& T, int src) { launch_reverse(a, R, T, src, c->stream); }, ctx_fail);
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         if (rc) {
@@ -820,7 +850,7 @@ int sph_adjoint_backward(sph_ctx* c, const sph_float4* dL_dpos, const sph_float4
             a->graph = nullptr;
             return set_err(c, SPH_ECUDA, "backward graph instantiate: %s", cudaGetErrorString(e));
         }
-        graph_key(a, c->stream);
+        graph_key(a, c->stream, 0);
     }
     CK(c, cudaGraphLaunch(a->graph, c->stream));
     CK(c, store_results(a, dL_dpos0, dL_dvel0, dL_dveleval0, c->stream));
@@ -870,7 +900,7 @@ int sph_loss_mse(sph_ctx* c, const sph_float4* target, sph_float4* dL_dpos, doub
     if (n > 0)
         k_loss_mse<<<blocks, 256, 0, c->stream>>>(c->pos_u, reinterpret_cast<const float4*>(target),
                                                   reinterpret_cast<float4*>(dL_dpos), n, nullptr, nullptr, nullptr, n,
-                                                  c->adj->visc_acc);
+                                                  1.f, nullptr, 0.f, c->adj->visc_acc);
     CK_LAUNCH(c);
     CK(c, cudaMemcpyAsync(c->adj->host_visc, c->adj->visc_acc, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     if ((rc = read_info(c))) return rc;
@@ -924,14 +954,15 @@ int sph_batch_adjoint_record(sph_batch* b, float dt, int nsteps, int K) {
     return SPH_OK;
 }
 
-int sph_batch_adjoint_backward(sph_batch* b, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
-                               const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0,
-                               sph_float4* dL_dveleval0, double* dL_dvisc) {
-    int rc = batch_adj_check(b);
-    if (rc) return rc;
+namespace {
+
+int batch_backward(sph_batch* b, bool seeded, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
+                   const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0, sph_float4* dL_dveleval0,
+                   double* dL_dvisc) {
     sph_batch_adjoint* a = b->adj;
+    int rc;
     BCK(b, load_seeds(a, dL_dpos, dL_dvel, dL_dveleval, b->stream));
-    if (graph_stale(a, b->stream)) {
+    if (graph_stale(a, b->stream, seeded)) {
         drop_graph(a);
         float4* st[3];
         batch_state(b, st);
@@ -939,7 +970,7 @@ int sph_batch_adjoint_backward(sph_batch* b, const sph_float4* dL_dpos, const sp
         BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         const float dt = a->dt;
         rc = enqueue_backward(
-            b, a, st, b->stream, [&](int slot) { return batch_taped_step(b, slot, dt); },
+            b, a, st, b->stream, seeded, [&](int slot) { return batch_taped_step(b, slot, dt); },
             [&](const TapeStep& T, int src) {
                 const sphk::ManyScenes R{b->d_table, b->d_cbase, T.keys, b->cell_bits};
                 launch_reverse(a, R, T, src, b->stream);
@@ -957,7 +988,7 @@ int sph_batch_adjoint_backward(sph_batch* b, const sph_float4* dL_dpos, const sp
             a->graph = nullptr;
             return berr(b, SPH_ECUDA, "backward graph instantiate: %s", cudaGetErrorString(e));
         }
-        graph_key(a, b->stream);
+        graph_key(a, b->stream, seeded);
     }
     BCK(b, cudaGraphLaunch(a->graph, b->stream));
     BCK(b, store_results(a, dL_dpos0, dL_dvel0, dL_dveleval0, b->stream));
@@ -965,6 +996,77 @@ int sph_batch_adjoint_backward(sph_batch* b, const sph_float4* dL_dpos, const sp
     if (dL_dvisc)
         for (int s = 0; s < b->nscenes; ++s) dL_dvisc[s] = a->host_visc[s];
     return SPH_OK;
+}
+
+int nseg_of(const AdjState* a) { return (a->nsteps + a->K - 1) / a->K; }
+
+}  // namespace
+
+int sph_batch_adjoint_backward(sph_batch* b, const sph_float4* dL_dpos, const sph_float4* dL_dvel,
+                               const sph_float4* dL_dveleval, sph_float4* dL_dpos0, sph_float4* dL_dvel0,
+                               sph_float4* dL_dveleval0, double* dL_dvisc) {
+    int rc = batch_adj_check(b);
+    if (rc) return rc;
+    return batch_backward(b, false, dL_dpos, dL_dvel, dL_dveleval, dL_dpos0, dL_dvel0, dL_dveleval0, dL_dvisc);
+}
+
+int sph_batch_trajectory(sph_batch* b, sph_float4* pos_traj) {
+    int rc = batch_adj_check(b);
+    if (rc) return rc;
+    if (!pos_traj) return berr(b, SPH_EINVAL, "sph_batch_trajectory: null array");
+    sph_batch_adjoint* a = b->adj;
+    const int nseg = nseg_of(a);
+    for (int c = 0; c <= nseg; ++c)
+        BCK(b, cudaMemcpyAsync(pos_traj + (size_t)c * a->N, ckpt_slot(a, c, 0), a->N * 16, cudaMemcpyDeviceToDevice,
+                               b->stream));
+    return sph_batch_sync(b);
+}
+
+int sph_batch_loss_traj(sph_batch* b, const sph_float4* targets, sph_float4* dL_dpos_traj, float huber,
+                        double* loss) {
+    int rc = batch_adj_check(b);
+    if (rc) return rc;
+    if (!targets || !dL_dpos_traj || !(huber >= 0.f)) return berr(b, SPH_EINVAL, "sph_batch_loss_traj: bad arguments");
+    sph_batch_adjoint* a = b->adj;
+    const int nseg = nseg_of(a);
+    const size_t N = a->N;
+    BCK(b, cudaMemsetAsync(a->visc_acc, 0, sizeof(double) * b->nscenes, b->stream));
+    BCK(b, cudaMemsetAsync(dL_dpos_traj, 0, N * 16, b->stream));  // time 0: the given initial positions
+    const float w = 1.f / (float)nseg;
+    const int blocks = (b->nslots + 255) / 256;
+    for (int c = 1; c <= nseg; ++c)
+        k_loss_mse<<<blocks, 256, 0, b->stream>>>(ckpt_slot(a, c, 0), reinterpret_cast<const float4*>(targets) + c * N,
+                                                  reinterpret_cast<float4*>(dL_dpos_traj) + c * N, b->nslots,
+                                                  b->scene_of, b->d_slot_off, b->d_num, 0, w, b->d_table, huber,
+                                                  a->visc_acc);
+    BCK(b, cudaGetLastError());
+    BCK(b, cudaMemcpyAsync(a->host_visc, a->visc_acc, sizeof(double) * b->nscenes, cudaMemcpyDeviceToHost,
+                           b->stream));
+    if ((rc = sph_batch_sync(b))) return rc;
+    if (loss)
+        for (int s = 0; s < b->nscenes; ++s) loss[s] = a->host_visc[s];
+    return SPH_OK;
+}
+
+int sph_batch_adjoint_backward_traj(sph_batch* b, const sph_float4* dL_dpos_traj, sph_float4* dL_dpos0,
+                                    sph_float4* dL_dvel0, sph_float4* dL_dveleval0, double* dL_dvisc) {
+    int rc = batch_adj_check(b);
+    if (rc) return rc;
+    if (!dL_dpos_traj) return berr(b, SPH_EINVAL, "sph_batch_adjoint_backward_traj: null array");
+    sph_batch_adjoint* a = b->adj;
+    const int nseg = nseg_of(a);
+    if (nseg + 1 > a->cap_seeds) {
+        if (a->seeds) cudaFree(a->seeds);
+        a->seeds = nullptr;
+        a->cap_seeds = 0;
+        drop_graph(a);
+        BCK(b, cudaMalloc((void**)&a->seeds, (size_t)(nseg + 1) * a->N * 16));
+        a->cap_seeds = nseg + 1;
+    }
+    BCK(b, cudaMemcpyAsync(a->seeds, dL_dpos_traj, (size_t)(nseg + 1) * a->N * 16, cudaMemcpyDeviceToDevice,
+                           b->stream));
+    return batch_backward(b, true, dL_dpos_traj + (size_t)nseg * a->N, nullptr, nullptr, dL_dpos0, dL_dvel0,
+                          dL_dveleval0, dL_dvisc);
 }
 
 int sph_batch_adjoint_rewind(sph_batch* b) {
@@ -994,7 +1096,7 @@ int sph_batch_loss_mse(sph_batch* b, const sph_float4* target, sph_float4* dL_dp
     const int blocks = (b->nslots + 255) / 256;
     k_loss_mse<<<blocks, 256, 0, b->stream>>>(b->pos_u, reinterpret_cast<const float4*>(target),
                                               reinterpret_cast<float4*>(dL_dpos), b->nslots, b->scene_of,
-                                              b->d_slot_off, b->d_num, 0, a->visc_acc);
+                                              b->d_slot_off, b->d_num, 0, 1.f, nullptr, 0.f, a->visc_acc);
     BCK(b, cudaGetLastError());
     BCK(b, cudaMemcpyAsync(a->host_visc, a->visc_acc, sizeof(double) * b->nscenes, cudaMemcpyDeviceToHost,
                            b->stream));

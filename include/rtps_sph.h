@@ -390,6 +390,28 @@ int sph_batch_adjoint_rewind(sph_batch* batch);
  * unused slots).  Blocking. */
 int sph_batch_loss_mse(sph_batch* batch, const sph_float4* target, sph_float4* dL_dpos, double* loss);
 
+/* Trajectory form (losses on the positions at the checkpoint times 0, K, 2K,
+ * ..., nsteps of the recorded rollout; nck = ceil(nsteps / K) + 1 of them).
+ * Arrays of positions or gradients over the trajectory are DEVICE pointers of
+ * nck * nslots float4, time-major (checkpoint c at offset c * nslots).
+ *   sph_batch_trajectory      copy the recorded positions at those times
+ *   sph_batch_loss_traj       per scene, the mean over the times 1..nck-1 of
+ *                             (1/N_s) sum_i rho(|x_i - x*_i|), and its
+ *                             gradient (zero at time 0); rho(d) = d^2 when
+ *                             huber = 0, else the Huber function with
+ *                             delta = huber * smoothing_distance of the scene
+ *                             (quadratic up to delta, linear beyond: a few
+ *                             particles far from their targets cannot
+ *                             dominate the loss)
+ *   sph_batch_adjoint_backward_traj  backward pass with a position-loss
+ *                             gradient at every checkpoint time
+ * All blocking. */
+int sph_batch_trajectory(sph_batch* batch, sph_float4* pos_traj);
+int sph_batch_loss_traj(sph_batch* batch, const sph_float4* targets, sph_float4* dL_dpos_traj, float huber,
+                        double* loss);
+int sph_batch_adjoint_backward_traj(sph_batch* batch, const sph_float4* dL_dpos_traj, sph_float4* dL_dpos0,
+                                    sph_float4* dL_dvel0, sph_float4* dL_dveleval0, double* dL_dvisc);
+
 /* Sort n (key, value) pairs held in caller-owned device memory, without
  * allocating any device memory.  No counterpart in the reference.
  *

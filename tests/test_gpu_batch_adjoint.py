@@ -7,7 +7,7 @@ import torch
 
 from enjaparticles_gb300 import abi
 from enjaparticles_gb300.batch import Batch, dambreak_batch_scenes
-from enjaparticles_gb300.calibrate import calibrate_viscosity
+from enjaparticles_gb300.calibrate import calibrate_viscosity, checkpoints, record_targets
 from enjaparticles_gb300.scenes import dambreak, uniform
 from enjaparticles_gb300.sph import SPH
 
@@ -87,24 +87,54 @@ def test_batch_loss_matches_numpy():
     b.close()
 
 
+def test_batch_trajectory_backward_seeds_intermediate_times():
+    """A loss gradient injected at checkpoint time 8 of a 12-step rollout gives
+    the same initial-state gradients as the 8-step rollout seeded at its end."""
+    ns = [3000, 6000]
+    params = [abi.dambreak_params(n, mu) for n, mu in zip(ns, (0.01, 0.03))]
+    data = [dambreak(n, scene=20 + k, velocity_sigma=0.2, velocity_seed=90 + k) for k, n in enumerate(ns)]
+    b = Batch(params, ns)
+
+    def load():
+        for k, (pos, vel) in enumerate(data):
+            b.upload(k, pos, vel)
+
+    seed = _slot_tensor(b, [(2.0 * uniform(95 + k, 4 * n) - 1.0).reshape(n, 4) for k, n in enumerate(ns)])
+    seed[:, 3] = 0
+    load()
+    b.adjoint_record(DT, 8, 4)
+    v8 = torch.zeros_like(seed)
+    torch.cuda.synchronize()
+    mu8 = b.adjoint_backward(dpos=seed.data_ptr(), out_vel=v8.data_ptr())
+    load()
+    b.adjoint_record(DT, 12, 4)
+    grads = torch.zeros((checkpoints(12, 4), b.nslots, 4), dtype=torch.float32, device="cuda")
+    grads[2] = seed
+    v12 = torch.zeros_like(seed)
+    torch.cuda.synchronize()
+    mu12 = b.adjoint_backward_traj(grads.data_ptr(), out_vel=v12.data_ptr())
+    for k, (n, off) in enumerate(zip(ns, b.slot_offsets())):
+        assert torch.equal(v8[off:off + n, :3], v12[off:off + n, :3])
+        assert abs(mu8[k] - mu12[k]) <= 1e-9 * abs(mu8[k])
+    b.close()
+
+
 def test_batch_calibration_recovers_viscosity():
-    """8 scenes with hidden viscosities: 30 batched gradient steps from 0.02."""
+    """8 scenes with hidden viscosities: 30 batched gradient steps from 0.02
+    on the trajectory loss."""
     S, steps, K = 8, 60, 10
     ns, _ = dambreak_batch_scenes(S, seed_n=21, n_lo=4096, n_hi=12000)
     hidden = [float(np.float32(0.005 + u * 0.045)) for u in uniform(22, S)]
-    params = [abi.dambreak_params(n, mu) for n, mu in zip(ns, hidden)]
+    params = [abi.dambreak_params(n, 0.02) for n in ns]
     data = [dambreak(n, scene=k) for k, n in enumerate(ns)]
     b = Batch(params, ns)
     for k, (pos, vel) in enumerate(data):
         b.upload(k, pos, vel)
-    b.step(DT, steps)
-    target = _slot_tensor(b, [b.get(k, "pos_u") for k in range(S)])
-    for k, (pos, vel) in enumerate(data):
-        b.upload(k, pos, vel)
-    mu, hist = calibrate_viscosity(b, target.data_ptr(), [0.02] * S, iterations=30, nsteps=steps, K=K, dt=DT)
+    targets = record_targets(b, hidden, steps, K, DT, torch)
+    mu, hist = calibrate_viscosity(b, targets, [0.02] * S, iterations=30, nsteps=steps, K=K, dt=DT)
     err = np.abs(mu - np.asarray(hidden)) / np.asarray(hidden)
     print("calibration: hidden %s\n recovered %s\n rel err %s\n loss %s -> %s" % (
         np.round(hidden, 5), np.round(mu, 5), np.round(err, 4), hist[0][0], hist[-1][0]))
-    assert np.median(err) < 0.05
+    assert np.max(err) < 0.05
     assert (hist[-1][0] <= hist[0][0]).all()
     b.close()
