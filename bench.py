@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-n", type=int, default=131072, help="particles per step of the reference (CPU) arm")
+    ap.add_argument("--ref-seconds", type=float, default=120.0, help="time bound of the reference (CPU) arm")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=100)
@@ -173,35 +173,48 @@ def cpu_baseline_port(n, seconds):
 
 
 def run_reference(args):
+    """The reference arm: the reference's SPH step on the host cores, on the
+    same 2,097,152-particle dam break.  The reference's own kernels are OpenCL
+    and need an OpenCL driver, which these machines lack; they also compile
+    for the host here (oracle/_ref) but only where the reference tree is, and
+    x86 builds do not run on the Arm GPU hosts.  The oracle's port of those
+    kernels (bit-identical to them on the host, all host threads) stands in.
+    Each step is one full step of the whole system; the run stops after
+    --steps steps or --ref-seconds seconds, whichever comes first."""
     rank, _, world = dist_env()
     if rank != 0:
         return 0
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_bind
     from enjaparticles_gb300 import abi, scenes
-    n = args.ref_n
+    n = args.n
     sp, g, gs = abi.dambreak_params(n)
     pos, vel = scenes.dambreak(n)
     sim = oracle_bind.OracleSim(sp, g, gs, n)
     sim.upload(pos, vel)
-    sim.step(DT, args.warmup)
-    t0 = time.perf_counter()
-    sim.step(DT, args.steps)
+    warm = min(args.warmup, 2)
+    sim.step(DT, warm)
+    steps, t0 = 0, time.perf_counter()
+    while steps < args.steps:
+        sim.step(DT, 1)
+        steps += 1
+        if time.perf_counter() - t0 >= args.ref_seconds:
+            break
     el = time.perf_counter() - t0
-    value = n * args.steps / el
+    value = n * steps / el
     threads = oracle_bind.oracle().oracle_threads()
     line = {
         "metric": "particle-updates/s at 2M SPH", "value": value, "unit": "particle-updates/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / max(args.steps, 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config_block(args.n, None),
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / max(steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded dam-break lattice, zero initial velocity)",
+        "config": config_block(n, g.nb_cells),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads, "kind": "port",
-                         "sample": "each step: one full SPH step of a %d-particle dam break (same lattice rule and "
-                                   "physics as the 2,097,152-particle workload) on %d host threads; the reference's "
-                                   "OpenCL kernels need an OpenCL driver, which these machines lack, so the CPU "
-                                   "port of those kernels (bit-identical to them on the host) stands in" % (
-                                       n, threads)},
+                         "sample": "%d full SPH steps of the %d-particle dam break after %d warm-up steps (%.1f s; "
+                                   "time-bounded at %.0f s) on %d host threads: the oracle's port of the "
+                                   "reference's OpenCL kernels (bit-identical to them on the host)" % (
+                                       steps, n, warm, el, args.ref_seconds, threads)},
         "e2e": {"value": value, "unit": "particle-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -375,9 +388,8 @@ def main():
     rank, local_rank, world = dist_env()
     import torch
     torch.cuda.set_device(local_rank)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    from enjaparticles_gb300.replicas import Replicas
+    reps = Replicas(device=torch.device("cuda", local_rank))
     from enjaparticles_gb300 import abi, scenes
     from enjaparticles_gb300.sph import SPH
     import ctypes as C
@@ -393,17 +405,8 @@ def main():
     torch.cuda.set_stream(stream)
     abi.check(lib, s.ctx, lib.sph_set_stream(s.ctx, C.c_void_p(stream.cuda_stream)))
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    barrier = reps.barrier
+    max_over_ranks = reps.max
 
     sampler = ClockSampler(torch.cuda.current_device())
     # --- device-resident throughput (graph replay) --------------------------
@@ -508,8 +511,7 @@ def main():
     if rank == 0:
         print(json.dumps(line))
     s.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    reps.close()
     return 0
 
 

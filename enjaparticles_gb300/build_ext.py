@@ -14,6 +14,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librtps_sph.so")
+DRIVER = os.path.join(PKG, "sph_bench")
 
 SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cells.cu", "sph_density.cu", "sph_force.cu", "sph_integrate.cu",
            "sph_batch.cu", "sph_noalloc.cu", "sph_adjoint.cu", "sph_params.cpp"]
@@ -63,9 +64,24 @@ def build(verbose=False, ptxas_verbose=False):
     if r.returncode:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB)
+    build_driver()
     for line in logs:
         print(line)
     return LIB
+
+
+def build_driver():
+    """The headless C++ driver (driver/sph_bench.cpp) over include/rtps_sph.hpp,
+    linked against librtps_sph.so (found next to it at run time)."""
+    src = os.path.join(PKG, "driver", "sph_bench.cpp")
+    tmp = DRIVER + ".tmp"
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", src, "-o", tmp, "-I",
+           os.path.join(PKG, "..", "include"), "-L", PKG, "-lrtps_sph", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("driver build failed:\n" + r.stdout + r.stderr)
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

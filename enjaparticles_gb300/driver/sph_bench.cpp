@@ -1,0 +1,137 @@
+// sph_bench.cpp — headless C++ driver of the SPH step through the rtps::SPH
+// class (include/rtps_sph.hpp), the way a reference frame loop drives
+// rtps::SPH (test/glwidget.cpp:876-916, test/benchmarks/rb_sph_benchmark.cpp:
+// 162-198), without a window.
+//
+// Builds the dam-break scene of n particles (the seeded jittered lattice of
+// enjaparticles_gb300/scenes.py, same numbers), steps it, and prints one JSON
+// line: particle-updates/s and an FP64 checksum of the final positions.
+//
+//   sph_bench [--n N] [--steps S] [--warmup W] [--dt DT] [--viscosity MU]
+//             [--frames] [--exact]
+//   --frames: one update()+integrate() pair per step (the reference's frame
+//             loop, staged kernels) instead of the fused graph-replayed step.
+//   sph_bench --n N --dump-scene FILE: write the scene's positions (N x 4
+//             float32) to FILE and exit (no GPU needed).
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rtps_sph.hpp"
+
+namespace {
+
+uint64_t splitmix64(uint64_t seed, uint64_t k) {
+    uint64_t z = seed + k * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// k-th (from 0) double in [0, 1) of the stream `seed`.
+double uniform(uint64_t seed, uint64_t k) {
+    return (double)(splitmix64(seed, k + 1) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+float lattice_spacing(int n) { return (float)std::pow(0.125 / n, 1.0 / 3.0); }
+
+// Points ((i+1/2)s, (j+1/2)s, (k+1/2)s), z outermost, each coordinate
+// jittered by U(-0.01 s, 0.01 s).
+std::vector<rtps::float4> dambreak_positions(int n, uint64_t seed) {
+    const double s = lattice_spacing(n);
+    const long side = (long)std::ceil(0.5 / s - 1e-9), layer = side * side;
+    std::vector<rtps::float4> pos((size_t)n);
+    for (long k = 0; k < n; ++k) {
+        const long iz = k / layer, rem = k % layer, iy = rem / side, ix = rem % side;
+        double jit[3];
+        for (int a = 0; a < 3; ++a) jit[a] = (2.0 * uniform(seed, 3 * (uint64_t)k + a) - 1.0) * (0.01 * s);
+        pos[k] = rtps::make_float4((float)((ix + 0.5) * s + jit[0]), (float)((iy + 0.5) * s + jit[1]),
+                                   (float)((iz + 0.5) * s + jit[2]), 1.0f);
+    }
+    return pos;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    int n = 262144, steps = 200, warmup = 10, frames = 0, exact = 0;
+    float dt = 0.001f, mu = 0.01f;
+    std::string dump;
+    for (int i = 1; i < argc; ++i) {
+        const std::string a = argv[i];
+        auto next = [&]() -> const char* {
+            if (i + 1 >= argc) {
+                std::fprintf(stderr, "missing value for %s\n", a.c_str());
+                std::exit(2);
+            }
+            return argv[++i];
+        };
+        if (a == "--n") n = std::atoi(next());
+        else if (a == "--steps") steps = std::atoi(next());
+        else if (a == "--warmup") warmup = std::atoi(next());
+        else if (a == "--dt") dt = (float)std::atof(next());
+        else if (a == "--viscosity") mu = (float)std::atof(next());
+        else if (a == "--frames") frames = 1;
+        else if (a == "--exact") exact = 1;
+        else if (a == "--dump-scene") dump = next();
+        else {
+            std::fprintf(stderr, "unknown argument %s\n", a.c_str());
+            return 2;
+        }
+    }
+    if (n <= 0 || steps < 0 || warmup < 0) return 2;
+    if (!dump.empty()) {
+        const std::vector<rtps::float4> pos = dambreak_positions(n, 20250101ull);
+        FILE* f = std::fopen(dump.c_str(), "wb");
+        if (!f || std::fwrite(pos.data(), sizeof(rtps::float4), pos.size(), f) != pos.size()) return 1;
+        return std::fclose(f) == 0 ? 0 : 1;
+    }
+    SPHParams sp;
+    GridParams g, gs;
+    if (sph_dambreak_params(n, lattice_spacing(n), mu, &sp, &g, &gs) != SPH_OK) {
+        std::fprintf(stderr, "sph_dambreak_params failed\n");
+        return 1;
+    }
+    try {
+        rtps::SPH sph(sp, g, n, &gs, dt);
+        if (exact) sph_set_exact(sph.handle(), 1);
+        sph.pushParticles(dambreak_positions(n, 20250101ull), rtps::make_float4(0, 0, 0, 0));
+        auto frame = [&](int k) {
+            if (frames) {
+                for (int s = 0; s < k; ++s) {
+                    sph.acquireGLBuffers();
+                    sph.update();
+                    sph.interact();
+                    sph.integrate();
+                    sph.postProcess();
+                    sph.releaseGLBuffers();
+                }
+            } else {
+                sph.step(k);
+            }
+        };
+        frame(warmup);
+        sph.sync();
+        const auto t0 = std::chrono::steady_clock::now();
+        frame(steps);
+        sph.sync();
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        const std::vector<rtps::float4> p = sph.getPositions();
+        double sum = 0.0;
+        for (const rtps::float4& q : p) sum += (double)q.x + 2.0 * q.y + 3.0 * q.z;
+        std::printf("{\"metric\": \"particle-updates/s\", \"value\": %.6g, \"n\": %d, \"steps\": %d, \"warmup\": %d, "
+                    "\"seconds\": %.6g, \"mode\": \"%s\", \"exact\": %d, \"num_after\": %d, "
+                    "\"checksum\": %.17g, \"build\": \"%s\"}\n",
+                    steps > 0 && el > 0 ? (double)n * steps / el : 0.0, n, steps, warmup, el,
+                    frames ? "frames" : "fused", exact, sph.getNum(), sum, sph_build_info());
+    } catch (const rtps::SPHError& e) {
+        std::fprintf(stderr, "error %d: %s\n", e.code(), e.what());
+        return 1;
+    }
+    return 0;
+}

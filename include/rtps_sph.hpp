@@ -1,0 +1,183 @@
+// rtps_sph.hpp — header-only C++ class with the method names of the
+// reference's rtps::System / rtps::SPH (rtpslib/system/System.h:61-186,
+// rtpslib/system/SPH.h:56-155), forwarding to the C ABI of rtps_sph.h.
+//
+// A frame loop written against the reference (acquireGLBuffers -> update ->
+// interact -> integrate -> postProcess -> releaseGLBuffers, as in
+// test/glwidget.cpp:876-916) runs unchanged against this class.  Rendering
+// is not part of the library: the GL buffer calls are no-ops and the particle
+// arrays are device buffers (devicePointer) or host copies (getPositions).
+// Errors, which the reference prints and ignores, throw rtps::SPHError.
+#ifndef RTPS_SPH_HPP
+#define RTPS_SPH_HPP
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "rtps_sph.h"
+
+namespace rtps {
+
+typedef sph_float4 float4;
+
+inline float4 make_float4(float x, float y, float z, float w) {
+    float4 v;
+    v.x = x;
+    v.y = y;
+    v.z = z;
+    v.w = w;
+    return v;
+}
+
+class SPHError : public std::runtime_error {
+public:
+    SPHError(int code, const std::string& what) : std::runtime_error(what), code_(code) {}
+    int code() const { return code_; }
+
+private:
+    int code_;
+};
+
+// addRect (rtpslib/domain/IV.cpp:165-202): lattice points of spacing
+// `spacing` from min to max, z outermost, at most num of them.
+inline std::vector<float4> addRect(int num, float4 min, float4 max, float spacing, float scale) {
+    const float xmin = min.x / scale, xmax = max.x / scale;
+    const float ymin = min.y / scale, ymax = max.y / scale;
+    const float zmin = min.z / scale, zmax = max.z / scale;
+    std::vector<float4> rvec(num > 0 ? num : 0);
+    int i = 0;
+    for (float z = zmin; z <= zmax; z += spacing)
+        for (float y = ymin; y <= ymax; y += spacing)
+            for (float x = xmin; x <= xmax; x += spacing) {
+                if (i >= num) break;
+                rvec[i] = make_float4(x, y, z, 1.0f);
+                ++i;
+            }
+    rvec.resize(i);
+    return rvec;
+}
+
+class SPH {
+public:
+    // The reference builds its parameters from a settings map
+    // (SPH::calculate, SPHSettings.cpp:30-144) and its grid with
+    // System::setupDomain; here both come in as the C structs.
+    SPH(const SPHParams& sphp, const GridParams& grid, int max_num, const GridParams* grid_scaled = nullptr,
+        float time_step = 0.001f)
+        : dt_(time_step) {
+        check(sph_create(&sphp, &grid, grid_scaled, max_num, &ctx_), nullptr);
+        max_num_ = max_num;
+    }
+    ~SPH() {
+        if (ctx_) sph_destroy(ctx_);
+    }
+    SPH(const SPH&) = delete;
+    SPH& operator=(const SPH&) = delete;
+    SPH(SPH&& o) noexcept : ctx_(o.ctx_), max_num_(o.max_num_), dt_(o.dt_) { o.ctx_ = nullptr; }
+
+    // --- System virtual API (System.h:64-75) ---
+    void update() { check(sph_update(ctx_)); }           // hash .. density, force, walls (SPH::updateGPU)
+    void interact() {}                                    // no coupled systems
+    void integrate() { check(sph_integrate(ctx_, dt_)); } // leapfrog (SPH::integrate)
+    void postProcess() {}
+    // update + integrate fused, nsteps times, replayed from a CUDA graph
+    void step(int nsteps = 1) { check(sph_step(ctx_, dt_, nsteps)); }
+
+    // Headless: there are no GL buffers to acquire or release.
+    void acquireGLBuffers() {}
+    void releaseGLBuffers() {}
+
+    // --- particles (System.h:80-90, 120-160; SPH.h:81-84) ---
+    int getNum() {
+        int n = 0;
+        check(sph_get_num(ctx_, &n));
+        return n;
+    }
+    void setNum(int nn) { check(sph_set_num(ctx_, nn)); }
+    int getMaxNum() const { return max_num_; }
+    float getSpacing() {
+        SPHParams p = params();
+        return p.rest_distance / p.simulation_scale;  // SPHSettings.cpp:94
+    }
+    // System::addBox (System.cpp:331-338): addRect at the SPH spacing, zero
+    // velocity.  color and mass are accepted for interface parity and unused.
+    int addBox(int nn, float4 min, float4 max, bool scaled, float4 color = make_float4(1, 0, 0, 1),
+               float mass = 0.0f) {
+        (void)scaled;
+        (void)color;
+        (void)mass;
+        std::vector<float4> rect = addRect(nn, min, max, getSpacing(), 1.0f);
+        pushParticles(rect, make_float4(0, 0, 0, 0));
+        return (int)rect.size();
+    }
+    void pushParticles(const std::vector<float4>& pos, float4 velo, float4 color = make_float4(1, 0, 0, 1),
+                       float mass = 0.0f) {
+        pushParticles(pos, std::vector<float4>(pos.size(), velo), color, mass);
+    }
+    // SPH::pushParticles (SPH.cpp:560-602): appends after the current
+    // particles; exceeding max_num throws (the reference prints and returns).
+    void pushParticles(const std::vector<float4>& pos, const std::vector<float4>& vel,
+                       float4 color = make_float4(1, 0, 0, 1), float mass = 0.0f) {
+        (void)color;
+        (void)mass;
+        if (pos.size() != vel.size()) throw SPHError(SPH_EINVAL, "pushParticles: pos and vel sizes differ");
+        check(sph_push_particles(ctx_, pos.data(), vel.data(), (int)pos.size()));
+    }
+    std::vector<float4> getDeletedPos() { return deleted(true); }
+    std::vector<float4> getDeletedVel() { return deleted(false); }
+
+    // Host copies of the state (original particle order).
+    std::vector<float4> getPositions() { return download(SPH_FIELD_POS_U); }
+    std::vector<float4> getVelocities() { return download(SPH_FIELD_VEL_U); }
+    std::vector<float4> getVelEval() { return download(SPH_FIELD_VELEVAL_U); }
+    // Device view of a field (what the reference's Buffer<T> objects held).
+    void* devicePointer(int field) {
+        void* p = nullptr;
+        check(sph_get_device_ptr(ctx_, field, &p));
+        return p;
+    }
+
+    // --- parameters ---
+    SPHParams params() {
+        SPHParams p;
+        check(sph_get_params(ctx_, &p, nullptr, nullptr));
+        return p;
+    }
+    void updateParams(const SPHParams& p) { check(sph_set_params(ctx_, &p)); }
+    void setTimeStep(float dt) { dt_ = dt; }
+    float getTimeStep() const { return dt_; }
+    void sync() { check(sph_sync(ctx_)); }
+    void printTimers() {}
+    sph_ctx* handle() { return ctx_; }
+
+private:
+    void check(int rc, sph_ctx* c) {
+        if (rc == SPH_OK) return;
+        char buf[512];
+        sph_last_error(c, buf, (int)sizeof(buf));
+        throw SPHError(rc, buf);
+    }
+    void check(int rc) { check(rc, ctx_); }
+    std::vector<float4> download(int field) {
+        std::vector<float4> out((size_t)getNum());
+        if (!out.empty()) check(sph_download(ctx_, field, out.data(), (int)out.size()));
+        return out;
+    }
+    std::vector<float4> deleted(bool pos) {
+        int count = 0;
+        check(sph_get_deleted(ctx_, nullptr, nullptr, 0, &count));
+        std::vector<float4> out((size_t)count);
+        if (count > 0)
+            check(sph_get_deleted(ctx_, pos ? out.data() : nullptr, pos ? nullptr : out.data(), count, &count));
+        return out;
+    }
+
+    sph_ctx* ctx_ = nullptr;
+    int max_num_ = 0;
+    float dt_ = 0.001f;
+};
+
+}  // namespace rtps
+
+#endif  // RTPS_SPH_HPP
