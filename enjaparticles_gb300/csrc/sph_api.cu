@@ -132,6 +132,12 @@ int sph_make_step_params(const SPHParams& s, const GridParams& gp, const GridPar
     const double span = (double)(P.res_x + 4) * (P.res_y + 4) * (P.res_z + 4);
     P.int_hash_ok = (integral && span < 16777216.0) ? 1 : 0;
     P.unit_scale = s.simulation_scale == 1.0f ? 1 : 0;
+    P.n_grav = 0;
+    P.grav_pos = nullptr;
+    P.grav_mass = nullptr;
+    P.grav_alpha = nullptr;
+    P.integrator = sphk::kIntegratorLeapfrog;
+    P.exact = 0;
     return SPH_OK;
 }
 
@@ -163,6 +169,12 @@ int build_step_params(sph_ctx* c) {
     std::string err;
     const int rc = sph_make_step_params(c->sp, c->gp, c->gps, c->P, err);
     if (rc != SPH_OK) return set_err(c, rc, "%s", err.c_str());
+    c->P.n_grav = c->n_grav;
+    c->P.grav_pos = c->grav;
+    c->P.grav_mass = reinterpret_cast<const float*>(c->grav + sphk::kMaxGravitySources);
+    c->P.grav_alpha = c->P.grav_mass + sphk::kMaxGravitySources;
+    c->P.integrator = c->integrator;
+    c->P.exact = c->exact;
     c->params_version++;
     return SPH_OK;
 }
@@ -210,7 +222,7 @@ void free_all(sph_ctx* c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
                     c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
-                    c->cell_start, c->cell_end, c->info, c->scratch};
+                    c->cell_start, c->cell_end, c->info, c->scratch, c->grav};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
@@ -379,6 +391,8 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->cell_start, C1 * 4);
     ALLOC(c->cell_end, C1 * 4);
     ALLOC(c->info, sizeof(int) * sphk::kInfoSlots);
+    // point sources: kMaxGravitySources float4 positions, then masses, then alphas
+    ALLOC(c->grav, sizeof(float4) * sphk::kMaxGravitySources + 2 * sizeof(float) * sphk::kMaxGravitySources);
     c->scratch_words = 4 * 256 + (size_t)c->passes * c->tiles_cap * 256;
     ALLOC(c->scratch, c->scratch_words * 4);
 #undef ALLOC
@@ -471,7 +485,41 @@ int sph_set_stream(sph_ctx* c, void* stream) {
 int sph_set_exact(sph_ctx* c, int exact) {
     if (!c) return SPH_EINVAL;
     c->exact = exact ? 1 : 0;
+    c->P.exact = c->exact;
     return SPH_OK;
+}
+
+int sph_set_gravity_sources(sph_ctx* c, int count, const sph_float4* points, const float* masses,
+                            const float* alphas) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (count < 0 || count > sphk::kMaxGravitySources)
+        return set_err(c, SPH_EINVAL, "sph_set_gravity_sources: count %d outside [0, %d]", count,
+                       sphk::kMaxGravitySources);
+    if (count > 0 && (!points || !masses || !alphas))
+        return set_err(c, SPH_EINVAL, "sph_set_gravity_sources: null array");
+    for (int k = 0; k < count; ++k)
+        if (!std::isfinite(points[k].x) || !std::isfinite(points[k].y) || !std::isfinite(points[k].z) ||
+            !std::isfinite(points[k].w) || !std::isfinite(masses[k]) || !std::isfinite(alphas[k]))
+            return set_err(c, SPH_EINVAL, "sph_set_gravity_sources: source %d is not finite", k);
+    if (count > 0) {
+        float* m = reinterpret_cast<float*>(c->grav + sphk::kMaxGravitySources);
+        CK(c, cudaMemcpyAsync(c->grav, points, sizeof(float4) * count, cudaMemcpyHostToDevice, c->stream));
+        CK(c, cudaMemcpyAsync(m, masses, sizeof(float) * count, cudaMemcpyHostToDevice, c->stream));
+        CK(c, cudaMemcpyAsync(m + sphk::kMaxGravitySources, alphas, sizeof(float) * count, cudaMemcpyHostToDevice,
+                              c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));  // host arrays may go away
+    }
+    c->n_grav = count;
+    return build_step_params(c);
+}
+
+int sph_set_integrator(sph_ctx* c, int integrator) {
+    if (!c) return SPH_EINVAL;
+    if (integrator != SPH_INTEGRATOR_LEAPFROG && integrator != SPH_INTEGRATOR_EULER)
+        return set_err(c, SPH_EINVAL, "sph_set_integrator: unknown integrator %d", integrator);
+    c->integrator = integrator;
+    return build_step_params(c);
 }
 
 int sph_upload(sph_ctx* c, const sph_float4* pos, const sph_float4* vel, const sph_float4* veleval, int n) {
@@ -635,6 +683,24 @@ int sph_stage_collision(sph_ctx* c) {
     return SPH_OK;
 }
 
+int sph_stage_gravity(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    sphk::launch_gravity(c->pos_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
+int sph_stage_euler(sph_ctx* c, float dt) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (!std::isfinite(dt)) return set_err(c, SPH_EINVAL, "dt must be finite");
+    sphk::launch_euler(c->pos_s, c->vel_s, c->force_s, c->idx_cur, c->pos_u, c->vel_u, c->info, c->P, dt,
+                       c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
 int sph_stage_leapfrog(sph_ctx* c, float dt) {
     int rc = check_ctx(c);
     if (rc) return rc;
@@ -656,12 +722,16 @@ int sph_update(sph_ctx* c) {
                                c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
     density_launch(c, c->idx_a, false, c->stream);
     force_launch(c, c->idx_a, false, 0.f, c->stream);
+    sphk::launch_gravity(c->pos_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
     sphk::launch_collision(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
     CK_LAUNCH(c);
     return SPH_OK;
 }
 
-int sph_integrate(sph_ctx* c, float dt) { return sph_stage_leapfrog(c, dt); }
+int sph_integrate(sph_ctx* c, float dt) {
+    if (!c) return SPH_EINVAL;
+    return c->integrator == SPH_INTEGRATOR_EULER ? sph_stage_euler(c, dt) : sph_stage_leapfrog(c, dt);
+}
 
 int sph_step(sph_ctx* c, float dt, int nsteps) {
     int rc = check_ctx(c);

@@ -44,6 +44,10 @@ struct sph_ctx {
     // force before the walls (keep_f) and the step's input velocity (keep_v):
     // the tape of the differentiable rollout.
     float4 *keep_f = nullptr, *keep_v = nullptr;
+    // point gravity sources (device: positions, masses, alphas) and the integrator
+    float4* grav = nullptr;
+    int n_grav = 0;
+    int integrator = 0;
     // graph of one fused step
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.f;

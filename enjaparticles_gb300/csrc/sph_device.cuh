@@ -55,7 +55,17 @@ struct StepParams {
     int res_x, res_y, res_z;      // integer grid_res of the scaled grid
     int int_hash_ok;              // integer neighbour hashing equals the float formula
     int unit_scale;               // simulation_scale == 1.0f
+    // point gravity sources (gravity.cl), none by default
+    int n_grav;
+    const float4* grav_pos;
+    const float* grav_mass;
+    const float* grav_alpha;
+    int integrator;               // kIntegratorLeapfrog or kIntegratorEuler
+    int exact;                    // exact arithmetic in the elementwise stages
 };
+constexpr int kIntegratorLeapfrog = 0;
+constexpr int kIntegratorEuler = 1;
+constexpr int kMaxGravitySources = 64;
 
 // Scenes of the neighbour passes.
 //   OneScene: one particle system; the step parameters are the kernel
@@ -159,6 +169,10 @@ void launch_collision(const float4* pos_s, const float4* vel_s, float4* force_s,
 void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
                      uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
                      const StepParams& p, float dt, int grid_items, cudaStream_t st);
+void launch_gravity(const float4* pos_s, float4* force_s, const int* info, const StepParams& p, int grid_items,
+                    cudaStream_t st);
+void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_s, uint32_t* idx, float4* pos_u,
+                  float4* vel_u, const int* info, const StepParams& p, float dt, int grid_items, cudaStream_t st);
 void launch_delete_staged(const float4* pos_s, const float4* vel_s, const float4* veleval_s, uint32_t* idx,
                           float4* pos_u, float4* vel_u, float4* veleval_u, float4* del_pos, float4* del_vel, int* info,
                           int grid_items, cudaStream_t st);

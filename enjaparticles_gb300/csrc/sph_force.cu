@@ -210,9 +210,17 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
         keep_v[i] = v;
     }
     const float4 pp = __ldg(pos_s + i);
+    // point sources after force (SPH.cpp:289-296), then the walls
+    if (P.n_grav > 0) f = gravity_add<Exact>(f, pp, P);
     const float4 psc = Unit ? pp : v4scale(pp, P.sc);
     f = collide_walls(psc, v, f, P);
     float4 po, vo, eo;
+    if (P.integrator == kIntegratorEuler) {
+        euler_core(psc, v, f, dt, P, po, vo);
+        vel_u[orig] = vo;
+        pos_u[orig] = po;
+        return;
+    }
     leapfrog_core(psc, v, f, xs, dt, P, po, vo, eo);
     vel_u[orig] = vo;
     veleval_u[orig] = eo;

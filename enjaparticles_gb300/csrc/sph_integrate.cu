@@ -1,6 +1,8 @@
 // sph_integrate.cu — the staged (unfused) elementwise stages.
 //   collision_wall: rtpslib/system/sph/cl_src/collision_wall.cl:31-118
 //   leapfrog:       rtpslib/system/sph/cl_src/leapfrog.cl:30-121
+//   gravity:        rtpslib/system/common/cl_src/gravity.cl:9-35
+//   euler:          rtpslib/system/sph/cl_src/euler.cl:33-78
 //   out-of-grid deletion bookkeeping of SPH::updateGPU (SPH.cpp:220-250)
 // The fused step runs the same device functions (sph_physics.cuh) inside the
 // force kernel.
@@ -51,6 +53,49 @@ void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* for
     int blocks = (grid_items + 255) / 256;
     if (blocks < 1) blocks = 1;
     k_leapfrog<<<blocks, 256, 0, st>>>(pos_s, vel_s, force_s, xsph_s, idx, pos_u, vel_u, veleval_u, info, p, dt);
+}
+
+template <bool Exact>
+__global__ void __launch_bounds__(256) k_gravity(const float4* __restrict__ pos_s, float4* __restrict__ force_s,
+                                                 const int* __restrict__ info, const StepParams P) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    force_s[i] = gravity_add<Exact>(force_s[i], __ldg(pos_s + i), P);
+}
+
+void launch_gravity(const float4* pos_s, float4* force_s, const int* info, const StepParams& p, int grid_items,
+                    cudaStream_t st) {
+    if (p.n_grav <= 0) return;
+    int blocks = (grid_items + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    if (p.exact)
+        k_gravity<true><<<blocks, 256, 0, st>>>(pos_s, force_s, info, p);
+    else
+        k_gravity<false><<<blocks, 256, 0, st>>>(pos_s, force_s, info, p);
+}
+
+__global__ void __launch_bounds__(256) k_euler(const float4* __restrict__ pos_s, const float4* __restrict__ vel_s,
+                                               const float4* __restrict__ force_s, const uint32_t* __restrict__ idx,
+                                               float4* __restrict__ pos_u, float4* __restrict__ vel_u,
+                                               const int* __restrict__ info, const StepParams P, float dt) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 po, vo;
+    euler_core(scaled(__ldg(pos_s + i), P), __ldg(vel_s + i), __ldg(force_s + i), dt, P, po, vo);
+    const uint32_t o = __ldg(idx + i);
+    vel_u[o] = vo;
+    pos_u[o] = po;
+}
+
+void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_s, uint32_t* idx, float4* pos_u,
+                  float4* vel_u, const int* info, const StepParams& p, float dt, int grid_items, cudaStream_t st) {
+    int blocks = (grid_items + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    k_euler<<<blocks, 256, 0, st>>>(pos_s, vel_s, force_s, idx, pos_u, vel_u, info, p, dt);
 }
 
 // Staged deletion: after cellindices + permute, when some particles left the

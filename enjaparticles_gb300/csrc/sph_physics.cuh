@@ -76,6 +76,53 @@ __device__ __forceinline__ void leapfrog_core(float4 p, float4 v, float4 f, floa
     vel_out = vnext;
 }
 
+// Point-source gravity (system/common/cl_src/gravity.cl:9-35), added to the
+// force f of the particle at unscaled sorted position pos, as
+// SPH::updateGPU does after force (SPH.cpp:289-296): per source,
+// vect = sc * (point - pos) (w = 0), direction = vect / |vect|,
+// f += (alpha * mass / d) * direction with d = |vect|^2, or
+// d = -(0.5 sc)^2 inside that radius (the pull turns into a push).  The
+// normalisation is OpenCL's fast_normalize, whose precision the
+// implementation chooses: exact arithmetic takes vect * (1 / sqrt(|vect|^2))
+// with both operations correctly rounded, fast arithmetic an rsqrt.
+template <bool Exact>
+__device__ __forceinline__ float4 gravity_add(float4 f, float4 pos, const StepParams& P) {
+    const float cut0 = __fmul_rn(0.5f, P.sc);
+    const float cut = __fmul_rn(cut0, cut0);
+    for (int s = 0; s < P.n_grav; ++s) {
+        float4 vect = v4scale(v4sub(__ldg(P.grav_pos + s), pos), P.sc);
+        vect.w = 0.f;
+        const float d2 = v4dot(vect, vect);
+        const float inv = Exact ? __fdiv_rn(1.f, __fsqrt_rn(d2)) : rsqrtf(d2);
+        const float4 dir = v4scale(vect, inv);
+        float mag = __fmul_rn(__ldg(P.grav_alpha + s), __ldg(P.grav_mass + s));
+        mag = d2 < cut ? __fdiv_rn(mag, -cut) : __fdiv_rn(mag, d2);
+        f = v4add(f, v4scale(dir, mag));
+    }
+    return f;
+}
+
+// The SPH Euler integrator (sph/cl_src/euler.cl:33-78) for one particle: p is
+// pos_s*simulation_scale.  Its gravity is the constant -9.8 in z and its
+// acceleration limit the constant 600 (SPHParams.gravity / velocity_limit are
+// not used); it gives position and velocity (veleval is left as it was).
+__device__ __forceinline__ void euler_core(float4 p, float4 v, float4 f, float dt, const StepParams& P,
+                                           float4& pos_out, float4& vel_out) {
+    f.z = __fadd_rn(f.z, -9.8f);
+    const float speed =
+        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(f.x, f.x), __fmul_rn(f.y, f.y)), __fmul_rn(f.z, f.z)));
+    if (speed > 600.0f) f = v4scale(f, __fdiv_rn(600.0f, speed));
+    v = v4add(v, v4scale(f, dt));
+    p = v4add(p, v4scale(v, dt));
+    if (!P.unit_scale) {
+        p.x = __fdiv_rn(p.x, P.sc);
+        p.y = __fdiv_rn(p.y, P.sc);
+        p.z = __fdiv_rn(p.z, P.sc);
+    }
+    pos_out = make_float4(p.x, p.y, p.z, 1.0f);
+    vel_out = v;
+}
+
 __device__ __forceinline__ float4 scaled(float4 p, const StepParams& P) {
     return P.unit_scale ? p : v4scale(p, P.sc);
 }

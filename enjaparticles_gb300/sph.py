@@ -137,6 +137,25 @@ class SPH:
     def leapfrog(self, dt):
         self._ck(self.lib.sph_stage_leapfrog(self.ctx, float(dt)))
 
+    def gravity(self):
+        """Gravity::execute: force_s += the point sources' pull."""
+        self._ck(self.lib.sph_stage_gravity(self.ctx))
+
+    def euler(self, dt):
+        self._ck(self.lib.sph_stage_euler(self.ctx, float(dt)))
+
+    # -- point sources and integrator (System.cpp:260-272, SPH.cpp:392-436) --
+    def setGravitySources(self, points, masses, alphas):
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+        m = np.ascontiguousarray(masses, np.float32)
+        a = np.ascontiguousarray(alphas, np.float32)
+        self._ck(self.lib.sph_set_gravity_sources(self.ctx, len(m), pts.ctypes.data, m.ctypes.data, a.ctypes.data))
+
+    def setIntegrator(self, name):
+        """'leapfrog' or 'euler'."""
+        kind = {"leapfrog": abi.SPH_INTEGRATOR_LEAPFROG, "euler": abi.SPH_INTEGRATOR_EULER}[name]
+        self._ck(self.lib.sph_set_integrator(self.ctx, kind))
+
     # -- whole steps --------------------------------------------------------
     def update(self):
         """SPH::update: hash ... collision."""

@@ -245,16 +245,43 @@ int sph_stage_collision(sph_ctx* ctx);
 /* LeapFrog::execute (sph/LeapFrog.cpp:42-83; leapfrog.cl:30-121): integrate and
  * scatter to pos_u, vel_u, veleval_u. */
 int sph_stage_leapfrog(sph_ctx* ctx, float dt);
+/* Gravity::execute (common/Gravity.cpp:43-75; gravity.cl:9-35) as
+ * SPH::updateGPU calls it after force (SPH.cpp:289-296): force_s += the pull
+ * of the point sources set by sph_set_gravity_sources on the sorted
+ * positions.  No-op without sources. */
+int sph_stage_gravity(sph_ctx* ctx);
+/* Euler::execute (sph/cl_src/euler.cl:33-78): the SPH Euler integrator.  Its
+ * gravity is the constant -9.8 in z and its acceleration limit the constant
+ * 600, as in the reference; it writes pos_u and vel_u and leaves veleval_u. */
+int sph_stage_euler(sph_ctx* ctx, float dt);
+
+/* Point gravity sources: the settings gravity_sources / gravity_mass /
+ * gravity_alphas of System::prepareSorted (System.cpp:260-272).  count
+ * sources (0 removes them, at most SPH_MAX_GRAVITY_SOURCES) with positions
+ * points[k] (unscaled), masses[k] and strengths alphas[k]; each pulls a
+ * particle at squared scaled distance d with alpha*mass/d, and pushes it with
+ * alpha*mass/(0.5*simulation_scale)^2 inside that radius.  Blocking. */
+#define SPH_MAX_GRAVITY_SOURCES 64
+int sph_set_gravity_sources(sph_ctx* ctx, int count, const sph_float4* points, const float* masses,
+                            const float* alphas);
+
+/* The integrator of SPH::integrate (SPH.cpp:392-436), the setting
+ * "integrator": leapfrog (the default) or euler.  Used by sph_integrate and
+ * the fused step. */
+#define SPH_INTEGRATOR_LEAPFROG 0
+#define SPH_INTEGRATOR_EULER 1
+int sph_set_integrator(sph_ctx* ctx, int integrator);
 
 /* SPH::update (SPH.cpp:117-125 -> updateGPU :149-300) with the wall collision
  * of SPH::collision (SPH.cpp:303-336) enabled after gravity: hash, sort,
- * cellindices, permute, out-of-grid deletion, density, force, collision. */
+ * cellindices, permute, out-of-grid deletion, density, force, point-source
+ * gravity, collision. */
 int sph_update(sph_ctx* ctx);
-/* SPH::integrate (SPH.cpp:389-441), leapfrog integrator. */
+/* SPH::integrate (SPH.cpp:389-441): the integrator sph_set_integrator chose. */
 int sph_integrate(sph_ctx* ctx, float dt);
 
 /* nsteps x (update + integrate) on the fused path: hash -> sort ->
- * cellindices+permute -> density -> force+collision+leapfrog, replayed from a
+ * cellindices+permute -> density -> force+gravity+collision+integrator, replayed from a
  * captured CUDA graph.  Results equal nsteps staged update()+integrate()
  * calls.  Asynchronous. */
 int sph_step(sph_ctx* ctx, float dt, int nsteps);

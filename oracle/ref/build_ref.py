@@ -10,9 +10,10 @@ plain arithmetic, though, so this recipe compiles them for the host with g++:
      (rtpslib/system/common/cl_src, rtpslib/system/sph/cl_src) into a
      temporary directory laid out as the reference's build lays them out
      (cl_common/, cl_sph/; rtpslib/system/sph/CMakeLists.txt:3-11);
-  2. rewrite two pieces of OpenCL-only syntax there, nothing else:
+  2. rewrite three pieces of OpenCL-only syntax there, nothing else:
        `(float4)(a, b, c, d)` / `(int4)(...)`  ->  `make_float4(...)` / `make_int4(...)`
        kernel-scope `__local T name[N];` arrays  ->  `static T name[N];`
+       the identity swizzle `v.xyzw`  ->  `v`
      (work-groups run one at a time, so a static array is the group's local
      memory);
   3. compile them with clshim.hpp (vector types, built-ins, barrier) and the
@@ -37,19 +38,23 @@ ORACLE = os.path.dirname(HERE)
 OUT_DIR = os.path.join(ORACLE, "_ref")
 OUT_LIB = os.path.join(OUT_DIR, "librtps_ref.so")
 
-COMMON = ["hash.cl", "cl_hash.h", "cl_structs.h", "cl_macros.h", "cellindices.cl", "permute.cl", "bitonic.cl"]
-SPH = ["density.cl", "force.cl", "collision_wall.cl", "leapfrog.cl", "cl_sph_kernels.h", "cl_sph_neighbors.h",
+COMMON = ["hash.cl", "cl_hash.h", "cl_structs.h", "cl_macros.h", "cellindices.cl", "permute.cl", "bitonic.cl",
+          "gravity.cl"]
+SPH = ["density.cl", "force.cl", "collision_wall.cl", "leapfrog.cl", "euler.cl", "cl_sph_kernels.h", "cl_sph_neighbors.h",
        "cl_sph_structs.h", "cl_sph_collision.h", "cl_sph_macros.h"]
 DRIVERS = ["ref_runtime.cpp", "ref_hash.cpp", "ref_bitonic.cpp", "ref_cellindices.cpp", "ref_permute.cpp",
-           "ref_density.cpp", "ref_force.cpp", "ref_collision.cpp", "ref_leapfrog.cpp", "ref_domain.cpp"]
+           "ref_density.cpp", "ref_force.cpp", "ref_collision.cpp", "ref_leapfrog.cpp", "ref_domain.cpp",
+           "ref_gravity.cpp", "ref_euler.cpp"]
 
 VEC_LITERAL = re.compile(r"\((float4|int4)\)\s*\(")
 LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
+IDENTITY_SWIZZLE = re.compile(r"\.xyzw\b")
 
 
 def rewrite(text):
     text = VEC_LITERAL.sub(lambda m: "make_%s(" % m.group(1), text)
     text = LOCAL_ARRAY.sub(r"\1static\2", text)
+    text = IDENTITY_SWIZZLE.sub("", text)
     return text
 
 

@@ -14,6 +14,7 @@
 //
 // Semantics chosen where OpenCL leaves room (they match sph_oracle.hpp):
 //   length(v) = sqrtf(((x*x + y*y) + z*z) + w*w), dot likewise;
+//   fast_normalize(v) = v * (1 / sqrtf(dot(v, v)));
 //   float4 / scalar is a true per-component division;
 //   a double scalar times a float4 is rounded to float first (OpenCL converts
 //   the scalar operand to the vector's element type);
@@ -158,6 +159,9 @@ inline float4 operator/(const float4& a, double s) { return a / (float)s; }
 
 inline float dot(const float4& a, const float4& b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
 inline float length(const float4& a) { return std::sqrt(dot(a, a)); }
+// fast_normalize: OpenCL leaves its precision to the implementation; here
+// v * (1 / sqrt(dot(v, v))), each operation correctly rounded.
+inline float4 fast_normalize(const float4& v) { return v * (1.0f / std::sqrt(dot(v, v))); }
 inline float max(float a, float b) { return a < b ? b : a; }
 inline float min(float a, float b) { return b < a ? b : a; }
 

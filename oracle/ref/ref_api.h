@@ -16,6 +16,10 @@ void ref_collision_wall(int n, const float* pos_s, const float* vel_s, float* fo
                         const void* sphp);
 void ref_leapfrog(int n, float* pos_u, const float* pos_s, float* vel_u, const float* vel_s, float* veleval_u,
                   const float* force, const float* xsph, const uint32_t* idx, const void* sphp, float dt);
+void ref_gravity(int n, int nsrc, const float* points, const float* masses, const float* alphas, const float* pos_s,
+                 float* force, float scale);
+void ref_euler(int n, float* pos_u, const float* pos_s, float* vel_u, const float* vel_s, const float* force,
+               const uint32_t* idx, const void* sphp, float dt);
 void ref_setup_domain(const float* bnd_min, const float* bnd_max, float cell_size, float sim_scale, void* grid,
                       void* grid_scaled);
 }

@@ -121,6 +121,9 @@ struct OracleSim {
     std::vector<uint32_t> keys, idx, start, end, nbr;
     std::vector<float> deleted_pos, deleted_vel;
     int last_nc = -1;
+    // point sources (System.cpp:260-272) and the integrator (SPH.cpp:392-436)
+    std::vector<float> grav_points, grav_masses, grav_alphas;
+    int integrator = 0;  // 0 leapfrog, 1 euler
 };
 
 template <class T>
@@ -148,6 +151,23 @@ static void run_leapfrog(OracleSim& s, float dt) {
     for (int i = 0; i < s.num; ++i)
         leapfrog_one<T>(i, s.pos_s.data(), s.vel_s.data(), s.force_s.data(), s.xsph_s.data(), s.idx.data(), s.sp, dt,
                         s.pos_u.data(), s.vel_u.data(), s.veleval_u.data());
+}
+
+template <class T>
+static void run_gravity(OracleSim& s) {
+    const int nsrc = (int)s.grav_masses.size();
+    if (nsrc == 0) return;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < s.num; ++i)
+        gravity_one<T>(i, nsrc, s.grav_points.data(), s.grav_masses.data(), s.grav_alphas.data(), s.pos_s.data(),
+                       s.force_s.data(), s.sp.simulation_scale);
+}
+template <class T>
+static void run_euler(OracleSim& s, float dt) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < s.num; ++i)
+        euler_one<T>(i, s.pos_s.data(), s.vel_s.data(), s.force_s.data(), s.idx.data(), s.sp, dt, s.pos_u.data(),
+                     s.vel_u.data());
 }
 
 static void run_hash_and_sort(OracleSim& s) {
@@ -190,19 +210,28 @@ static void sim_update(OracleSim& s) {
     if (s.use_f64) {
         run_density<double>(s);
         run_force<double>(s);
+        run_gravity<double>(s);
         run_collision<double>(s);
     } else {
         run_density<float>(s);
         run_force<float>(s);
+        run_gravity<float>(s);
         run_collision<float>(s);
     }
 }
 
+// SPH::integrate (SPH.cpp:389-441): euler or leapfrog.
 static void sim_integrate(OracleSim& s, float dt) {
-    if (s.use_f64)
+    if (s.integrator == 1) {
+        if (s.use_f64)
+            run_euler<double>(s, dt);
+        else
+            run_euler<float>(s, dt);
+    } else if (s.use_f64) {
         run_leapfrog<double>(s, dt);
-    else
+    } else {
         run_leapfrog<float>(s, dt);
+    }
 }
 
 extern "C" {
@@ -299,6 +328,27 @@ void oracle_leapfrog(int f64, int n, const float* pos_s, const float* vel_s, con
     }
 }
 
+void oracle_gravity(int f64, int n, int nsrc, const float* points, const float* masses, const float* alphas,
+                    const float* pos_s, float* force, float scale) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        if (f64)
+            gravity_one<double>(i, nsrc, points, masses, alphas, pos_s, force, scale);
+        else
+            gravity_one<float>(i, nsrc, points, masses, alphas, pos_s, force, scale);
+    }
+}
+void oracle_euler(int f64, int n, const float* pos_s, const float* vel_s, const float* force, const uint32_t* idx,
+                  const SPHParams* sp, float dt, float* pos_u, float* vel_u) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        if (f64)
+            euler_one<double>(i, pos_s, vel_s, force, idx, *sp, dt, pos_u, vel_u);
+        else
+            euler_one<float>(i, pos_s, vel_s, force, idx, *sp, dt, pos_u, vel_u);
+    }
+}
+
 // --- whole system ----------------------------------------------------------
 void* oracle_sim_create(const SPHParams* sp, const GridParams* gp, const GridParams* gps, int max_num, int f64) {
     OracleSim* s = new OracleSim();
@@ -342,6 +392,13 @@ void oracle_sim_step(void* h, float dt, int nsteps) {
         sim_integrate(*s, dt);
     }
 }
+void oracle_sim_set_gravity(void* h, int nsrc, const float* points, const float* masses, const float* alphas) {
+    OracleSim* s = (OracleSim*)h;
+    s->grav_points.assign(points, points + 4 * (size_t)(nsrc > 0 ? nsrc : 0));
+    s->grav_masses.assign(masses, masses + (nsrc > 0 ? nsrc : 0));
+    s->grav_alphas.assign(alphas, alphas + (nsrc > 0 ? nsrc : 0));
+}
+void oracle_sim_set_integrator(void* h, int integrator) { ((OracleSim*)h)->integrator = integrator; }
 int oracle_sim_num(void* h) { return ((OracleSim*)h)->num; }
 int oracle_sim_last_nc(void* h) { return ((OracleSim*)h)->last_nc; }
 // field ids follow enum sph_field of include/rtps_sph.h

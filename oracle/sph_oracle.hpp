@@ -288,4 +288,56 @@ inline void leapfrog_one(int i, const float* pos_s, const float* vel_s, const fl
     store4(pos_u + 4 * (size_t)o, V4<T>{p.x, p.y, p.z, (T)1});
 }
 
+// Point-source gravity, gravity (system/common/cl_src/gravity.cl:9-35) as
+// SPH::updateGPU calls it after force (SPH.cpp:289-296): for each source s,
+// vect = scale * (point_s - pos_s[i]) with w = 0, accel += mag * direction,
+// direction = fast_normalize(vect) = vect * (1 / sqrt(dot(vect, vect))) (the
+// precision of fast_normalize is the implementation's; this is the choice of
+// the host build of the reference kernels too), mag = alpha_s * mass_s divided
+// by dist2, or by -(0.5 scale)^2 inside that radius.
+template <class T>
+inline void gravity_one(int i, int nsrc, const float* points, const float* masses, const float* alphas,
+                        const float* pos_s, float* accel, float scale_f) {
+    const T scale = (T)scale_f;
+    const V4<T> p = load4<T>(pos_s + 4 * (size_t)i);
+    V4<T> a = load4<T>(accel + 4 * (size_t)i);
+    for (int s = 0; s < nsrc; ++s) {
+        V4<T> vect = smul(scale, sub(load4<T>(points + 4 * (size_t)s), p));
+        vect.w = 0;
+        const V4<T> direction = mul(vect, (T)1 / std::sqrt(dot4(vect, vect)));
+        const T dist2 = dot4(vect, vect);
+        T mag = (T)alphas[s] * (T)masses[s];
+        T cutoff = (T)0.5f * scale;
+        cutoff *= cutoff;
+        if (dist2 < cutoff)
+            mag /= -cutoff;
+        else
+            mag /= dist2;
+        a = add(a, smul(mag, direction));
+    }
+    store4(accel + 4 * (size_t)i, a);
+}
+
+// SPH Euler integrator, euler (sph/cl_src/euler.cl:33-78), the integrator of
+// SPH::integrate when the settings say "euler" (SPH.cpp:392-411).  Its
+// gravity is the constant -9.8 in z and its acceleration limit the constant
+// 600 (not SPHParams.gravity / velocity_limit); it writes pos_u and vel_u and
+// leaves veleval_u alone; no XSPH.
+template <class T>
+inline void euler_one(int i, const float* pos_s, const float* vel_s, const float* force, const uint32_t* idx,
+                      const SPHParams& sp, float dt_f, float* pos_u, float* vel_u) {
+    const T sc = (T)sp.simulation_scale, dt = (T)dt_f;
+    V4<T> p = mul(load4<T>(pos_s + 4 * (size_t)i), sc);
+    V4<T> v = load4<T>(vel_s + 4 * (size_t)i);
+    V4<T> f = load4<T>(force + 4 * (size_t)i);
+    f.z += (T)-9.8f;
+    const T speed = std::sqrt(f.x * f.x + f.y * f.y + f.z * f.z);
+    if (speed > (T)600.0f) f = mul(f, (T)600.0f / speed);
+    v = add(v, smul(dt, f));
+    p = add(p, smul(dt, v));
+    const uint32_t o = idx[i];
+    store4(vel_u + 4 * (size_t)o, v);
+    store4(pos_u + 4 * (size_t)o, V4<T>{p.x / sc, p.y / sc, p.z / sc, (T)1});
+}
+
 }  // namespace sph_oracle

@@ -16,7 +16,10 @@ Fixtures
   outofgrid_n512.npz N=512 with 37 particles placed outside the grid: the
                      out-of-grid deletion path of SPH.cpp:220-250, 2 steps
   cfg0_n16384.npz    the 16,384-particle dam break: pos/vel after 1, 10, 100 steps
-Usage: python tests/golden/make_golden.py
+  gravity_n2048.npz  N=2048, v0 ~ N(0, 0.1^2), two point gravity sources
+                     (gravity.cl), with the leapfrog and with the Euler
+                     integrator (euler.cl): step 1 forces, state after 1 and 5
+Usage: python tests/golden/make_golden.py [--only NAME ...]
 """
 import ctypes as C
 import os
@@ -110,11 +113,49 @@ def cfg0_fixture():
     return out
 
 
+# Two point sources: one above the fluid pulling it up, one inside it, whose
+# pull turns into a push within 0.5 * simulation_scale (gravity.cl:26-31).
+GRAV_POINTS = np.array([[0.25, 0.25, 0.9, 1.0], [0.2, 0.3, 0.15, 1.0]], np.float32)
+GRAV_MASSES = np.array([4.0, 0.5], np.float32)
+GRAV_ALPHAS = np.array([2.0, 1.5], np.float32)
+
+
+def gravity_fixture():
+    n = 2048
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n, velocity_sigma=0.1)
+    out = dict(params_blob(sp, g, gs))
+    out.update({"in_pos": pos, "in_vel": vel, "dt": np.float32(DT), "grav_points": GRAV_POINTS,
+                "grav_masses": GRAV_MASSES, "grav_alphas": GRAV_ALPHAS})
+    for integ in ("leapfrog", "euler"):
+        R = ref_driver.RefSystem(sp, g, gs, n)
+        R.set_gravity(GRAV_POINTS, GRAV_MASSES, GRAV_ALPHAS)
+        R.integrator = integ
+        R.upload(pos, vel)
+        R.update()
+        out["%s_s1_force_sph" % integ] = R.trace["force_sph"]
+        out["%s_s1_force_pre" % integ] = R.trace["force_pre_collision"]
+        out["%s_s1_force_s" % integ] = R.force_s[:n].copy()
+        R.integrate(DT)
+        out.update(state(R, "%s_s1_" % integ))
+        R.step(DT, 4)
+        out.update(state(R, "%s_s5_" % integ))
+    return out
+
+
+FIXTURES = {
+    "stages_n4096.npz": lambda: stages_fixture(4096, 0.1),
+    "ragged_n1000.npz": lambda: stages_fixture(1000, 0.1, steps_after=(3,)),
+    "outofgrid_n512.npz": outofgrid_fixture,
+    "cfg0_n16384.npz": cfg0_fixture,
+    "gravity_n2048.npz": gravity_fixture,
+}
+
+
 def main():
-    np.savez_compressed(os.path.join(HERE, "stages_n4096.npz"), **stages_fixture(4096, 0.1))
-    np.savez_compressed(os.path.join(HERE, "ragged_n1000.npz"), **stages_fixture(1000, 0.1, steps_after=(3,)))
-    np.savez_compressed(os.path.join(HERE, "outofgrid_n512.npz"), **outofgrid_fixture())
-    np.savez_compressed(os.path.join(HERE, "cfg0_n16384.npz"), **cfg0_fixture())
+    names = sys.argv[sys.argv.index("--only") + 1:] if "--only" in sys.argv else list(FIXTURES)
+    for name in names:
+        np.savez_compressed(os.path.join(HERE, name), **FIXTURES[name]())
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

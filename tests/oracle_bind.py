@@ -59,6 +59,10 @@ def oracle():
             "oracle_sim_last_nc": (_I, [_P]),
             "oracle_sim_get": (_I, [_P, _I, _P, _I]),
             "oracle_sim_deleted": (_I, [_P, _P, _P, _I]),
+            "oracle_gravity": (None, [_I, _I, _I, _P, _P, _P, _P, _P, _F]),
+            "oracle_euler": (None, [_I, _I, _P, _P, _P, _P, _P, _F, _P, _P]),
+            "oracle_sim_set_gravity": (None, [_P, _I, _P, _P, _P]),
+            "oracle_sim_set_integrator": (None, [_P, _I]),
             "oracle_rollout64": (_I, [_P, _P, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_rollout64_jvp": (_I, [_P, _P, C.c_double, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P,
                                           _P, _P, _P]),
@@ -90,6 +94,8 @@ def ref():
             "ref_collision_wall": (None, [_I, _P, _P, _P, _P, _P]),
             "ref_leapfrog": (None, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _F]),
             "ref_setup_domain": (None, [_P, _P, _F, _F, _P, _P]),
+            "ref_gravity": (None, [_I, _I, _P, _P, _P, _P, _P, _F]),
+            "ref_euler": (None, [_I, _P, _P, _P, _P, _P, _P, _P, _F]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -127,6 +133,17 @@ class OracleSim:
 
     def set_params(self, sphp):
         self.lib.oracle_sim_set_params(self.h, C.addressof(sphp))
+
+    def set_gravity(self, points, masses, alphas):
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+        m = np.ascontiguousarray(masses, np.float32)
+        a = np.ascontiguousarray(alphas, np.float32)
+        self._grav = (pts, m, a)
+        self.lib.oracle_sim_set_gravity(self.h, len(m), ptr(pts), ptr(m), ptr(a))
+
+    def set_integrator(self, kind):
+        """0: leapfrog, 1: euler."""
+        self.lib.oracle_sim_set_integrator(self.h, int(kind))
 
     def upload(self, pos, vel, veleval=None):
         pos = np.ascontiguousarray(pos, np.float32)

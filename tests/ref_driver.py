@@ -52,6 +52,13 @@ class RefSystem:
         self.deleted_pos = np.zeros((0, 4), np.float32)
         self.deleted_vel = np.zeros((0, 4), np.float32)
         self.trace = {}
+        # point sources (System.cpp:260-272) and integrator (SPH.cpp:392-436)
+        self.grav = None
+        self.integrator = "leapfrog"
+
+    def set_gravity(self, points, masses, alphas):
+        self.grav = (np.ascontiguousarray(points, np.float32).reshape(-1, 4),
+                     np.ascontiguousarray(masses, np.float32), np.ascontiguousarray(alphas, np.float32))
 
     def upload(self, pos, vel):
         n = pos.shape[0]
@@ -98,12 +105,22 @@ class RefSystem:
         L.ref_density(n, P(self.pos_s), P(self.density_s), P(self.start), P(self.end), C.addressof(self.gs), sp)
         L.ref_force(n, P(self.pos_s), P(self.density_s), P(self.veleval_s), P(self.force_s), P(self.xsph_s),
                     P(self.start), P(self.end), C.addressof(self.gs), sp)
+        self.trace["force_sph"] = self.force_s[:n].copy()
+        if self.grav is not None:
+            # gravity.execute after force (SPH.cpp:289-296)
+            pts, m, a = self.grav
+            L.ref_gravity(n, len(m), P(pts), P(m), P(a), P(self.pos_s), P(self.force_s),
+                          float(self.sp.simulation_scale))
         self.trace["force_pre_collision"] = self.force_s[:n].copy()
         if collision:
             L.ref_collision_wall(n, P(self.pos_s), P(self.vel_s), P(self.force_s), C.addressof(self.gs), sp)
 
     def integrate(self, dt):
         n = self.num
+        if self.integrator == "euler":
+            self.lib.ref_euler(n, P(self.pos_u), P(self.pos_s), P(self.vel_u), P(self.vel_s), P(self.force_s),
+                               P(self.idx), self._params(), float(dt))
+            return
         self.lib.ref_leapfrog(n, P(self.pos_u), P(self.pos_s), P(self.vel_u), P(self.vel_s), P(self.veleval_u),
                               P(self.force_s), P(self.xsph_s), P(self.idx), self._params(), float(dt))
 

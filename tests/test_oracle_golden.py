@@ -104,3 +104,52 @@ def test_oracle_cfg0_rollout_matches_reference_golden():
         done = k
         np.testing.assert_array_equal(sim.get("pos_u"), d["s%d_pos_u" % k])
         np.testing.assert_array_equal(sim.get("vel_u"), d["s%d_vel_u" % k])
+
+
+@pytest.mark.parametrize("integrator", ["leapfrog", "euler"])
+def test_oracle_gravity_sources_and_integrators_match_reference_golden(integrator):
+    """Point-source gravity (gravity.cl) after force, and both integrators of
+    SPH::integrate (leapfrog.cl, euler.cl): step-1 forces and the state after
+    1 and 5 steps equal the reference kernels' bit for bit."""
+    d, sp, g, gs = golden_io.load("gravity_n2048.npz")
+    n = d["in_pos"].shape[0]
+    sim = ob.OracleSim(sp, g, gs, n)
+    sim.set_gravity(d["grav_points"], d["grav_masses"], d["grav_alphas"])
+    sim.set_integrator(1 if integrator == "euler" else 0)
+    sim.upload(d["in_pos"], d["in_vel"])
+    sim.update()
+    np.testing.assert_array_equal(sim.get("force_s"), d["%s_s1_force_s" % integrator])
+    sim.integrate(float(d["dt"]))
+    for k, done in ((1, 1), (5, 5)):
+        if k > 1:
+            sim.step(float(d["dt"]), 4)
+        for f in ("pos_u", "vel_u", "veleval_u"):
+            np.testing.assert_array_equal(sim.get(f), d["%s_s%d_%s" % (integrator, k, f)], err_msg=f)
+
+
+@pytest.mark.skipif(not ob.ref_available(), reason="reference kernels not built here (needs the reference tree)")
+def test_oracle_gravity_and_euler_equal_reference_kernels_on_random_data():
+    from enjaparticles_gb300.scenes import uniform
+    R = ob.ref()
+    O = ob.oracle()
+    n, nsrc = 3000, 5
+    pos = (uniform(501, 4 * n).reshape(n, 4) * 1.2 - 0.1).astype(np.float32)
+    pos[:, 3] = 1.0
+    pts = (uniform(502, 4 * nsrc).reshape(nsrc, 4)).astype(np.float32)
+    m = (uniform(503, nsrc) * 3).astype(np.float32)
+    a = (uniform(504, nsrc) * 2 - 0.5).astype(np.float32)
+    f0 = ((uniform(505, 4 * n).reshape(n, 4) - 0.5) * 40).astype(np.float32)
+    fr, fo = f0.copy(), f0.copy()
+    R.ref_gravity(n, nsrc, P(pts), P(m), P(a), P(pos), P(fr), 1.0)
+    O.oracle_gravity(0, n, nsrc, P(pts), P(m), P(a), P(pos), P(fo), 1.0)
+    np.testing.assert_array_equal(fo, fr)
+    sp, _, _ = __import__("enjaparticles_gb300.abi", fromlist=["abi"]).dambreak_params(n)
+    vel = ((uniform(506, 4 * n).reshape(n, 4) - 0.5)).astype(np.float32)
+    big = f0 * 30  # some accelerations above the Euler limit of 600
+    idx = np.random.default_rng(7).permutation(n).astype(np.uint32)
+    pr, vr = np.zeros_like(pos), np.zeros_like(pos)
+    po, vo = np.zeros_like(pos), np.zeros_like(pos)
+    R.ref_euler(n, P(pr), P(pos), P(vr), P(vel), P(big), P(idx), C.addressof(sp), 0.001)
+    O.oracle_euler(0, n, P(pos), P(vel), P(big), P(idx), C.addressof(sp), 0.001, P(po), P(vo))
+    np.testing.assert_array_equal(po, pr)
+    np.testing.assert_array_equal(vo, vr)
