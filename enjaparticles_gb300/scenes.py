@@ -97,3 +97,57 @@ def sample_coordinates(n, count, seed=13, offset=0):
         seen.add(c)
         out.append((c // 3, c % 3))
     return out, k
+
+
+# --- triangle meshes (rtps Triangle: three vertices and a normal, 16 floats,
+#     rtpslib/structs.h:586-590) ------------------------------------------------
+
+def _triangles(verts):
+    """(m, 3, 3) vertices -> (m, 4, 4) float32 triangles: vertices with w = 1,
+    then the unit normal (b - a) x (c - a) with w = 0."""
+    v = np.asarray(verts, np.float64)
+    n = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    t = np.zeros((v.shape[0], 4, 4), np.float32)
+    t[:, :3, :3] = v
+    t[:, :3, 3] = 1.0
+    t[:, 3, :3] = n
+    return t
+
+
+def ramp_mesh(nx=16, ny=16, z0=0.12, z1=0.22, lo=(0.0, 0.0), hi=(1.0, 1.0)):
+    """A plane z = z0 + (z1 - z0) x over [lo, hi] in x, y, as nx*ny quads of
+    two triangles each, normals pointing up."""
+    xs = np.linspace(lo[0], hi[0], nx + 1)
+    ys = np.linspace(lo[1], hi[1], ny + 1)
+    z = lambda x: z0 + (z1 - z0) * x
+    tris = []
+    for j in range(ny):
+        for i in range(nx):
+            a = (xs[i], ys[j], z(xs[i]))
+            b = (xs[i + 1], ys[j], z(xs[i + 1]))
+            c = (xs[i + 1], ys[j + 1], z(xs[i + 1]))
+            d = (xs[i], ys[j + 1], z(xs[i]))
+            tris.append((a, b, c))
+            tris.append((a, c, d))
+    return _triangles(tris)
+
+
+def box_mesh(lo, hi):
+    """The surface of an axis-aligned box, 12 triangles, normals outwards."""
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    c = [(x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0),
+         (x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1)]
+    quads = [(0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (2, 3, 7, 6), (1, 2, 6, 5), (3, 0, 4, 7)]
+    tris = []
+    for a, b, cc, d in quads:
+        tris.append((c[a], c[b], c[cc]))
+        tris.append((c[a], c[cc], c[d]))
+    return _triangles(tris)
+
+
+def ramp_and_box_mesh():
+    """The triangle-collision scene's mesh: a 16 x 16-quad ramp through the
+    dam-break block (512 triangles) and a box obstacle beside it (12)."""
+    return np.concatenate([ramp_mesh(), box_mesh((0.6, 0.3, 0.0), (0.75, 0.6, 0.3))])

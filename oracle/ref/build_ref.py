@@ -10,10 +10,14 @@ plain arithmetic, though, so this recipe compiles them for the host with g++:
      (rtpslib/system/common/cl_src, rtpslib/system/sph/cl_src) into a
      temporary directory laid out as the reference's build lays them out
      (cl_common/, cl_sph/; rtpslib/system/sph/CMakeLists.txt:3-11);
-  2. rewrite three pieces of OpenCL-only syntax there, nothing else:
+  2. rewrite four pieces of OpenCL-only syntax there, nothing else:
        `(float4)(a, b, c, d)` / `(int4)(...)`  ->  `make_float4(...)` / `make_int4(...)`
        kernel-scope `__local T name[N];` arrays  ->  `static T name[N];`
        the identity swizzle `v.xyzw`  ->  `v`
+       the implicit Triangle* -> float* argument conversion of one call in
+       collision_tri.cl  ->  the same conversion as an explicit cast, with a
+       barrier in front (the order of shared-memory reads and writes that the
+       32-wide lockstep work-group gives on the GPU)
      (work-groups run one at a time, so a static array is the group's local
      memory);
   3. compile them with clshim.hpp (vector types, built-ins, barrier) and the
@@ -40,21 +44,32 @@ OUT_LIB = os.path.join(OUT_DIR, "librtps_ref.so")
 
 COMMON = ["hash.cl", "cl_hash.h", "cl_structs.h", "cl_macros.h", "cellindices.cl", "permute.cl", "bitonic.cl",
           "gravity.cl"]
-SPH = ["density.cl", "force.cl", "collision_wall.cl", "leapfrog.cl", "euler.cl", "cl_sph_kernels.h", "cl_sph_neighbors.h",
+SPH = ["density.cl", "force.cl", "collision_wall.cl", "collision_tri.cl", "leapfrog.cl", "euler.cl", "cl_sph_kernels.h", "cl_sph_neighbors.h",
        "cl_sph_structs.h", "cl_sph_collision.h", "cl_sph_macros.h"]
 DRIVERS = ["ref_runtime.cpp", "ref_hash.cpp", "ref_bitonic.cpp", "ref_cellindices.cpp", "ref_permute.cpp",
            "ref_density.cpp", "ref_force.cpp", "ref_collision.cpp", "ref_leapfrog.cpp", "ref_domain.cpp",
-           "ref_gravity.cpp", "ref_euler.cpp"]
+           "ref_gravity.cpp", "ref_euler.cpp", "ref_collision_tri.cpp"]
 
 VEC_LITERAL = re.compile(r"\((float4|int4)\)\s*\(")
 LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
 IDENTITY_SWIZZLE = re.compile(r"\.xyzw\b")
+# collision_tri.cl passes its Triangle arrays where float* is declared; C
+# converts the pointers implicitly, C++ needs the cast written out.  The same
+# call refills the shared chunk of 220 triangles with no barrier after the
+# previous chunk's reads: on the GPU the 32 work-items of a group run in
+# lockstep, so every read of chunk k precedes every write of chunk k+1; the
+# fibers here switch only at barriers, so the barrier that lockstep gives is
+# written in front of the copy.
+TRI_TO_FLOATS = "global_to_shared_tri(triangles_glob, triangles,"
+TRI_TO_FLOATS_CPP = ("barrier(CLK_LOCAL_MEM_FENCE); "
+                     "global_to_shared_tri((float*)triangles_glob, (float*)triangles,")
 
 
 def rewrite(text):
     text = VEC_LITERAL.sub(lambda m: "make_%s(" % m.group(1), text)
     text = LOCAL_ARRAY.sub(r"\1static\2", text)
     text = IDENTITY_SWIZZLE.sub("", text)
+    text = text.replace(TRI_TO_FLOATS, TRI_TO_FLOATS_CPP)
     return text
 
 

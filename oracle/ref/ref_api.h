@@ -20,6 +20,8 @@ void ref_gravity(int n, int nsrc, const float* points, const float* masses, cons
                  float* force, float scale);
 void ref_euler(int n, float* pos_u, const float* pos_s, float* vel_u, const float* vel_s, const float* force,
                const uint32_t* idx, const void* sphp, float dt);
+void ref_collision_triangles(int n, const float* pos_s, const float* vel_s, float* force, const float* tris, int ntri,
+                             const void* sphp, float dt);
 void ref_setup_domain(const float* bnd_min, const float* bnd_max, float cell_size, float sim_scale, void* grid,
                       void* grid_scaled);
 }

@@ -124,6 +124,7 @@ struct OracleSim {
     // point sources (System.cpp:260-272) and the integrator (SPH.cpp:392-436)
     std::vector<float> grav_points, grav_masses, grav_alphas;
     int integrator = 0;  // 0 leapfrog, 1 euler
+    std::vector<float> triangles;  // 16 floats per triangle (CollisionTriangle::loadTriangles)
 };
 
 template <class T>
@@ -161,6 +162,14 @@ static void run_gravity(OracleSim& s) {
     for (int i = 0; i < s.num; ++i)
         gravity_one<T>(i, nsrc, s.grav_points.data(), s.grav_masses.data(), s.grav_alphas.data(), s.pos_s.data(),
                        s.force_s.data(), s.sp.simulation_scale);
+}
+template <class T>
+static void run_triangles(OracleSim& s) {
+    const int ntri = (int)(s.triangles.size() / 16);
+    if (ntri == 0) return;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < s.num; ++i)
+        collision_tri_one<T>(i, s.pos_s.data(), s.vel_s.data(), s.force_s.data(), s.triangles.data(), ntri, s.sp);
 }
 template <class T>
 static void run_euler(OracleSim& s, float dt) {
@@ -212,11 +221,13 @@ static void sim_update(OracleSim& s) {
         run_force<double>(s);
         run_gravity<double>(s);
         run_collision<double>(s);
+        run_triangles<double>(s);
     } else {
         run_density<float>(s);
         run_force<float>(s);
         run_gravity<float>(s);
         run_collision<float>(s);
+        run_triangles<float>(s);
     }
 }
 
@@ -338,6 +349,16 @@ void oracle_gravity(int f64, int n, int nsrc, const float* points, const float* 
             gravity_one<float>(i, nsrc, points, masses, alphas, pos_s, force, scale);
     }
 }
+void oracle_collision_triangles(int f64, int n, const float* pos_s, const float* vel_s, float* force,
+                                const float* tris, int ntri, const SPHParams* sp) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < n; ++i) {
+        if (f64)
+            collision_tri_one<double>(i, pos_s, vel_s, force, tris, ntri, *sp);
+        else
+            collision_tri_one<float>(i, pos_s, vel_s, force, tris, ntri, *sp);
+    }
+}
 void oracle_euler(int f64, int n, const float* pos_s, const float* vel_s, const float* force, const uint32_t* idx,
                   const SPHParams* sp, float dt, float* pos_u, float* vel_u) {
 #pragma omp parallel for schedule(static)
@@ -399,6 +420,9 @@ void oracle_sim_set_gravity(void* h, int nsrc, const float* points, const float*
     s->grav_alphas.assign(alphas, alphas + (nsrc > 0 ? nsrc : 0));
 }
 void oracle_sim_set_integrator(void* h, int integrator) { ((OracleSim*)h)->integrator = integrator; }
+void oracle_sim_set_triangles(void* h, const float* tris, int ntri) {
+    ((OracleSim*)h)->triangles.assign(tris, tris + 16 * (size_t)(ntri > 0 ? ntri : 0));
+}
 int oracle_sim_num(void* h) { return ((OracleSim*)h)->num; }
 int oracle_sim_last_nc(void* h) { return ((OracleSim*)h)->last_nc; }
 // field ids follow enum sph_field of include/rtps_sph.h

@@ -340,4 +340,82 @@ inline void euler_one(int i, const float* pos_s, const float* vel_s, const float
     store4(pos_u + 4 * (size_t)o, V4<T>{p.x / sc, p.y / sc, p.z / sc, (T)1});
 }
 
+// Triangle-mesh collision, collision_triangle (sph/cl_src/collision_tri.cl:
+// 436-520 with collisions_triangle :274-374 and intersect_triangle_segment
+// :203-247), run by SPH::collision after the walls (SPH.cpp:303-336).
+// Triangles: 16 floats each (three vertices and a normal, rtpslib/structs.h:
+// 586-590); the normal is not read: the kernel recomputes it from the
+// scaled vertices.  Per particle, triangles in groups of 220 (the kernel's
+// shared-memory chunk): f sums the contributions of a group, then rf += f.
+// A triangle contributes when the segment pos -+ boundary_distance * v/|v|
+// crosses it (Ericson's segment test) at a point tp with
+// d = boundary_distance - |pos - tp| > 1e-6: f += n_hat (k d - c n_hat.v)
+// (repulsion) and then the zero-coefficient "friction" (as the walls).
+// f.w counts the triangles, so force.w grows by the triangle count.  A zero
+// velocity gives NaNs, and no contribution.
+template <class T>
+inline V4<T> cross3(V4<T> a, V4<T> b) {
+    return V4<T>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x, (T)0};
+}
+template <class T>
+inline V4<T> v3normalize(V4<T> a) {
+    const T mag = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    return V4<T>{a.x / mag, a.y / mag, a.z / mag, (T)0};
+}
+template <class T>
+inline T tri_segment_distance(V4<T> pos, V4<T> vel, V4<T> a, V4<T> b, V4<T> c, V4<T> n, T dist) {
+    const V4<T> ab = sub(b, a), ac = sub(c, a);
+    const V4<T> vn = v3normalize(vel);
+    const V4<T> p = sub(pos, mul(vn, dist));
+    const V4<T> q = add(pos, mul(vn, dist));
+    const V4<T> qp = sub(p, q);
+    const T d = dot4(qp, n);
+    if (d <= (T)0) return (T)2 * dist;
+    const V4<T> ap = sub(p, a);
+    T t = dot4(ap, n);
+    if (t < (T)0 || t > d) return (T)2 * dist;
+    const V4<T> e = cross3(qp, ap);
+    T v = dot4(ac, e);
+    if (v < (T)0 || v > d) return (T)2 * dist;
+    T w = -dot4(ab, e);
+    if (w < (T)0 || v + w > d) return (T)2 * dist;
+    const T ood = (T)1 / d;
+    t *= ood;
+    v *= ood;
+    w *= ood;
+    const T u = (T)1 - v - w;
+    const V4<T> tp = add(add(smul(u, a), smul(v, b)), smul(w, c));
+    const V4<T> r = sub(pos, tp);
+    return std::sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+}
+template <class T>
+inline void collision_tri_one(int i, const float* pos_s, const float* vel_s, float* force, const float* tris,
+                              int ntri, const SPHParams& sp) {
+    const T scale = (T)sp.simulation_scale, bound = (T)sp.boundary_distance;
+    const T k = (T)sp.boundary_stiffness, c = (T)sp.boundary_dampening, eps = (T)1e-6f;
+    const V4<T> pos = mul(load4<T>(pos_s + 4 * (size_t)i), scale);
+    const V4<T> vel = load4<T>(vel_s + 4 * (size_t)i);
+    const V4<T> f0 = load4<T>(force + 4 * (size_t)i);
+    V4<T> rf{0, 0, 0, 0};
+    for (int first = 0; first < ntri; first += 220) {
+        const int last = first + 220 < ntri ? first + 220 : ntri;
+        V4<T> f{0, 0, 0, 0};
+        for (int j = first; j < last; ++j) {
+            const float* tj = tris + 16 * (size_t)j;
+            const V4<T> a = mul(load4<T>(tj), scale), b = mul(load4<T>(tj + 4), scale),
+                        cc = mul(load4<T>(tj + 8), scale);
+            const V4<T> n = cross3(sub(b, a), sub(cc, a));
+            const V4<T> nhat = v3normalize(n);
+            const T dd = bound - tri_segment_distance(pos, vel, a, b, cc, n, bound);
+            if (dd > eps) {
+                f = add(f, repulsion(nhat, vel, k, c, dd));
+                f = add(f, friction(vel, f0, nhat));
+            }
+            f.w += (T)1;
+        }
+        rf = add(rf, f);
+    }
+    store4(force + 4 * (size_t)i, add(f0, rf));
+}
+
 }  // namespace sph_oracle

@@ -19,6 +19,10 @@ Fixtures
   gravity_n2048.npz  N=2048, v0 ~ N(0, 0.1^2), two point gravity sources
                      (gravity.cl), with the leapfrog and with the Euler
                      integrator (euler.cl): step 1 forces, state after 1 and 5
+  triangles_n2048.npz N=2048, v0 ~ N(0, 0.3^2), the 524-triangle ramp and box
+                     mesh of scenes.ramp_and_box_mesh (collision_tri.cl after
+                     the walls): step 1 forces before and after the triangle
+                     stage, state after 1, 5 and 20 steps
 Usage: python tests/golden/make_golden.py [--only NAME ...]
 """
 import ctypes as C
@@ -143,12 +147,36 @@ def gravity_fixture():
     return out
 
 
+def triangles_fixture():
+    n = 2048
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n, velocity_sigma=0.3)
+    tris = scenes.ramp_and_box_mesh()
+    out = dict(params_blob(sp, g, gs))
+    out.update({"in_pos": pos, "in_vel": vel, "dt": np.float32(DT), "triangles": tris})
+    R = ref_driver.RefSystem(sp, g, gs, n)
+    R.set_triangles(tris, DT)
+    R.upload(pos, vel)
+    R.update()
+    out["s1_force_pre_tri"] = R.trace["force_pre_triangles"]
+    out["s1_force_s"] = R.force_s[:n].copy()
+    out["s1_sort_indices"] = R.idx[:n].copy()
+    R.integrate(DT)
+    out.update(state(R, "s1_"))
+    R.step(DT, 4)
+    out.update(state(R, "s5_"))
+    R.step(DT, 15)
+    out.update(state(R, "s20_"))
+    return out
+
+
 FIXTURES = {
     "stages_n4096.npz": lambda: stages_fixture(4096, 0.1),
     "ragged_n1000.npz": lambda: stages_fixture(1000, 0.1, steps_after=(3,)),
     "outofgrid_n512.npz": outofgrid_fixture,
     "cfg0_n16384.npz": cfg0_fixture,
     "gravity_n2048.npz": gravity_fixture,
+    "triangles_n2048.npz": triangles_fixture,
 }
 
 

@@ -63,6 +63,8 @@ def oracle():
             "oracle_euler": (None, [_I, _I, _P, _P, _P, _P, _P, _F, _P, _P]),
             "oracle_sim_set_gravity": (None, [_P, _I, _P, _P, _P]),
             "oracle_sim_set_integrator": (None, [_P, _I]),
+            "oracle_collision_triangles": (None, [_I, _I, _P, _P, _P, _P, _I, _P]),
+            "oracle_sim_set_triangles": (None, [_P, _P, _I]),
             "oracle_rollout64": (_I, [_P, _P, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_rollout64_jvp": (_I, [_P, _P, C.c_double, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P,
                                           _P, _P, _P]),
@@ -96,6 +98,7 @@ def ref():
             "ref_setup_domain": (None, [_P, _P, _F, _F, _P, _P]),
             "ref_gravity": (None, [_I, _I, _P, _P, _P, _P, _P, _F]),
             "ref_euler": (None, [_I, _P, _P, _P, _P, _P, _P, _P, _F]),
+            "ref_collision_triangles": (None, [_I, _P, _P, _P, _P, _I, _P, _F]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -144,6 +147,12 @@ class OracleSim:
     def set_integrator(self, kind):
         """0: leapfrog, 1: euler."""
         self.lib.oracle_sim_set_integrator(self.h, int(kind))
+
+    def set_triangles(self, tris):
+        """(m, 4, 4) or (m, 16) float32 triangles; collision_triangle runs after the walls."""
+        t = np.ascontiguousarray(tris, np.float32).reshape(-1, 16)
+        self._tris = t
+        self.lib.oracle_sim_set_triangles(self.h, ptr(t), t.shape[0])
 
     def upload(self, pos, vel, veleval=None):
         pos = np.ascontiguousarray(pos, np.float32)

@@ -9,11 +9,11 @@ host logic between the launches follows rtpslib/system/SPH.cpp:149-300,
   cellindices (start reset to 0xffffffff, nc = start[C]) -> permute ->
   [0 <= nc <= num: keep the first nc sorted particles, copy sorted ->
    unsorted, hash + sort again] -> density -> force -> (gravity: no sources)
-  -> collision_wall -> leapfrog.
+  -> collision_wall -> (collision_triangle, with a mesh loaded) -> leapfrog.
 
 The bitonic sort is not stable.  With canonical=True the sort output is
-re-ordered within equal keys by original index, which is the order that
-BASELINE-level parity is defined in; with canonical=False the raw bitonic
+re-ordered within equal keys by original index, the stable order that the
+parity tests are defined in; with canonical=False the raw bitonic
 order is kept (results then differ from the stable order only by summation
 order within cells).
 """
@@ -55,10 +55,17 @@ class RefSystem:
         # point sources (System.cpp:260-272) and integrator (SPH.cpp:392-436)
         self.grav = None
         self.integrator = "leapfrog"
+        # triangle mesh of CollisionTriangle (sph/Collision_triangle.cpp:44-116)
+        self.tris = None
 
     def set_gravity(self, points, masses, alphas):
         self.grav = (np.ascontiguousarray(points, np.float32).reshape(-1, 4),
                      np.ascontiguousarray(masses, np.float32), np.ascontiguousarray(alphas, np.float32))
+
+    def set_triangles(self, tris, dt):
+        """(m, 4, 4) float32 triangles; dt is the time_step argument of the
+        kernel (passed, not read)."""
+        self.tris = (np.ascontiguousarray(tris, np.float32).reshape(-1, 16), float(dt))
 
     def upload(self, pos, vel):
         n = pos.shape[0]
@@ -114,6 +121,11 @@ class RefSystem:
         self.trace["force_pre_collision"] = self.force_s[:n].copy()
         if collision:
             L.ref_collision_wall(n, P(self.pos_s), P(self.vel_s), P(self.force_s), C.addressof(self.gs), sp)
+            if self.tris is not None:
+                # SPH::collision: collision_tri after collision_wall (SPH.cpp:303-336)
+                self.trace["force_pre_triangles"] = self.force_s[:n].copy()
+                t, dt = self.tris
+                L.ref_collision_triangles(n, P(self.pos_s), P(self.vel_s), P(self.force_s), P(t), t.shape[0], sp, dt)
 
     def integrate(self, dt):
         n = self.num

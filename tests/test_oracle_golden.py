@@ -153,3 +153,72 @@ def test_oracle_gravity_and_euler_equal_reference_kernels_on_random_data():
     O.oracle_euler(0, n, P(pos), P(vel), P(big), P(idx), C.addressof(sp), 0.001, P(po), P(vo))
     np.testing.assert_array_equal(po, pr)
     np.testing.assert_array_equal(vo, vr)
+
+
+def near_mesh_particles(tris, n, bound, scale, seed):
+    """n particles placed around the mesh: a random point of a random triangle
+    moved along its normal by up to 1.5 boundary distances, velocities
+    N(0, 1) (every 50th zero, every 7th along the normal)."""
+    from enjaparticles_gb300.scenes import normal, uniform
+    t = np.asarray(tris, np.float64).reshape(-1, 4, 4)
+    pick = (uniform(seed, n) * t.shape[0]).astype(np.int64)
+    b = uniform(seed + 1, 2 * n).reshape(n, 2)
+    flip = b.sum(1) > 1
+    b[flip] = 1 - b[flip]
+    a, e1, e2 = t[pick, 0, :3], t[pick, 1, :3] - t[pick, 0, :3], t[pick, 2, :3] - t[pick, 0, :3]
+    nrm = t[pick, 3, :3]
+    off = (2 * uniform(seed + 2, n) - 1) * 1.5 * bound / scale
+    pos = np.ones((n, 4), np.float32)
+    pos[:, :3] = a + b[:, :1] * e1 + b[:, 1:] * e2 + off[:, None] * nrm
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :3] = normal(seed + 3, 3 * n).reshape(n, 3)
+    vel[::7, :3] = -nrm[::7] * (0.5 + uniform(seed + 4, n)[::7, None])
+    vel[::50] = 0.0
+    return pos, vel
+
+
+@pytest.mark.skipif(not ob.ref_available(), reason="reference kernels not built here (needs the reference tree)")
+@pytest.mark.parametrize("scale", [1.0, 0.05])
+def test_oracle_triangle_collision_equals_reference_kernel_on_random_data(scale):
+    """collision_triangle (collision_tri.cl:436-520): 524 triangles (three
+    shared-memory chunks of 220), particles around every face moving in every
+    direction, zero velocities included; simulation_scale 1 and 0.05."""
+    from enjaparticles_gb300 import abi
+    from enjaparticles_gb300.scenes import ramp_and_box_mesh, uniform
+    R, O = ob.ref(), ob.oracle()
+    n = 3000
+    sp, _, _ = abi.dambreak_params(n)
+    tris = ramp_and_box_mesh()
+    if scale != 1.0:
+        sp.simulation_scale = scale
+        tris = tris.copy()
+        tris[:, :3, :3] /= scale
+    tris = np.ascontiguousarray(tris.reshape(-1, 16))
+    pos, vel = near_mesh_particles(tris, n, sp.boundary_distance, scale, 601)
+    f0 = ((uniform(605, 4 * n).reshape(n, 4) - 0.5) * 40).astype(np.float32)
+    fr, fo = f0.copy(), f0.copy()
+    R.ref_collision_triangles(n, P(pos), P(vel), P(fr), P(tris), tris.shape[0], C.addressof(sp), 0.001)
+    O.oracle_collision_triangles(0, n, P(pos), P(vel), P(fo), P(tris), tris.shape[0], C.addressof(sp))
+    hit = np.abs(fr[:, :3] - f0[:, :3]).max(1) > 0
+    assert hit.sum() > n // 5  # a good share of the particles touch the mesh
+    np.testing.assert_array_equal(fo, fr)
+
+
+def test_oracle_triangle_mesh_rollout_matches_reference_golden():
+    """SPH::collision with a triangle mesh loaded (collision_wall, then
+    collision_triangle; SPH.cpp:303-336): step-1 force and the state after 1,
+    5 and 20 steps equal the reference kernels' bit for bit."""
+    d, sp, g, gs = golden_io.load("triangles_n2048.npz")
+    n = d["in_pos"].shape[0]
+    sim = ob.OracleSim(sp, g, gs, n)
+    sim.set_triangles(d["triangles"])
+    sim.upload(d["in_pos"], d["in_vel"])
+    sim.update()
+    np.testing.assert_array_equal(sim.get("force_s"), d["s1_force_s"])
+    sim.integrate(float(d["dt"]))
+    done = 1
+    for k in (1, 5, 20):
+        sim.step(float(d["dt"]), k - done)
+        done = k
+        for f in ("pos_u", "vel_u", "veleval_u"):
+            np.testing.assert_array_equal(sim.get(f), d["s%d_%s" % (k, f)], err_msg="step %d %s" % (k, f))
