@@ -41,6 +41,7 @@ assert C.sizeof(GridParams) == 128 and GridParams.nb_cells.offset == 112
 SPH_OK, SPH_EINVAL, SPH_ENOMEM, SPH_ECUDA, SPH_EOOB, SPH_ETIMEOUT, SPH_ESTATE = 0, -1, -2, -3, -4, -5, -6
 SPH_INTEGRATOR_LEAPFROG, SPH_INTEGRATOR_EULER = 0, 1
 SPH_MAX_GRAVITY_SOURCES = 64
+SPH_MAX_TRIANGLES = 1 << 20
 STATUS_NAMES = {0: "SPH_OK", -1: "SPH_EINVAL", -2: "SPH_ENOMEM", -3: "SPH_ECUDA", -4: "SPH_EOOB",
                 -5: "SPH_ETIMEOUT", -6: "SPH_ESTATE"}
 EMPTY_CELL = 0xFFFFFFFF
@@ -100,6 +101,8 @@ SIGNATURES = {
     "sph_stage_euler": (_I, [_P, _F]),
     "sph_set_gravity_sources": (_I, [_P, _I, _P, _P, _P]),
     "sph_set_integrator": (_I, [_P, _I]),
+    "sph_stage_collision_triangles": (_I, [_P]),
+    "sph_load_triangles": (_I, [_P, _P, _I]),
     "sph_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
     "sph_adjoint_rollout": (_I, [_P, _I, _I, _P, _P, C.POINTER(_F)]),
     "sph_batch_create": (_I, [_I, _P, _P, _P, _P, C.POINTER(_P)]),

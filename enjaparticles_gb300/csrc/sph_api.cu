@@ -138,6 +138,11 @@ int sph_make_step_params(const SPHParams& s, const GridParams& gp, const GridPar
     P.grav_alpha = nullptr;
     P.integrator = sphk::kIntegratorLeapfrog;
     P.exact = 0;
+    P.n_tri = 0;
+    P.tri_bound = s.boundary_distance;
+    P.tri_raw = nullptr;
+    P.tri_geo = nullptr;
+    P.tri_box = nullptr;
     return SPH_OK;
 }
 
@@ -175,6 +180,12 @@ int build_step_params(sph_ctx* c) {
     c->P.grav_alpha = c->P.grav_mass + sphk::kMaxGravitySources;
     c->P.integrator = c->integrator;
     c->P.exact = c->exact;
+    c->P.n_tri = c->n_tri;
+    if (c->tri) {
+        c->P.tri_raw = c->tri;
+        c->P.tri_geo = c->tri + 4 * (size_t)c->tri_cap;
+        c->P.tri_box = c->tri + 8 * (size_t)c->tri_cap;
+    }
     c->params_version++;
     return SPH_OK;
 }
@@ -222,7 +233,7 @@ void free_all(sph_ctx* c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
                     c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
-                    c->cell_start, c->cell_end, c->info, c->scratch, c->grav};
+                    c->cell_start, c->cell_end, c->info, c->scratch, c->grav, c->tri};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
@@ -286,7 +297,40 @@ void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t 
 
 }  // namespace
 
+// SPH::update as staged launches: hash, sort, cellindices+permute,
+// out-of-grid deletion, density, force, gravity, walls, triangles.
+static int enqueue_update(sph_ctx* c) {
+    int rc = enqueue_hash(c);
+    if (rc) return rc;
+    if ((rc = enqueue_sort(c))) return rc;
+    sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
+                               c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 2, c->stream);
+    sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
+                               c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
+    density_launch(c, c->idx_a, false, c->stream);
+    force_launch(c, c->idx_a, false, 0.f, c->stream);
+    sphk::launch_gravity(c->pos_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
+    sphk::launch_collision(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
+    sphk::launch_triangles(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
 int enqueue_fused_step(sph_ctx* c, float dt) {
+    if (c->n_tri > 0) {
+        // the triangle stage sits between the walls and the integrator, so
+        // the step runs the staged sequence
+        int rc = enqueue_update(c);
+        if (rc) return rc;
+        if (c->integrator == sphk::kIntegratorEuler)
+            sphk::launch_euler(c->pos_s, c->vel_s, c->force_s, c->idx_a, c->pos_u, c->vel_u, c->info, c->P, dt,
+                               c->num_hint, c->stream);
+        else
+            sphk::launch_leapfrog(c->pos_s, c->vel_s, c->force_s, c->xsph_s, c->idx_a, c->pos_u, c->vel_u,
+                                  c->veleval_u, c->info, c->P, dt, c->num_hint, c->stream);
+        CK_LAUNCH(c);
+        return SPH_OK;
+    }
     int rc = enqueue_hash(c);
     if (rc) return rc;
     rc = enqueue_sort(c);
@@ -514,6 +558,35 @@ int sph_set_gravity_sources(sph_ctx* c, int count, const sph_float4* points, con
     return build_step_params(c);
 }
 
+int sph_load_triangles(sph_ctx* c, const sph_float4* tris, int count) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (count < 0 || count > sphk::kMaxTriangles)
+        return set_err(c, SPH_EINVAL, "sph_load_triangles: count %d outside [0, %d]", count, sphk::kMaxTriangles);
+    if (count > 0 && !tris) return set_err(c, SPH_EINVAL, "sph_load_triangles: null array");
+    for (int j = 0; j < count; ++j)
+        for (int k = 0; k < 3; ++k) {
+            const sph_float4& v = tris[4 * (size_t)j + k];
+            if (!std::isfinite(v.x) || !std::isfinite(v.y) || !std::isfinite(v.z) || !std::isfinite(v.w))
+                return set_err(c, SPH_EINVAL, "sph_load_triangles: vertex %d of triangle %d is not finite", k, j);
+        }
+    if (count > c->tri_cap) {
+        CK(c, cudaStreamSynchronize(c->stream));  // queued work may still read the old mesh
+        if (c->tri) CK(c, cudaFree(c->tri));
+        c->tri = nullptr;
+        c->tri_cap = 0;
+        c->n_tri = 0;
+        CK(c, cudaMalloc(&c->tri, sizeof(float4) * 10 * (size_t)count));
+        c->tri_cap = count;
+    }
+    if (count > 0) {
+        CK(c, cudaMemcpyAsync(c->tri, tris, sizeof(float4) * 4 * (size_t)count, cudaMemcpyHostToDevice, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));  // the host array may go away
+    }
+    c->n_tri = count;
+    return build_step_params(c);
+}
+
 int sph_set_integrator(sph_ctx* c, int integrator) {
     if (!c) return SPH_EINVAL;
     if (integrator != SPH_INTEGRATOR_LEAPFROG && integrator != SPH_INTEGRATOR_EULER)
@@ -691,6 +764,14 @@ int sph_stage_gravity(sph_ctx* c) {
     return SPH_OK;
 }
 
+int sph_stage_collision_triangles(sph_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    sphk::launch_triangles(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
 int sph_stage_euler(sph_ctx* c, float dt) {
     int rc = check_ctx(c);
     if (rc) return rc;
@@ -714,18 +795,7 @@ int sph_stage_leapfrog(sph_ctx* c, float dt) {
 int sph_update(sph_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
-    if ((rc = enqueue_hash(c))) return rc;
-    if ((rc = enqueue_sort(c))) return rc;
-    sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
-                               c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 2, c->stream);
-    sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
-                               c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
-    density_launch(c, c->idx_a, false, c->stream);
-    force_launch(c, c->idx_a, false, 0.f, c->stream);
-    sphk::launch_gravity(c->pos_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
-    sphk::launch_collision(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
-    CK_LAUNCH(c);
-    return SPH_OK;
+    return enqueue_update(c);
 }
 
 int sph_integrate(sph_ctx* c, float dt) {
@@ -785,6 +855,8 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
     if (rc) return rc;
     if (nsteps < 0 || !std::isfinite(dt) || !kernel_ms || cap <= 0)
         return set_err(c, SPH_EINVAL, "sph_step_profile: bad arguments");
+    if (c->n_tri > 0)
+        return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step; with a triangle mesh the step is staged");
     // Launches of one fused step: prologue, hash, sort reset, radix passes,
     // cells+permute, density, force+collision+leapfrog.
     const int nk = 6 + c->passes;

@@ -48,6 +48,10 @@ struct sph_ctx {
     float4* grav = nullptr;
     int n_grav = 0;
     int integrator = 0;
+    // triangle mesh: one allocation of tri_cap * 10 float4 (raw, geo, box)
+    float4* tri = nullptr;
+    int n_tri = 0;
+    int tri_cap = 0;
     // graph of one fused step
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.f;

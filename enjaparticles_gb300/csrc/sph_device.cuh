@@ -62,10 +62,17 @@ struct StepParams {
     const float* grav_alpha;
     int integrator;               // kIntegratorLeapfrog or kIntegratorEuler
     int exact;                    // exact arithmetic in the elementwise stages
+    // triangle mesh (collision_tri.cl), none by default
+    int n_tri;
+    float tri_bound;              // boundary_distance
+    const float4* tri_raw;        // 4 float4 per triangle, as loaded
+    float4* tri_geo;              // 4 float4 per triangle (sph_triangles.cu)
+    float4* tri_box;              // 2 float4 per triangle
 };
 constexpr int kIntegratorLeapfrog = 0;
 constexpr int kIntegratorEuler = 1;
 constexpr int kMaxGravitySources = 64;
+constexpr int kMaxTriangles = 1 << 20;
 
 // Scenes of the neighbour passes.
 //   OneScene: one particle system; the step parameters are the kernel
@@ -171,6 +178,9 @@ void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* for
                      const StepParams& p, float dt, int grid_items, cudaStream_t st);
 void launch_gravity(const float4* pos_s, float4* force_s, const int* info, const StepParams& p, int grid_items,
                     cudaStream_t st);
+// collision_triangle after the walls; no-op without a mesh.
+void launch_triangles(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info, const StepParams& p,
+                      int grid_items, cudaStream_t st);
 void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_s, uint32_t* idx, float4* pos_u,
                   float4* vel_u, const int* info, const StepParams& p, float dt, int grid_items, cudaStream_t st);
 void launch_delete_staged(const float4* pos_s, const float4* vel_s, const float4* veleval_s, uint32_t* idx,

@@ -144,6 +144,17 @@ class SPH:
     def euler(self, dt):
         self._ck(self.lib.sph_stage_euler(self.ctx, float(dt)))
 
+    def collision_triangles(self):
+        """CollisionTriangle::execute: force_s += the loaded mesh's contacts."""
+        self._ck(self.lib.sph_stage_collision_triangles(self.ctx))
+
+    # -- triangle mesh (sph/Collision_triangle.cpp:44-82) ---------------------
+    def loadTriangles(self, tris):
+        """(m, 4, 4) or (m, 16) float32: three vertices and a normal per
+        triangle (scenes.ramp_mesh and box_mesh make them); m = 0 unloads."""
+        t = np.ascontiguousarray(tris, np.float32).reshape(-1, 16)
+        self._ck(self.lib.sph_load_triangles(self.ctx, t.ctypes.data if t.shape[0] else None, t.shape[0]))
+
     # -- point sources and integrator (System.cpp:260-272, SPH.cpp:392-436) --
     def setGravitySources(self, points, masses, alphas):
         pts = np.ascontiguousarray(points, np.float32).reshape(-1, 4)

@@ -254,6 +254,13 @@ int sph_stage_gravity(sph_ctx* ctx);
  * gravity is the constant -9.8 in z and its acceleration limit the constant
  * 600, as in the reference; it writes pos_u and vel_u and leaves veleval_u. */
 int sph_stage_euler(sph_ctx* ctx, float dt);
+/* CollisionTriangle::execute (sph/Collision_triangle.cpp:84-116;
+ * collision_tri.cl:436-520), the second half of SPH::collision (SPH.cpp:
+ * 303-336): force_s += the repulsion and friction of the triangles of the
+ * mesh loaded by sph_load_triangles whose segment test (particle position
+ * -+ boundary_distance along the velocity) hits them, and force_s.w += the
+ * triangle count.  Always in exact arithmetic.  No-op without a mesh. */
+int sph_stage_collision_triangles(sph_ctx* ctx);
 
 /* Point gravity sources: the settings gravity_sources / gravity_mass /
  * gravity_alphas of System::prepareSorted (System.cpp:260-272).  count
@@ -272,18 +279,29 @@ int sph_set_gravity_sources(sph_ctx* ctx, int count, const sph_float4* points, c
 #define SPH_INTEGRATOR_EULER 1
 int sph_set_integrator(sph_ctx* ctx, int integrator);
 
-/* SPH::update (SPH.cpp:117-125 -> updateGPU :149-300) with the wall collision
- * of SPH::collision (SPH.cpp:303-336) enabled after gravity: hash, sort,
- * cellindices, permute, out-of-grid deletion, density, force, point-source
- * gravity, collision. */
+/* SPH::loadTriangles -> CollisionTriangle::loadTriangles (sph/
+ * Collision_triangle.cpp:44-82).  count triangles of four sph_float4 each
+ * (three vertices, unscaled, and a normal: rtps Triangle, structs.h:586-590);
+ * the stored normal is not read, the kernel uses (b-a)x(c-a) normalised.
+ * count 0 unloads the mesh.  The reference's buffer holds 2048 triangles;
+ * this one grows to SPH_MAX_TRIANGLES.  Non-finite vertices are rejected.
+ * Blocking. */
+#define SPH_MAX_TRIANGLES (1 << 20)
+int sph_load_triangles(sph_ctx* ctx, const sph_float4* tris, int count);
+
+/* SPH::update (SPH.cpp:117-125 -> updateGPU :149-300) with SPH::collision
+ * (SPH.cpp:303-336) enabled after gravity: hash, sort, cellindices, permute,
+ * out-of-grid deletion, density, force, point-source gravity, walls, and the
+ * triangle mesh when one is loaded. */
 int sph_update(sph_ctx* ctx);
 /* SPH::integrate (SPH.cpp:389-441): the integrator sph_set_integrator chose. */
 int sph_integrate(sph_ctx* ctx, float dt);
 
 /* nsteps x (update + integrate) on the fused path: hash -> sort ->
  * cellindices+permute -> density -> force+gravity+collision+integrator, replayed from a
- * captured CUDA graph.  Results equal nsteps staged update()+integrate()
- * calls.  Asynchronous. */
+ * captured CUDA graph.  With a triangle mesh loaded the graph holds the
+ * staged launches of update + integrate instead.  Results equal nsteps staged
+ * update()+integrate() calls.  Asynchronous. */
 int sph_step(sph_ctx* ctx, float dt, int nsteps);
 
 /* The same fused step launched kernel by kernel, without a graph (for
@@ -294,7 +312,8 @@ int sph_step_eager(sph_ctx* ctx, float dt, int nsteps);
  * launches on the context stream, for per-kernel timing.  kernel_ms[k]
  * accumulates the device time of launch k of the step (k < cap); *nkernels
  * gets the number of launches per step; names come from
- * sph_profile_kernel_name.  Blocking. */
+ * sph_profile_kernel_name.  SPH_ESTATE with a triangle mesh loaded.
+ * Blocking. */
 int sph_step_profile(sph_ctx* ctx, float dt, int nsteps, float* kernel_ms, int cap, int* nkernels);
 const char* sph_profile_kernel_name(sph_ctx* ctx, int k);
 

@@ -30,6 +30,13 @@ inline float4 make_float4(float x, float y, float z, float w) {
     return v;
 }
 
+// rtps::Triangle (rtpslib/structs.h:586-590): three vertices and a normal.
+struct Triangle {
+    float4 verts[3];
+    float4 normal;
+};
+static_assert(sizeof(Triangle) == 64, "Triangle must be 16 floats");
+
 class SPHError : public std::runtime_error {
 public:
     SPHError(int code, const std::string& what) : std::runtime_error(what), code_(code) {}
@@ -77,7 +84,7 @@ public:
     SPH(SPH&& o) noexcept : ctx_(o.ctx_), max_num_(o.max_num_), dt_(o.dt_) { o.ctx_ = nullptr; }
 
     // --- System virtual API (System.h:64-75) ---
-    void update() { check(sph_update(ctx_)); }           // hash .. density, force, walls (SPH::updateGPU)
+    void update() { check(sph_update(ctx_)); }           // hash .. density, force, walls, mesh (SPH::updateGPU)
     void interact() {}                                    // no coupled systems
     void integrate() { check(sph_integrate(ctx_, dt_)); } // leapfrog (SPH::integrate)
     void postProcess() {}
@@ -123,6 +130,12 @@ public:
         (void)mass;
         if (pos.size() != vel.size()) throw SPHError(SPH_EINVAL, "pushParticles: pos and vel sizes differ");
         check(sph_push_particles(ctx_, pos.data(), vel.data(), (int)pos.size()));
+    }
+    // SPH::loadTriangles (sph/Collision_triangle.cpp:44-82): the mesh that
+    // SPH::collision tests after the walls; an empty vector unloads it.
+    void loadTriangles(std::vector<Triangle>& triangles) {
+        check(sph_load_triangles(ctx_, triangles.empty() ? nullptr : &triangles[0].verts[0],
+                                 (int)triangles.size()));
     }
     std::vector<float4> getDeletedPos() { return deleted(true); }
     std::vector<float4> getDeletedVel() { return deleted(false); }
