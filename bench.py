@@ -17,6 +17,8 @@ synthetic dam-break lattice (no dataset exists for it).
          HBM copy bandwidth.
   cpu_baseline  the CPU oracle (a port of the reference's kernels) on the
          host cores for a bounded sample.
+  triangles  the same dam break with a 524-triangle mesh (collision_tri.cl
+         after the walls): step time and the triangle stage's roofline.
 
 `--impl reference` times the reference's CPU implementation instead: the
 reference's OpenCL kernels cannot run on these machines (no OpenCL driver),
@@ -70,6 +72,8 @@ def parse():
     ap.add_argument("--adj-n", type=int, default=65536)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-k", type=int, default=20)
+    ap.add_argument("--no-triangles", action="store_true")
+    ap.add_argument("--tri-steps", type=int, default=0, help="0: same as --steps")
     return ap.parse_args()
 
 
@@ -374,6 +378,57 @@ def bench_calibration(args, torch):
             "note": "host wall clock around the whole loop (rollouts, losses, backward passes, iRprop- steps on log mu)"}
 
 
+def bench_triangles(args, torch, peak):
+    """Triangle-mesh collision (collision_tri.cl after the walls): the 2M
+    dam break with the 524-triangle ramp-and-box mesh of
+    scenes.ramp_and_box_mesh loaded (the ramp cuts through the fluid block).
+      step   as many steps as the headline run of sph_step (the staged sequence with the
+             triangle stage, replayed from a graph), CUDA events
+      stage  sph_stage_collision_triangles alone (prep + contact kernels)
+             over 50 launches on the state of the last step; its
+             algorithmic bytes are 64 per particle (read position,
+             velocity, force; write force) against the measured HBM copy
+             bandwidth."""
+    from enjaparticles_gb300 import abi, scenes
+    from enjaparticles_gb300.sph import SPH
+    import ctypes as C
+    n = args.n
+    sp, g, gs = abi.dambreak_params(n)
+    pos0, vel0 = scenes.dambreak(n)
+    tris = scenes.ramp_and_box_mesh()
+    s = SPH(sp, g, n, gs)
+    stream = torch.cuda.current_stream()
+    abi.check(s.lib, s.ctx, s.lib.sph_set_stream(s.ctx, C.c_void_p(stream.cuda_stream)))
+    s.loadTriangles(tris)
+    s.upload(pos0, vel0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = args.tri_steps or args.steps
+    s.step(DT, args.warmup)
+    s.sync()
+    e0.record(stream)
+    s.step(DT, steps)
+    e1.record(stream)
+    e1.synchronize()
+    t_step = e0.elapsed_time(e1) / steps
+    reps = 50
+    s.collision_triangles()
+    s.sync()
+    e0.record(stream)
+    for _ in range(reps):
+        abi.check(s.lib, s.ctx, s.lib.sph_stage_collision_triangles(s.ctx))
+    e1.record(stream)
+    e1.synchronize()
+    t_stage = e0.elapsed_time(e1) / reps
+    num = s.getNum()
+    s.close()
+    achieved = 64.0 * num / (t_stage / 1e3) / 1e9
+    return {"metric": "particle-updates/s with a triangle mesh", "value": num * 1e3 / t_step,
+            "unit": "particle-updates/s", "particles": num, "triangles": int(tris.shape[0]), "steps": steps,
+            "ms_per_step": t_step, "stage_ms": t_stage,
+            "stage_roofline": {"bound": "hbm", "algorithmic_bytes": 64 * num, "achieved": achieved, "peak": peak,
+                               "unit": "GB/s", "frac": achieved / peak}}
+
+
 def config_block(n, c):
     return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001, "
                         "1000-step rollout config" % n,
@@ -504,6 +559,8 @@ def main():
         line["batched"] = bench_batched(args, torch)
     if rank == 0 and not args.no_adjoint:
         line["adjoint"] = bench_adjoint(args, torch)
+    if rank == 0 and not args.no_triangles:
+        line["triangles"] = bench_triangles(args, torch, peak)
     if rank == 0 and not args.no_calibration:
         line["calibration"] = bench_calibration(args, torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
