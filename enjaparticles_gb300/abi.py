@@ -103,6 +103,17 @@ SIGNATURES = {
     "sph_set_integrator": (_I, [_P, _I]),
     "sph_stage_collision_triangles": (_I, [_P]),
     "sph_load_triangles": (_I, [_P, _P, _I]),
+    "sph_hose_create": (_I, [_F, _I, sph_float4, sph_float4, _F, _F, C.POINTER(_P)]),
+    "sph_hose_update": (_I, [_P, sph_float4, sph_float4, _F, _F]),
+    "sph_hose_refill": (_I, [_P, _I]),
+    "sph_hose_spray": (_I, [_P, C.POINTER(_I)]),
+    "sph_hose_particles": (_I, [_P, _P, _I, C.POINTER(sph_float4)]),
+    "sph_hose_remaining": (_I, [_P, C.POINTER(_I)]),
+    "sph_hose_destroy": (None, [_P]),
+    "sph_add_hose": (_I, [_P, _I, sph_float4, sph_float4, _F, _F, C.POINTER(_I)]),
+    "sph_update_hose": (_I, [_P, _I, sph_float4, sph_float4, _F]),
+    "sph_refill_hose": (_I, [_P, _I, _I]),
+    "sph_spray_hoses": (_I, [_P, C.POINTER(_I)]),
     "sph_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
     "sph_adjoint_rollout": (_I, [_P, _I, _I, _P, _P, C.POINTER(_F)]),
     "sph_batch_create": (_I, [_I, _P, _P, _P, _P, C.POINTER(_P)]),
@@ -133,6 +144,12 @@ SIGNATURES = {
 }
 
 _lib = None
+
+
+def vec4(v):
+    """A sph_float4 from a sequence of 3 or 4 numbers (w = 0 when absent)."""
+    v = [float(x) for x in v] + [0.0] * (4 - len(v))
+    return sph_float4(*v[:4])
 
 
 def load_library(path=None):

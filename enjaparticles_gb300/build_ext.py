@@ -17,10 +17,11 @@ LIB = os.path.join(PKG, "librtps_sph.so")
 DRIVER = os.path.join(PKG, "sph_bench")
 
 SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cells.cu", "sph_density.cu", "sph_force.cu", "sph_integrate.cu",
-           "sph_triangles.cu", "sph_batch.cu", "sph_noalloc.cu", "sph_adjoint.cu", "sph_params.cpp"]
-# Per-file flags: the density pass relies on every multiply and add being
-# rounded on its own.
-EXTRA = {"sph_density.cu": ["-fmad=false"]}
+           "sph_triangles.cu", "sph_batch.cu", "sph_noalloc.cu", "sph_adjoint.cu", "sph_params.cpp",
+           "sph_hose.cpp"]
+# Per-file flags: the density pass and the hose's host arithmetic rely on
+# every multiply and add being rounded on its own (no contraction, on any host).
+EXTRA = {"sph_density.cu": ["-fmad=false"], "sph_hose.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -41,7 +42,7 @@ def _compile(src, ptxas_verbose):
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]
     else:
-        cmd += ["-x", "c++"]
+        cmd += ["-x", "c++"] + EXTRA.get(src, [])
     r = subprocess.run(cmd, capture_output=True, text=True)
     return src, obj, r.returncode, r.stdout + r.stderr, " ".join(cmd)
 

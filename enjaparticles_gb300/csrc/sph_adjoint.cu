@@ -785,10 +785,10 @@ int sph_adjoint_record(sph_ctx* c, float dt, int nsteps, int K) {
     }
     sph_adjoint* a = c->adj;
     a->recorded = 0;
-    if (c->n_grav > 0 || c->n_tri > 0 || c->integrator != sphk::kIntegratorLeapfrog)
+    if (c->n_grav > 0 || c->n_tri > 0 || !c->hoses.empty() || c->integrator != sphk::kIntegratorLeapfrog)
         return set_err(c, SPH_ESTATE,
-                       "the differentiable rollout covers the leapfrog step without point gravity sources or a "
-                       "triangle mesh");
+                       "the differentiable rollout covers the leapfrog step without point gravity sources, a "
+                       "triangle mesh or hoses");
     if ((rc = read_info(c))) return rc;
     if (c->host_info[sphk::kOutStart] >= 0)
         return set_err(c, SPH_ESTATE, "an out-of-grid deletion is pending; step once before recording");

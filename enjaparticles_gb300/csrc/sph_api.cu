@@ -489,6 +489,7 @@ int sph_destroy(sph_ctx* c) {
     if (!c) return SPH_EINVAL;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (sph_hose* h : c->hoses) sph_hose_destroy(h);
     free_all(c);
     delete c;
     return SPH_OK;
@@ -795,7 +796,80 @@ int sph_stage_leapfrog(sph_ctx* c, float dt) {
 int sph_update(sph_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
+    if (!c->hoses.empty() && (rc = sph_spray_hoses(c, nullptr))) return rc;
     return enqueue_update(c);
+}
+
+// --- hoses (SPH.cpp:523-558) ---------------------------------------------------
+namespace {
+// The "spacing" setting (SPHSettings.cpp:94-97): rest_distance over
+// simulation_scale, through the settings' 6-digit round trip.
+float sph_spacing(const sph_ctx* c) { return sph_settings_round(c->sp.rest_distance / c->sp.simulation_scale); }
+}  // namespace
+
+int sph_add_hose(sph_ctx* c, int total_n, sph_float4 center, sph_float4 velocity, float radius, float dt,
+                 int* index) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    const float spacing = sph_spacing(c);
+    sph_hose* h = nullptr;
+    rc = sph_hose_create(dt, total_n, center, velocity, radius * spacing, spacing, &h);
+    if (rc) return set_err(c, rc, "sph_add_hose: bad arguments");
+    c->hoses.push_back(h);
+    if (index) *index = (int)c->hoses.size() - 1;
+    return SPH_OK;
+}
+
+int sph_update_hose(sph_ctx* c, int index, sph_float4 center, sph_float4 velocity, float radius) {
+    if (!c) return SPH_EINVAL;
+    if (index < 0 || index >= (int)c->hoses.size()) return set_err(c, SPH_EINVAL, "no hose %d", index);
+    const float spacing = sph_spacing(c);
+    const int rc = sph_hose_update(c->hoses[index], center, velocity, radius * spacing, spacing);
+    return rc ? set_err(c, rc, "sph_update_hose: bad arguments") : SPH_OK;
+}
+
+int sph_refill_hose(sph_ctx* c, int index, int n) {
+    if (!c) return SPH_EINVAL;
+    if (index < 0 || index >= (int)c->hoses.size()) return set_err(c, SPH_EINVAL, "no hose %d", index);
+    const int rc = sph_hose_refill(c->hoses[index], n);
+    return rc ? set_err(c, rc, "sph_refill_hose: bad arguments") : SPH_OK;
+}
+
+int sph_spray_hoses(sph_ctx* c, int* added) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (added) *added = 0;
+    const int hint0 = c->num_hint;
+    bool pushed = false;
+    for (sph_hose* h : c->hoses) {
+        int k = 0;
+        sph_hose_spray(h, &k);
+        if (k == 0) continue;
+        std::vector<sph_float4> pos((size_t)k), vel((size_t)k);
+        sph_float4 v;
+        sph_hose_particles(h, pos.data(), k, &v);
+        for (auto& e : vel) e = v;
+        int cur = 0;
+        if ((rc = sph_get_num(c, &cur))) return rc;
+        if (cur + k > c->max_num) continue;  // dropped, as SPH::pushParticles does (SPH.cpp:562-567)
+        if ((rc = sph_push_particles(c, pos.data(), vel.data(), k))) return rc;
+        pushed = true;
+        if (added) *added += k;
+    }
+    if (pushed) {
+        // An upper bound of the count that stays put while the hoses empty
+        // (pushes move particles from the hoses into the system), so that
+        // the step graph, sized by it, is not re-captured at every spray.
+        long pending = 0;
+        for (sph_hose* h : c->hoses) {
+            int r = 0;
+            sph_hose_remaining(h, &r);
+            pending += r;
+        }
+        const long bound = std::min<long>(c->max_num, (long)c->num_hint + pending);
+        c->num_hint = (int)std::max<long>(hint0, bound);
+    }
+    return SPH_OK;
 }
 
 int sph_integrate(sph_ctx* c, float dt) {
@@ -803,11 +877,34 @@ int sph_integrate(sph_ctx* c, float dt) {
     return c->integrator == SPH_INTEGRATOR_EULER ? sph_stage_euler(c, dt) : sph_stage_leapfrog(c, dt);
 }
 
+static int ensure_step_graph(sph_ctx* c, float dt);
+
 int sph_step(sph_ctx* c, float dt, int nsteps) {
     int rc = check_ctx(c);
     if (rc) return rc;
     if (nsteps < 0 || !std::isfinite(dt)) return set_err(c, SPH_EINVAL, "sph_step: bad arguments");
-    if (nsteps == 0 || c->num_hint == 0) return SPH_OK;
+    if (!c->hoses.empty()) {
+        // SPH::updateGPU sprays the hoses before every step (SPH.cpp:162-166)
+        for (int k = 0; k < nsteps; ++k) {
+            if ((rc = sph_spray_hoses(c, nullptr))) return rc;
+            if (c->num_hint == 0) continue;
+            if ((rc = ensure_step_graph(c, dt))) return rc;
+            CK(c, cudaGraphLaunch(c->graph, c->stream));
+        }
+    } else {
+        if (nsteps == 0 || c->num_hint == 0) return SPH_OK;
+        if ((rc = ensure_step_graph(c, dt))) return rc;
+        for (int k = 0; k < nsteps; ++k) CK(c, cudaGraphLaunch(c->graph, c->stream));
+    }
+    c->keys_cur = c->keys_a;
+    c->idx_cur = c->idx_a;
+    return SPH_OK;
+}
+
+// (Re-)captures the graph of one step when dt, the particle bound, the
+// arithmetic mode or the parameters changed since the last capture.
+static int ensure_step_graph(sph_ctx* c, float dt) {
+    int rc = SPH_OK;
     const bool stale = !c->graph || c->graph_dt != dt || c->graph_num != c->num_hint || c->graph_exact != c->exact ||
                        c->graph_version != c->params_version;
     if (stale) {
@@ -835,9 +932,6 @@ int sph_step(sph_ctx* c, float dt, int nsteps) {
         c->graph_exact = c->exact;
         c->graph_version = c->params_version;
     }
-    for (int k = 0; k < nsteps; ++k) CK(c, cudaGraphLaunch(c->graph, c->stream));
-    c->keys_cur = c->keys_a;
-    c->idx_cur = c->idx_a;
     return SPH_OK;
 }
 
@@ -845,8 +939,11 @@ int sph_step_eager(sph_ctx* c, float dt, int nsteps) {
     int rc = check_ctx(c);
     if (rc) return rc;
     if (nsteps < 0 || !std::isfinite(dt)) return set_err(c, SPH_EINVAL, "sph_step_eager: bad arguments");
-    for (int k = 0; k < nsteps && c->num_hint > 0; ++k)
+    for (int k = 0; k < nsteps; ++k) {
+        if (!c->hoses.empty() && (rc = sph_spray_hoses(c, nullptr))) return rc;
+        if (c->num_hint == 0) continue;
         if ((rc = enqueue_fused_step(c, dt))) return rc;
+    }
     return SPH_OK;
 }
 
@@ -857,6 +954,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         return set_err(c, SPH_EINVAL, "sph_step_profile: bad arguments");
     if (c->n_tri > 0)
         return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step; with a triangle mesh the step is staged");
+    if (!c->hoses.empty()) return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step without hoses");
     // Launches of one fused step: prologue, hash, sort reset, radix passes,
     // cells+permute, density, force+collision+leapfrog.
     const int nk = 6 + c->passes;

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include "sph_device.cuh"
 
@@ -52,6 +53,8 @@ struct sph_ctx {
     float4* tri = nullptr;
     int n_tri = 0;
     int tri_cap = 0;
+    // hoses (SPH::addHose), sprayed at the start of every update
+    std::vector<sph_hose*> hoses;
     // graph of one fused step
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.f;

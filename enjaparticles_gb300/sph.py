@@ -167,6 +167,26 @@ class SPH:
         kind = {"leapfrog": abi.SPH_INTEGRATOR_LEAPFROG, "euler": abi.SPH_INTEGRATOR_EULER}[name]
         self._ck(self.lib.sph_set_integrator(self.ctx, kind))
 
+    # -- hoses (SPH.cpp:523-558) ---------------------------------------------
+    def addHose(self, total_n, center, velocity, radius, dt):
+        """SPH::addHose: radius in particle spacings; returns the hose index."""
+        idx = C.c_int()
+        self._ck(self.lib.sph_add_hose(self.ctx, int(total_n), abi.vec4(center), abi.vec4(velocity), float(radius),
+                                       float(dt), C.byref(idx)))
+        return idx.value
+
+    def updateHose(self, index, center, velocity, radius):
+        self._ck(self.lib.sph_update_hose(self.ctx, int(index), abi.vec4(center), abi.vec4(velocity), float(radius)))
+
+    def refillHose(self, index, n):
+        self._ck(self.lib.sph_refill_hose(self.ctx, int(index), int(n)))
+
+    def sprayHoses(self):
+        """SPH::sprayHoses; returns the particles added."""
+        k = C.c_int()
+        self._ck(self.lib.sph_spray_hoses(self.ctx, C.byref(k)))
+        return k.value
+
     # -- whole steps --------------------------------------------------------
     def update(self):
         """SPH::update: hash ... collision."""
@@ -201,6 +221,51 @@ class SPH:
         self._ck(self.lib.sph_adjoint_backward(self.ctx, dpos, dvel, dveleval, out_pos, out_vel, out_veleval,
                                                C.byref(v)))
         return v.value
+
+
+class Hose:
+    """The reference's Hose (common/Hose.cpp) as a host object of the
+    library (sph_hose_*): spray() returns the (k, 4) positions one tick
+    emits and the velocity they are pushed with."""
+
+    def __init__(self, dt, total_n, center, velocity, radius, spacing):
+        self.lib = abi.load_library()
+        self.h = C.c_void_p()
+        abi.check(self.lib, None, self.lib.sph_hose_create(float(dt), int(total_n), abi.vec4(center),
+                                                           abi.vec4(velocity), float(radius), float(spacing),
+                                                           C.byref(self.h)))
+
+    def update(self, center, velocity, radius, spacing):
+        abi.check(self.lib, None, self.lib.sph_hose_update(self.h, abi.vec4(center), abi.vec4(velocity), float(radius),
+                                                           float(spacing)))
+
+    def refill(self, n):
+        abi.check(self.lib, None, self.lib.sph_hose_refill(self.h, int(n)))
+
+    def spray(self):
+        k = C.c_int()
+        abi.check(self.lib, None, self.lib.sph_hose_spray(self.h, C.byref(k)))
+        pos = np.zeros((k.value, 4), np.float32)
+        v = abi.sph_float4()
+        abi.check(self.lib, None, self.lib.sph_hose_particles(self.h, pos.ctypes.data if k.value else None, k.value,
+                                                              C.byref(v)))
+        return pos, np.array([v.x, v.y, v.z, v.w], np.float32)
+
+    def remaining(self):
+        n = C.c_int()
+        abi.check(self.lib, None, self.lib.sph_hose_remaining(self.h, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if self.h:
+            self.lib.sph_hose_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def dambreak_system(n, viscosity=0.01, max_num=None, exact=False, velocity_sigma=0.0, scene=0):

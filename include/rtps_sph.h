@@ -289,6 +289,49 @@ int sph_set_integrator(sph_ctx* ctx, int integrator);
 #define SPH_MAX_TRIANGLES (1 << 20)
 int sph_load_triangles(sph_ctx* ctx, const sph_float4* tris, int count);
 
+/* Hoses: a disc of new particles pushed into the system every few steps.
+ *
+ * sph_hose is the reference's Hose (common/Hose.cpp:30-130) on its own, a
+ * host object: total_n particles, emitted from a disc of the given radius
+ * around center, normal to velocity, on a jittered grid of the given
+ * spacing (addDiscRandom, domain/IV.cpp:313-367), every
+ * 1 + spacing/dt/|velocity|/10 sprays.  The jitter comes from the C
+ * library's rand(), as in the reference (seed it with srand).  A zero y or z
+ * velocity is replaced by 1e-7, as the reference does.  No GPU is involved. */
+typedef struct sph_hose sph_hose;
+int sph_hose_create(float dt, int total_n, sph_float4 center, sph_float4 velocity, float radius, float spacing,
+                    sph_hose** out);
+/* Hose::update and Hose::refill. */
+int sph_hose_update(sph_hose* hose, sph_float4 center, sph_float4 velocity, float radius, float spacing);
+int sph_hose_refill(sph_hose* hose, int n);
+/* Hose::spray: one tick of the emission clock; *count = the particles this
+ * tick emits (0 between emissions), kept until the next spray. */
+int sph_hose_spray(sph_hose* hose, int* count);
+/* The last spray's particles (at most cap) and the velocity they are pushed
+ * with (Hose::getVelocity). */
+int sph_hose_particles(const sph_hose* hose, sph_float4* pos, int cap, sph_float4* velocity);
+/* Particles left in the hose. */
+int sph_hose_remaining(const sph_hose* hose, int* n);
+void sph_hose_destroy(sph_hose* hose);
+
+/* SPH::addHose / updateHose / refillHose (SPH.cpp:523-545): hoses owned by
+ * the context.  radius is in particle spacings: it is multiplied by the
+ * "spacing" setting, rest_distance / simulation_scale.  dt is the time step
+ * the emission rate is computed for (the setting time_step). *index gets the
+ * hose's index. */
+int sph_add_hose(sph_ctx* ctx, int total_n, sph_float4 center, sph_float4 velocity, float radius, float dt,
+                 int* index);
+int sph_update_hose(sph_ctx* ctx, int index, sph_float4 center, sph_float4 velocity, float radius);
+int sph_refill_hose(sph_ctx* ctx, int index, int n);
+/* SPH::sprayHoses (SPH.cpp:547-558): every hose sprays once and what it
+ * emits is appended with sph_push_particles at the hose's velocity; a spray
+ * that would pass max_num is dropped, as SPH::pushParticles drops it
+ * (SPH.cpp:562-567).  sph_update, and sph_step and sph_step_eager before
+ * every step, call it first when the context has hoses, as SPH::updateGPU
+ * does (SPH.cpp:162-166).  *added (may be null) gets the particles added.
+ * Blocking when a hose emits. */
+int sph_spray_hoses(sph_ctx* ctx, int* added);
+
 /* SPH::update (SPH.cpp:117-125 -> updateGPU :149-300) with SPH::collision
  * (SPH.cpp:303-336) enabled after gravity: hash, sort, cellindices, permute,
  * out-of-grid deletion, density, force, point-source gravity, walls, and the

@@ -21,8 +21,9 @@ plain arithmetic, though, so this recipe compiles them for the host with g++:
      (work-groups run one at a time, so a static array is the group's local
      memory);
   3. compile them with clshim.hpp (vector types, built-ins, barrier) and the
-     ref_*.cpp drivers, plus the reference's host Domain.cpp / structs.cpp
-     unchanged, into oracle/_ref/librtps_ref.so.  -ffp-contract=off keeps
+     ref_*.cpp drivers, plus the reference's host Domain.cpp / IV.cpp /
+     structs.cpp unchanged (and its Hose.cpp, included unchanged by
+     ref_hose.cpp), into oracle/_ref/librtps_ref.so.  -ffp-contract=off keeps
      every multiply and add separately rounded, as written.
 
 The temporary copies are deleted; only the shared library is kept, under
@@ -48,7 +49,7 @@ SPH = ["density.cl", "force.cl", "collision_wall.cl", "collision_tri.cl", "leapf
        "cl_sph_structs.h", "cl_sph_collision.h", "cl_sph_macros.h"]
 DRIVERS = ["ref_runtime.cpp", "ref_hash.cpp", "ref_bitonic.cpp", "ref_cellindices.cpp", "ref_permute.cpp",
            "ref_density.cpp", "ref_force.cpp", "ref_collision.cpp", "ref_leapfrog.cpp", "ref_domain.cpp",
-           "ref_gravity.cpp", "ref_euler.cpp", "ref_collision_tri.cpp"]
+           "ref_gravity.cpp", "ref_euler.cpp", "ref_collision_tri.cpp", "ref_hose.cpp"]
 
 VEC_LITERAL = re.compile(r"\((float4|int4)\)\s*\(")
 LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
@@ -94,7 +95,8 @@ def build(reference, verbose=False):
         cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
                "-w", "-I", tmp, "-I", HERE, "-I", rtpslib]
         cmd += [os.path.join(HERE, d) for d in DRIVERS]
-        cmd += [os.path.join(rtpslib, "domain", "Domain.cpp"), os.path.join(rtpslib, "structs.cpp")]
+        cmd += [os.path.join(rtpslib, "domain", "Domain.cpp"), os.path.join(rtpslib, "domain", "IV.cpp"),
+                os.path.join(rtpslib, "structs.cpp")]
         cmd += ["-o", OUT_LIB]
         if verbose:
             print(" ".join(cmd))

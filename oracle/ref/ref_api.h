@@ -25,3 +25,12 @@ void ref_collision_triangles(int n, const float* pos_s, const float* vel_s, floa
 void ref_setup_domain(const float* bnd_min, const float* bnd_max, float cell_size, float sim_scale, void* grid,
                       void* grid_scaled);
 }
+
+// Hose (rtpslib/system/common/Hose.cpp): create, spray, update, refill.
+extern "C" void* ref_hose_create(float dt, int total_n, const float* center, const float* velocity, float radius,
+                                 float spacing);
+extern "C" int ref_hose_spray(void* h, float* out, int cap, float* velocity);
+extern "C" void ref_hose_update(void* h, const float* center, const float* velocity, float radius, float spacing);
+extern "C" void ref_hose_refill(void* h, int n);
+extern "C" void ref_hose_destroy(void* h);
+extern "C" void ref_srand(unsigned seed);

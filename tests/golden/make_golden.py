@@ -23,6 +23,9 @@ Fixtures
                      mesh of scenes.ramp_and_box_mesh (collision_tri.cl after
                      the walls): step 1 forces before and after the triangle
                      stage, state after 1, 5 and 20 steps
+  hose_sprays.npz    the reference's Hose (common/Hose.cpp, addDiscRandom)
+                     through the scripts of tests/hose_cases.py, rand()
+                     seeded per script: counts, positions, push velocities
 Usage: python tests/golden/make_golden.py [--only NAME ...]
 """
 import ctypes as C
@@ -170,6 +173,15 @@ def triangles_fixture():
     return out
 
 
+def hose_fixture():
+    import hose_cases
+    out = {}
+    for name in hose_cases.SCRIPTS:
+        counts, pos, vel = hose_cases.run_script(name, hose_cases.RefHose)
+        out.update({name + "_counts": counts, name + "_pos": pos, name + "_vel": vel})
+    return out
+
+
 FIXTURES = {
     "stages_n4096.npz": lambda: stages_fixture(4096, 0.1),
     "ragged_n1000.npz": lambda: stages_fixture(1000, 0.1, steps_after=(3,)),
@@ -177,6 +189,7 @@ FIXTURES = {
     "cfg0_n16384.npz": cfg0_fixture,
     "gravity_n2048.npz": gravity_fixture,
     "triangles_n2048.npz": triangles_fixture,
+    "hose_sprays.npz": hose_fixture,
 }
 
 

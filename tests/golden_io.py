@@ -9,6 +9,10 @@ from enjaparticles_gb300 import abi
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+def path(name):
+    return os.path.join(GOLDEN, name)
+
+
 def load(name):
     z = np.load(os.path.join(GOLDEN, name))
     d = {k: z[k] for k in z.files}

@@ -99,6 +99,12 @@ def ref():
             "ref_gravity": (None, [_I, _I, _P, _P, _P, _P, _P, _F]),
             "ref_euler": (None, [_I, _P, _P, _P, _P, _P, _P, _P, _F]),
             "ref_collision_triangles": (None, [_I, _P, _P, _P, _P, _I, _P, _F]),
+            "ref_hose_create": (_P, [_F, _I, _P, _P, _F, _F]),
+            "ref_hose_spray": (_I, [_P, _P, _I, _P]),
+            "ref_hose_update": (None, [_P, _P, _P, _F, _F]),
+            "ref_hose_refill": (None, [_P, _I]),
+            "ref_hose_destroy": (None, [_P]),
+            "ref_srand": (None, [C.c_uint]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
