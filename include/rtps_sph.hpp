@@ -137,6 +137,24 @@ public:
         check(sph_load_triangles(ctx_, triangles.empty() ? nullptr : &triangles[0].verts[0],
                                  (int)triangles.size()));
     }
+    // SPH::addHose / updateHose / refillHose (SPH.cpp:523-545): radius in
+    // particle spacings; update() sprays the hoses first.  color and mass are
+    // accepted for interface parity and unused.
+    int addHose(int total_n, float4 center, float4 velocity, float radius, float4 color = make_float4(1, 0, 0, 1),
+                float mass = 0.0f) {
+        (void)color;
+        (void)mass;
+        int index = -1;
+        check(sph_add_hose(ctx_, total_n, center, velocity, radius, dt_, &index));
+        return index;
+    }
+    void updateHose(int index, float4 center, float4 velocity, float radius,
+                    float4 color = make_float4(1, 0, 0, 1)) {
+        (void)color;
+        check(sph_update_hose(ctx_, index, center, velocity, radius));
+    }
+    void refillHose(int index, int refill) { check(sph_refill_hose(ctx_, index, refill)); }
+    void sprayHoses() { check(sph_spray_hoses(ctx_, nullptr)); }
     std::vector<float4> getDeletedPos() { return deleted(true); }
     std::vector<float4> getDeletedVel() { return deleted(false); }
 
