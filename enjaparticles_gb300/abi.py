@@ -114,6 +114,12 @@ SIGNATURES = {
     "sph_update_hose": (_I, [_P, _I, sph_float4, sph_float4, _F]),
     "sph_refill_hose": (_I, [_P, _I, _I]),
     "sph_spray_hoses": (_I, [_P, C.POINTER(_I)]),
+    "sph_colorfield": (_I, [_P, _I]),
+    "sph_marching_cubes": (_I, [_P, _P, _I, _F, C.POINTER(_I)]),
+    "sph_post_process": (_I, [_P, _I, C.POINTER(_I)]),
+    "sph_get_surface": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_I), C.POINTER(_I)]),
+    "sph_download_surface": (_I, [_P, _P, _P, _P, _I]),
+    "sph_mc_case_table": (_I, [_P, _P, C.POINTER(_I)]),
     "sph_adjoint_backward": (_I, [_P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
     "sph_adjoint_rollout": (_I, [_P, _I, _I, _P, _P, C.POINTER(_F)]),
     "sph_batch_create": (_I, [_I, _P, _P, _P, _P, C.POINTER(_P)]),

@@ -55,6 +55,18 @@ struct sph_ctx {
     int tri_cap = 0;
     // hoses (SPH::addHose), sprayed at the start of every update
     std::vector<sph_hose*> hoses;
+    // surface (sph_surface.cu): colour field, marching-cubes scan scratch, the
+    // case table on the device, the mesh (vertices, then normals)
+    float* cf = nullptr;
+    size_t cf_cap = 0;
+    int cf_res = 0;
+    unsigned* mc_scan = nullptr;
+    size_t mc_scan_cap = 0;
+    signed char* mc_table = nullptr;
+    float* mesh = nullptr;
+    size_t mesh_cap = 0;
+    int mesh_tri = 0;
+    int mesh_res = 0;
     // graph of one fused step
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.f;

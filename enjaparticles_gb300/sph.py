@@ -187,6 +187,35 @@ class SPH:
         self._ck(self.lib.sph_spray_hoses(self.ctx, C.byref(k)))
         return k.value
 
+    # -- post-process: colour field and surface (SPH.cpp:338-386) -------------
+    def colorfield(self, res):
+        """The res^3 colour field of the last update, as a numpy array [r, t, s]."""
+        self._ck(self.lib.sph_colorfield(self.ctx, int(res)))
+        res = max(int(res), 2)
+        out = np.empty(res ** 3, np.float32)
+        self._ck(self.lib.sph_download_surface(self.ctx, out.ctypes.data, None, None, 0))
+        return out.reshape(res, res, res)
+
+    def marchingCubes(self, res, isolevel=0.0001, field_ptr=None):
+        """Marching cubes on the context's colour field (or a device field);
+        returns (vertices, normals) as (ntri, 3, 3) arrays."""
+        n = C.c_int()
+        self._ck(self.lib.sph_marching_cubes(self.ctx, field_ptr, int(res), float(isolevel), C.byref(n)))
+        return self._mesh(n.value)
+
+    def postProcess(self, res):
+        """SPH::postProcess: colour field + marching cubes (isolevel 0.0001)."""
+        n = C.c_int()
+        self._ck(self.lib.sph_post_process(self.ctx, int(res), C.byref(n)))
+        return self._mesh(n.value)
+
+    def _mesh(self, n):
+        v = np.empty((n, 3, 3), np.float32)
+        nr = np.empty((n, 3, 3), np.float32)
+        if n:
+            self._ck(self.lib.sph_download_surface(self.ctx, None, v.ctypes.data, nr.ctypes.data, n))
+        return v, nr
+
     # -- whole steps --------------------------------------------------------
     def update(self):
         """SPH::update: hash ... collision."""

@@ -332,6 +332,43 @@ int sph_refill_hose(sph_ctx* ctx, int index, int n);
  * Blocking when a hose emits. */
 int sph_spray_hoses(sph_ctx* ctx, int* added);
 
+/* SPH::postProcess (SPH.cpp:338-386), headless: the colour field and its
+ * marching-cubes surface, kept in device buffers owned by the context.
+ *
+ * sph_colorfield: ColorField::execute (sph/ColorField.cpp:84-121;
+ * colorfield.cl): res^3 samples spanning the scaled grid's bounds, sample
+ * (s, t, r) at index s + t*res + r*res^2, value mass * sum over particles within
+ * h of Wspiky(max(|r|, EPSILON)) / rho_j, from the sorted state of the last
+ * update.  res below 2 becomes 2; at most 512.  Asynchronous. */
+int sph_colorfield(sph_ctx* ctx, int res);
+/* MarchingCubes::execute (common/MarchingCubes.cpp:166-370; classifycubes.cl,
+ * constructhp.cl, traversehp.cl) on a res^3 field: the device array `field`
+ * (s + t*res + r*res^2 order), or the context's colour field when field is
+ * null.  Writes the context's mesh: *ntri triangles, 9 floats each for the
+ * vertices (grid position / (res - 1) * 10, the reference's render box) and
+ * 9 for the vertex normals, in the reference's cube order.  The per-case
+ * triangulation is sph_mc_case_table's: per cube the triangle count and the
+ * vertices equal the reference's; which diagonal splits a quad can differ.
+ * Blocking (reads the count). */
+int sph_marching_cubes(sph_ctx* ctx, const float* field, int res, float isolevel, int* ntri);
+/* Colour field + marching cubes at the reference's isolevel 0.0001;
+ * nothing (0 triangles) without particles. */
+int sph_post_process(sph_ctx* ctx, int res, int* ntri);
+/* Device views of the colour field (res^3 floats), the mesh vertices and
+ * normals (ntri*9 floats each); valid until the next surface call. */
+int sph_get_surface(sph_ctx* ctx, const float** field, const float** vertices, const float** normals, int* res,
+                    int* ntri);
+/* Host copies of the field (res^3 floats) and of at most cap_tri triangles'
+ * vertices and normals; any pointer may be null.  Blocking. */
+int sph_download_surface(sph_ctx* ctx, float* field, float* vertices, float* normals, int cap_tri);
+/* The marching-cubes case table, no reference counterpart (the reference
+ * uses a published table): for case c (bit k set when corner k is above the
+ * isolevel, corners in the reference's order), count[c] triangles given by
+ * tri[c*18 .. c*18+3*count[c]-1] as local edge numbers (the reference's edge
+ * list); *max_triangles gets the largest count.  Host only. */
+#define SPH_MC_CASE_EDGES 18
+int sph_mc_case_table(signed char* tri, unsigned char* count, int* max_triangles);
+
 /* SPH::update (SPH.cpp:117-125 -> updateGPU :149-300) with SPH::collision
  * (SPH.cpp:303-336) enabled after gravity: hash, sort, cellindices, permute,
  * out-of-grid deletion, density, force, point-source gravity, walls, and the

@@ -81,13 +81,35 @@ public:
     }
     SPH(const SPH&) = delete;
     SPH& operator=(const SPH&) = delete;
-    SPH(SPH&& o) noexcept : ctx_(o.ctx_), max_num_(o.max_num_), dt_(o.dt_) { o.ctx_ = nullptr; }
+    SPH(SPH&& o) noexcept
+        : ctx_(o.ctx_),
+          max_num_(o.max_num_),
+          dt_(o.dt_),
+          color_field_(o.color_field_),
+          color_field_res_(o.color_field_res_) {
+        o.ctx_ = nullptr;
+    }
 
     // --- System virtual API (System.h:64-75) ---
     void update() { check(sph_update(ctx_)); }           // hash .. density, force, walls, mesh (SPH::updateGPU)
     void interact() {}                                    // no coupled systems
     void integrate() { check(sph_integrate(ctx_, dt_)); } // leapfrog (SPH::integrate)
-    void postProcess() {}
+    // SPH::postProcess (SPH.cpp:338-386) with the settings use_color_field /
+    // color_field_res set by useColorField: the colour field and its mesh,
+    // kept on the device (getMesh gives views of them).
+    void postProcess() {
+        if (color_field_) check(sph_post_process(ctx_, color_field_res_, nullptr));
+    }
+    void useColorField(bool on, int res = 2) {
+        color_field_ = on;
+        color_field_res_ = res;
+    }
+    // Device views of the last mesh: ntri triangles, 9 floats each.
+    int getMesh(const float** vertices, const float** normals) {
+        int ntri = 0;
+        check(sph_get_surface(ctx_, nullptr, vertices, normals, nullptr, &ntri));
+        return ntri;
+    }
     // update + integrate fused, nsteps times, replayed from a CUDA graph
     void step(int nsteps = 1) { check(sph_step(ctx_, dt_, nsteps)); }
 
@@ -207,6 +229,8 @@ private:
     sph_ctx* ctx_ = nullptr;
     int max_num_ = 0;
     float dt_ = 0.001f;
+    bool color_field_ = false;
+    int color_field_res_ = 2;
 };
 
 }  // namespace rtps

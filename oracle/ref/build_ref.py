@@ -11,7 +11,8 @@ plain arithmetic, though, so this recipe compiles them for the host with g++:
      temporary directory laid out as the reference's build lays them out
      (cl_common/, cl_sph/; rtpslib/system/sph/CMakeLists.txt:3-11);
   2. rewrite four pieces of OpenCL-only syntax there, nothing else:
-       `(float4)(a, b, c, d)` / `(int4)(...)`  ->  `make_float4(...)` / `make_int4(...)`
+       `(float4)(a, b, c, d)` / `(int4)(...)` / `(float3)(...)` / `(int2)(...)`
+           ->  `make_float4(...)` / `make_int4(...)` / `make_float3(...)` / `make_int2(...)`
        kernel-scope `__local T name[N];` arrays  ->  `static T name[N];`
        the identity swizzle `v.xyzw`  ->  `v`
        the implicit Triangle* -> float* argument conversion of one call in
@@ -44,14 +45,15 @@ OUT_DIR = os.path.join(ORACLE, "_ref")
 OUT_LIB = os.path.join(OUT_DIR, "librtps_ref.so")
 
 COMMON = ["hash.cl", "cl_hash.h", "cl_structs.h", "cl_macros.h", "cellindices.cl", "permute.cl", "bitonic.cl",
-          "gravity.cl"]
-SPH = ["density.cl", "force.cl", "collision_wall.cl", "collision_tri.cl", "leapfrog.cl", "euler.cl", "cl_sph_kernels.h", "cl_sph_neighbors.h",
-       "cl_sph_structs.h", "cl_sph_collision.h", "cl_sph_macros.h"]
+          "gravity.cl", "indexmap.h", "classifycubes.cl", "constructhp.cl", "traversehp.cl"]
+SPH = ["density.cl", "force.cl", "collision_wall.cl", "collision_tri.cl", "leapfrog.cl", "euler.cl", "colorfield.cl",
+       "cl_sph_kernels.h", "cl_sph_neighbors.h", "cl_sph_structs.h", "cl_sph_collision.h", "cl_sph_macros.h"]
 DRIVERS = ["ref_runtime.cpp", "ref_hash.cpp", "ref_bitonic.cpp", "ref_cellindices.cpp", "ref_permute.cpp",
            "ref_density.cpp", "ref_force.cpp", "ref_collision.cpp", "ref_leapfrog.cpp", "ref_domain.cpp",
-           "ref_gravity.cpp", "ref_euler.cpp", "ref_collision_tri.cpp", "ref_hose.cpp"]
+           "ref_gravity.cpp", "ref_euler.cpp", "ref_collision_tri.cpp", "ref_hose.cpp",
+           "ref_colorfield.cpp", "ref_marching_cubes.cpp"]
 
-VEC_LITERAL = re.compile(r"\((float4|int4)\)\s*\(")
+VEC_LITERAL = re.compile(r"\((float4|int4|float3|int2)\)\s*\(")
 LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
 IDENTITY_SWIZZLE = re.compile(r"\.xyzw\b")
 # collision_tri.cl passes its Triangle arrays where float* is declared; C

@@ -34,3 +34,14 @@ extern "C" void ref_hose_update(void* h, const float* center, const float* veloc
 extern "C" void ref_hose_refill(void* h, int n);
 extern "C" void ref_hose_destroy(void* h);
 extern "C" void ref_srand(unsigned seed);
+
+// Colour field (sph/cl_src/colorfield.cl) and its image tiling.
+extern "C" int ref_colorfield_slices(int res);
+extern "C" int ref_colorfield(int res, int n, const float* pos_s, const float* density, const unsigned* cell_start,
+                              const unsigned* cell_end, const void* grid_scaled, const void* sphp, float* field,
+                              float* image);
+
+// Marching cubes (common/cl_src/classifycubes.cl, constructhp.cl, traversehp.cl)
+// on a res^3 field in (s + t res + r res^2) order; returns the triangle count.
+extern "C" int ref_marching_cubes(int res, const float* field, float isolevel, float* tris, float* normals,
+                                  int cap_tri, float* base_level);

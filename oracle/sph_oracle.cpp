@@ -359,6 +359,16 @@ void oracle_collision_triangles(int f64, int n, const float* pos_s, const float*
             collision_tri_one<float>(i, pos_s, vel_s, force, tris, ntri, *sp);
     }
 }
+void oracle_colorfield(int f64, int res, const float* pos_s, const float* density, const uint32_t* start,
+                       const uint32_t* end, const GridParams* gps, const SPHParams* sp, float* field) {
+    const long total = (long)res * res * res;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < total; ++k) {
+        const int s = (int)(k % res), t = (int)((k / res) % res), r = (int)(k / ((long)res * res));
+        field[k] = f64 ? colorfield_one<double>(s, t, r, res, pos_s, density, start, end, *gps, *sp)
+                       : colorfield_one<float>(s, t, r, res, pos_s, density, start, end, *gps, *sp);
+    }
+}
 void oracle_euler(int f64, int n, const float* pos_s, const float* vel_s, const float* force, const uint32_t* idx,
                   const SPHParams* sp, float dt, float* pos_u, float* vel_u) {
 #pragma omp parallel for schedule(static)

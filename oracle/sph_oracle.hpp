@@ -418,4 +418,42 @@ inline void collision_tri_one(int i, const float* pos_s, const float* vel_s, flo
     store4(force + 4 * (size_t)i, add(f0, rf));
 }
 
+// Colour field, colorfield_update (sph/cl_src/colorfield.cl:66-103; Wspiky
+// cl_sph_kernels.h:71-78), as ColorField::execute runs it over res^3 sample
+// points (sph/ColorField.cpp:84-121) with the scaled grid.  Sample (s, t, r)
+// sits at (s, t, r) / (res - 1) of the way from bnd_min to bnd_max; its value
+// is mass * sum over the particles within h (27-cell walk, as density) of
+// Wspiky(max(|r|, EPSILON)) / rho_j.  The kernel forms 1/rho_j and the product
+// in double (1.0 is a double literal) and rounds the product to float.
+template <class T>
+inline T wspiky(T rlen, T h) {
+    const T h6 = h * h * h * h * h * h;
+    const T alpha = (T)15.f / (T)3.14159265358979323846f / h6;
+    const T hr2 = h - rlen;
+    return alpha * hr2 * hr2 * hr2;
+}
+template <class T>
+inline float colorfield_one(int s, int t, int r, int res, const float* pos_s, const float* density,
+                            const uint32_t* start, const uint32_t* end, const GridParams& gps, const SPHParams& sp) {
+    const float tmp = 1.0f / (float)(unsigned)(res - 1);
+    const float fx = (float)(unsigned)s * tmp, fy = (float)(unsigned)t * tmp, fz = (float)(unsigned)r * tmp;
+    V4<T> p{(T)fx * ((T)gps.bnd_max.x - (T)gps.bnd_min.x) + (T)gps.bnd_min.x,
+            (T)fy * ((T)gps.bnd_max.y - (T)gps.bnd_min.y) + (T)gps.bnd_min.y,
+            (T)fz * ((T)gps.bnd_max.z - (T)gps.bnd_min.z) + (T)gps.bnd_min.z, (T)1};
+    const T sc = (T)sp.simulation_scale, h = (T)sp.smoothing_distance, eps = (T)sp.EPSILON;
+    T acc = 0;
+    for_each_candidate(p, gps, start, end, [&](uint32_t j) {
+        V4<T> pj = mul(load4<T>(pos_s + 4 * (size_t)j), sc);
+        V4<T> d = sub(p, pj);
+        d.w = 0;
+        T rlen = length4(d);
+        if (rlen <= h) {
+            rlen = rlen < eps ? eps : rlen;
+            const T kern = (T)((double)wspiky(rlen, h) * (1.0 / (double)density[j]));
+            acc += kern;
+        }
+    });
+    return (float)(acc * (T)sp.mass);
+}
+
 }  // namespace sph_oracle

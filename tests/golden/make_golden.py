@@ -23,6 +23,10 @@ Fixtures
                      mesh of scenes.ramp_and_box_mesh (collision_tri.cl after
                      the walls): step 1 forces before and after the triangle
                      stage, state after 1, 5 and 20 steps
+  surface_n4096.npz  N=4096, v0 ~ N(0, 0.2^2), after 20 steps: the reference's
+                     colour field (colorfield.cl) at res 16 and 32 and its
+                     marching-cubes mesh (classifycubes/constructhp/
+                     traversehp.cl) at isolevel 0.0001
   hose_sprays.npz    the reference's Hose (common/Hose.cpp, addDiscRandom)
                      through the scripts of tests/hose_cases.py, rand()
                      seeded per script: counts, positions, push velocities
@@ -173,6 +177,37 @@ def triangles_fixture():
     return out
 
 
+def surface_fixture():
+    import ctypes as C
+    n, steps = 4096, 20
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n, velocity_sigma=0.2)
+    R = ref_driver.RefSystem(sp, g, gs, n)
+    R.upload(pos, vel)
+    R.step(DT, steps)
+    out = dict(params_blob(sp, g, gs))
+    out.update({"in_pos": pos, "in_vel": vel, "dt": np.float32(DT), "steps": np.int32(steps)})
+    L = R.lib
+    P = lambda a: a.ctypes.data
+    spn = R.sp
+    spn.num = R.num
+    for res in (16, 32):
+        field = np.zeros(res ** 3, np.float32)
+        L.ref_colorfield(res, R.num, P(R.pos_s), P(R.density_s), P(R.start), P(R.end), C.addressof(gs),
+                         C.addressof(spn), P(field), None)
+        cap = 200000
+        v = np.zeros((cap, 9), np.float32)
+        nr = np.zeros((cap, 9), np.float32)
+        L.ref_marching_cubes.restype = C.c_int
+        L.ref_marching_cubes.argtypes = [C.c_int, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_int,
+                                         C.c_void_p]
+        tot = L.ref_marching_cubes(res, P(field), 0.0001, P(v), P(nr), cap, None)
+        out["field%d" % res] = field
+        out["mesh%d_vertices" % res] = v[:tot].reshape(-1, 3, 3).copy()
+        out["mesh%d_normals" % res] = nr[:tot].reshape(-1, 3, 3).copy()
+    return out
+
+
 def hose_fixture():
     import hose_cases
     out = {}
@@ -190,6 +225,7 @@ FIXTURES = {
     "gravity_n2048.npz": gravity_fixture,
     "triangles_n2048.npz": triangles_fixture,
     "hose_sprays.npz": hose_fixture,
+    "surface_n4096.npz": surface_fixture,
 }
 
 

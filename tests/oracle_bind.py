@@ -65,6 +65,7 @@ def oracle():
             "oracle_sim_set_integrator": (None, [_P, _I]),
             "oracle_collision_triangles": (None, [_I, _I, _P, _P, _P, _P, _I, _P]),
             "oracle_sim_set_triangles": (None, [_P, _P, _I]),
+            "oracle_colorfield": (None, [_I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_rollout64": (_I, [_P, _P, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_rollout64_jvp": (_I, [_P, _P, C.c_double, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P,
                                           _P, _P, _P]),
@@ -105,6 +106,9 @@ def ref():
             "ref_hose_refill": (None, [_P, _I]),
             "ref_hose_destroy": (None, [_P]),
             "ref_srand": (None, [C.c_uint]),
+            "ref_colorfield_slices": (_I, [_I]),
+            "ref_colorfield": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+            "ref_marching_cubes": (_I, [_I, _P, _F, _P, _P, _I, _P]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)

@@ -201,3 +201,32 @@ def test_oracle_triangle_mesh_rollout_matches_reference_golden():
         done = k
         for f in ("pos_u", "vel_u", "veleval_u"):
             np.testing.assert_array_equal(sim.get(f), d["s%d_%s" % (k, f)], err_msg="step %d %s" % (k, f))
+
+
+def _sorted_state(n=4096, steps=3):
+    """pos_s, density_s, cell_start, cell_end of a dam break after `steps`
+    oracle steps and one more update."""
+    from enjaparticles_gb300 import abi, scenes
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n, velocity_sigma=0.2)
+    sim = ob.OracleSim(sp, g, gs, n)
+    sim.upload(pos, vel)
+    sim.step(0.001, steps)
+    sim.update()
+    return (sp, g, gs, sim.num, sim.get("pos_s"), sim.get("density_s"), sim.get("cell_start", g.nb_cells + 1),
+            sim.get("cell_end", g.nb_cells + 1))
+
+
+@pytest.mark.skipif(not ob.ref_available(), reason="reference kernels not built here (needs the reference tree)")
+@pytest.mark.parametrize("res", [2, 7, 16, 32])
+def test_oracle_colorfield_equals_reference_kernel(res):
+    """colorfield_update (colorfield.cl) at res^3 sample points over the
+    scaled grid bounds: the oracle equals the reference's kernel bit for bit."""
+    sp, g, gs, n, ps, dens, cs, ce = _sorted_state()
+    R, O = ob.ref(), ob.oracle()
+    want = np.zeros(res ** 3, np.float32)
+    R.ref_colorfield(res, n, P(ps), P(dens), P(cs), P(ce), C.addressof(gs), C.addressof(sp), P(want), None)
+    got = np.zeros(res ** 3, np.float32)
+    O.oracle_colorfield(0, res, P(ps), P(dens), P(cs), P(ce), C.addressof(gs), C.addressof(sp), P(got))
+    assert (want > 0).sum() > res ** 3 // 20
+    np.testing.assert_array_equal(got, want)
