@@ -19,6 +19,8 @@ synthetic dam-break lattice (no dataset exists for it).
          host cores for a bounded sample.
   triangles  the same dam break with a 524-triangle mesh (collision_tri.cl
          after the walls): step time and the triangle stage's roofline.
+  surface  SPH::postProcess on the 2M state: colour field and marching
+         cubes at res 64 and 128.
 
 `--impl reference` times the reference's CPU implementation instead: the
 reference's OpenCL kernels cannot run on these machines (no OpenCL driver),
@@ -73,6 +75,7 @@ def parse():
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-k", type=int, default=20)
     ap.add_argument("--no-triangles", action="store_true")
+    ap.add_argument("--no-surface", action="store_true")
     ap.add_argument("--tri-steps", type=int, default=0, help="0: same as --steps")
     return ap.parse_args()
 
@@ -429,6 +432,54 @@ def bench_triangles(args, torch, peak):
                                "unit": "GB/s", "frac": achieved / peak}}
 
 
+def bench_surface(args, torch, peak):
+    """SPH::postProcess on the 2M dam break after args.warmup + 100 steps:
+    the colour field (res^3 samples, 27-cell walk) and marching cubes at
+    isolevel 0.0001, at res 64 (the largest the reference's tiled image
+    holds) and 128.  Device time per call (CUDA events, mean of 10), split
+    into the colour field and the marching cubes (count, scan, emit; the
+    count read back to the host in between).  Marching-cubes bytes: the field
+    read by both passes plus the mesh written (72 B per triangle)."""
+    from enjaparticles_gb300 import abi, scenes
+    from enjaparticles_gb300.sph import SPH
+    import ctypes as C
+    n = args.n
+    sp, g, gs = abi.dambreak_params(n)
+    pos0, vel0 = scenes.dambreak(n)
+    s = SPH(sp, g, n, gs)
+    stream = torch.cuda.current_stream()
+    abi.check(s.lib, s.ctx, s.lib.sph_set_stream(s.ctx, C.c_void_p(stream.cuda_stream)))
+    s.upload(pos0, vel0)
+    s.step(DT, args.warmup + 100)
+    s.sync()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    out = {}
+    for res in (64, 128):
+        ntri = C.c_int()
+        abi.check(s.lib, s.ctx, s.lib.sph_post_process(s.ctx, res, C.byref(ntri)))
+        t_cf = t_mc = 0.0
+        reps = 10
+        for _ in range(reps):
+            e0.record(stream)
+            abi.check(s.lib, s.ctx, s.lib.sph_colorfield(s.ctx, res))
+            e1.record(stream)
+            abi.check(s.lib, s.ctx, s.lib.sph_marching_cubes(s.ctx, None, res, 0.0001, C.byref(ntri)))
+            e2.record(stream)
+            e2.synchronize()
+            t_cf += e0.elapsed_time(e1) / reps
+            t_mc += e1.elapsed_time(e2) / reps
+        mc_bytes = 2 * 4 * res ** 3 + 72 * ntri.value
+        out["res%d" % res] = {"triangles": ntri.value, "colorfield_ms": t_cf, "marching_cubes_ms": t_mc,
+                              "samples_per_s": res ** 3 / (t_cf / 1e3),
+                              "mc_roofline": {"bound": "hbm", "algorithmic_bytes": mc_bytes,
+                                              "achieved": mc_bytes / (t_mc / 1e3) / 1e9, "peak": peak,
+                                              "unit": "GB/s", "frac": mc_bytes / (t_mc / 1e3) / 1e9 / peak}}
+    s.close()
+    out["particles"] = n
+    out["state_after_steps"] = args.warmup + 100
+    return out
+
+
 def config_block(n, c):
     return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001, "
                         "1000-step rollout config" % n,
@@ -561,6 +612,8 @@ def main():
         line["adjoint"] = bench_adjoint(args, torch)
     if rank == 0 and not args.no_triangles:
         line["triangles"] = bench_triangles(args, torch, peak)
+    if rank == 0 and not args.no_surface:
+        line["surface"] = bench_surface(args, torch, peak)
     if rank == 0 and not args.no_calibration:
         line["calibration"] = bench_calibration(args, torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
