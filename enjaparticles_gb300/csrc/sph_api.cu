@@ -233,8 +233,8 @@ void free_all(sph_ctx* c) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
                     c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
-                    c->cell_start, c->cell_end, c->info, c->scratch, c->grav, c->tri, c->cf, c->mc_scan,
-                    c->mc_table, c->mesh};
+                    c->cell_start, c->cell_end, c->info, c->scratch, c->grav, c->tri, c->cf, c->cf_inv,
+                    c->mc_scan, c->mc_table, c->mesh};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);

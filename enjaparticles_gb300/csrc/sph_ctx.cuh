@@ -59,6 +59,8 @@ struct sph_ctx {
     // case table on the device, the mesh (vertices, then normals)
     float* cf = nullptr;
     size_t cf_cap = 0;
+    double* cf_inv = nullptr;  // 1/rho per sorted particle, in double
+    size_t cf_inv_cap = 0;
     int cf_res = 0;
     unsigned* mc_scan = nullptr;
     size_t mc_scan_cap = 0;

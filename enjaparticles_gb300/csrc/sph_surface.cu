@@ -7,9 +7,10 @@
 // Colour field.  One thread per sample point of a res^3 lattice spanning the
 // scaled grid's bounds; the 27-cell walk of the density pass; per particle
 // within h, Wspiky(max(|r|, EPSILON)) / rho_j, the reciprocal and product in
-// double as the reference's double literal makes them; times mass.  Every
-// operation is the reference's, explicitly rounded: the field equals the
-// oracle's bit for bit.  It is stored linearly (s + t res + r res^2) where the
+// double as the reference's double literal makes them; times mass.  In exact
+// mode every operation is the reference's, explicitly rounded: the field
+// equals the oracle's bit for bit; the default mode forms the product in
+// float.  It is stored linearly (s + t res + r res^2) where the
 // reference tiles z slices into a 2-D image; the reference's tiling holds
 // all slices only up to res = 64.
 //
@@ -42,6 +43,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <numeric>
 #include <vector>
 
 #include "sph_ctx.cuh"
@@ -189,13 +191,38 @@ __device__ __forceinline__ float wspiky_f(float alpha, float h, float rlen) {
     return __fmul_rn(__fmul_rn(__fmul_rn(alpha, hr), hr), hr);
 }
 
+// 1/rho_j in double, once per particle: the value the reference's
+// (1.0 / density[j]) forms for every pair.
+__global__ void __launch_bounds__(kSurfThreads) k_inv_density(const float* __restrict__ density, int n,
+                                                              double* __restrict__ inv) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) inv[j] = __ddiv_rn(1.0, (double)__ldg(density + j));
+}
+
+// Work split: warps take 32 consecutive samples (one row piece, so their
+// neighbour runs mostly coincide), but chunk c goes to warp (c * stride) mod
+// chunks with stride coprime to the chunk count, so that every block mixes
+// chunks from the whole lattice: samples inside the fluid, which carry all
+// the work, would otherwise sit in a few blocks.
+//
+// The cutoff |r| <= h is tested as r^2 <= rcut2 (the same test, as in the
+// density pass); the square root is taken for neighbours only.  Exact: the
+// reference's double product W * (1/rho_j), rounded to float, with 1/rho_j
+// from k_inv_density (the double pipe bounds this mode).  Default: the
+// product in float with the float 1/rho_j the density pass stored in
+// rec_vi.w, within a few ulps of the exact term.
+template <bool Exact>
 __global__ void __launch_bounds__(kSurfThreads) k_colorfield(float* __restrict__ field, int res,
+                                                             unsigned long long chunks, unsigned long long stride,
                                                              const float4* __restrict__ pos_s,
-                                                             const float* __restrict__ density,
+                                                             const double* __restrict__ inv_rho,
+                                                             const float4* __restrict__ rec_vi,
                                                              const uint32_t* __restrict__ cs,
                                                              const uint32_t* __restrict__ ce, const StepParams P) {
     const long long total = (long long)res * res * res;
-    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned long long gw = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= chunks) return;
+    const long long k = (long long)(((gw * stride) % chunks) * 32ull + (threadIdx.x & 31));
     if (k >= total) return;
     const int s = (int)(k % res), t = (int)((k / res) % res), r = (int)(k / ((long long)res * res));
     const float tmp = __fdiv_rn(1.0f, (float)(unsigned)(res - 1));
@@ -213,11 +240,15 @@ __global__ void __launch_bounds__(kSurfThreads) k_colorfield(float* __restrict__
         for (uint32_t j = rs; j < re; ++j) {
             float4 q = __ldg(pos_s + j);
             if (!P.unit_scale) q = v4scale(q, P.sc);
-            float rlen = __fsqrt_rn(dist2_exact(__fsub_rn(px, q.x), __fsub_rn(py, q.y), __fsub_rn(pz, q.z)));
-            if (rlen <= h) {
+            const float r2 = dist2_exact(__fsub_rn(px, q.x), __fsub_rn(py, q.y), __fsub_rn(pz, q.z));
+            if (r2 <= P.rcut2) {
+                float rlen = __fsqrt_rn(r2);
                 rlen = rlen < eps ? eps : rlen;
-                const double inv = __ddiv_rn(1.0, (double)__ldg(density + j));
-                acc = __fadd_rn(acc, __double2float_rn(__dmul_rn((double)wspiky_f(alpha, h, rlen), inv)));
+                const float w = wspiky_f(alpha, h, rlen);
+                if (Exact)
+                    acc = __fadd_rn(acc, __double2float_rn(__dmul_rn((double)w, __ldg(inv_rho + j))));
+                else
+                    acc = __fadd_rn(acc, __fmul_rn(w, __ldg(&rec_vi[j].w)));
             }
         }
     });
@@ -452,8 +483,24 @@ int sph_colorfield(sph_ctx* c, int res) {
     if (res > kMaxSurfaceRes) return set_err(c, SPH_EINVAL, "sph_colorfield: res %d above %d", res, kMaxSurfaceRes);
     const size_t n = (size_t)res * res * res;
     if ((rc = grow(c, c->cf, c->cf_cap, n))) return rc;
-    sphk::k_colorfield<<<(unsigned)((n + sphk::kSurfThreads - 1) / sphk::kSurfThreads), sphk::kSurfThreads, 0,
-                         c->stream>>>(c->cf, res, c->pos_s, c->density, c->cell_start, c->cell_end, c->P);
+    if (c->exact) {
+        if ((rc = grow(c, c->cf_inv, c->cf_inv_cap, (size_t)c->max_num))) return rc;
+        if (c->num_hint > 0)
+            sphk::k_inv_density<<<(c->num_hint + sphk::kSurfThreads - 1) / sphk::kSurfThreads, sphk::kSurfThreads, 0,
+                                  c->stream>>>(c->density, c->num_hint, c->cf_inv);
+    }
+    const unsigned long long chunks = (n + 31) / 32;
+    unsigned long long stride = 7919;  // a prime; step past the chunk count's factors
+    while (std::gcd(stride, chunks) != 1) stride += 2;
+    const unsigned long long threads = chunks * 32;
+    const unsigned blocks = (unsigned)((threads + sphk::kSurfThreads - 1) / sphk::kSurfThreads);
+    const unsigned long long st = stride % chunks == 0 ? 1 : stride % chunks;
+    if (c->exact)
+        sphk::k_colorfield<true><<<blocks, sphk::kSurfThreads, 0, c->stream>>>(
+            c->cf, res, chunks, st, c->pos_s, c->cf_inv, c->rec_vi, c->cell_start, c->cell_end, c->P);
+    else
+        sphk::k_colorfield<false><<<blocks, sphk::kSurfThreads, 0, c->stream>>>(
+            c->cf, res, chunks, st, c->pos_s, c->cf_inv, c->rec_vi, c->cell_start, c->cell_end, c->P);
     CK_LAUNCH(c);
     c->cf_res = res;
     return SPH_OK;
