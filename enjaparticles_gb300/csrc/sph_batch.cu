@@ -182,7 +182,7 @@ int batch_enqueue_step(sph_batch* b, float dt) {
     const sphk::ManyScenes scenes = batch_scenes(b);
     sphk::launch_density_batch(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, nullptr, b->mask,
                                (size_t)b->nslots, b->cell_start, b->cell_end, b->info_nb, scenes, b->unit != 0,
-                               b->nvalid, st);
+                               b->exact, b->nvalid, st);
     sphk::launch_force_batch(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->cell_start, b->cell_end,
                              b->info_nb, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, b->keep_f, b->keep_v, scenes,
                              b->unit != 0, dt, b->exact, b->nvalid, st);

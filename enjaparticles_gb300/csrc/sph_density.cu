@@ -1,9 +1,12 @@
 // sph_density.cu — density pass (rtpslib/system/sph/cl_src/density.cl:44-126,
 // poly6 cl_sph_kernels.h:29-45).
 //
-// Density keeps the reference's summation order and rounding: it equals the
-// FP32 oracle bit for bit.  Every multiply and add is a separately rounded
-// scalar operation.  (Packed two-lane FP32 arithmetic was tried and rejected:
+// In exact mode density keeps the reference's summation order and rounding:
+// it equals the FP32 oracle bit for bit.  Every multiply and add is a
+// separately rounded scalar operation.  The default mode keeps the order but
+// forms r^2 and the poly6 sum with fused multiply-adds, two instructions fewer
+// per candidate in a loop that is instruction-issue bound; a neighbour on the
+// cutoff may fall either side there, where its poly6 weight is ~0.  (Packed two-lane FP32 arithmetic was tried and rejected:
 // with this compiler a packed multiply followed by a packed add does not give
 // the separately rounded result, even with contraction disabled, which would
 // change |r|^2 and with it the neighbour sets.)
@@ -20,7 +23,7 @@ namespace sphk {
 
 // When called from the fused step the kernel also does the out-of-grid
 // deletion bookkeeping (vel_s != nullptr).
-template <bool Unit, bool WantCount, class Scenes>
+template <bool Exact, bool Unit, bool WantCount, class Scenes>
 __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ veleval_s,
                                                  float* __restrict__ density, float4* __restrict__ rec_pd,
                                                  float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
@@ -77,10 +80,12 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
             for (; j < jend; ++j, bit <<= 1) {
                 float4 q = __ldg(pos_s + j);
                 if (!Unit) q = v4scale(q, P.sc);
-                const float r2 = dist2_exact(__fsub_rn(pi.x, q.x), __fsub_rn(pi.y, q.y), __fsub_rn(pi.z, q.z));
+                const float dx = __fsub_rn(pi.x, q.x), dy = __fsub_rn(pi.y, q.y), dz = __fsub_rn(pi.z, q.z);
+                const float r2 = Exact ? dist2_exact(dx, dy, dz) : __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
                 if (r2 <= rc2) {
                     const float hr2 = __fsub_rn(h2, r2);
-                    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(hr2, hr2), hr2));
+                    acc = Exact ? __fadd_rn(acc, __fmul_rn(__fmul_rn(hr2, hr2), hr2))
+                                : __fmaf_rn(__fmul_rn(hr2, hr2), hr2, acc);
                     if (WantCount) ++cnt;
                     if (j != (uint32_t)i) cur |= bit;
                 }
@@ -111,20 +116,27 @@ template <class Scenes>
 void launch_density_t(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                       uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                       const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
-                      float4* vel_s, float4* del_pos, float4* del_vel, const Scenes& R, bool unit, int grid_items,
-                      cudaStream_t st) {
+                      float4* vel_s, float4* del_pos, float4* del_vel, const Scenes& R, bool unit, bool exact,
+                      int grid_items, cudaStream_t st) {
     const int threads = 256;
     int blocks = (grid_items + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
-#define SPH_DENSITY_LAUNCH(U, W)                                                                                    \
-    k_density<U, W, Scenes><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask,      \
-                                                        mask_stride, cell_start, cell_end, (int*)info, idx, vel_u, \
-                                                        vel_s, del_pos, del_vel, R)
-    if (unit) {
-        if (nbr) SPH_DENSITY_LAUNCH(true, true); else SPH_DENSITY_LAUNCH(true, false);
-    } else {
-        if (nbr) SPH_DENSITY_LAUNCH(false, true); else SPH_DENSITY_LAUNCH(false, false);
+#define SPH_DENSITY_LAUNCH(E, U, W)                                                                                   \
+    k_density<E, U, W, Scenes><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask,     \
+                                                           mask_stride, cell_start, cell_end, (int*)info, idx, vel_u, \
+                                                           vel_s, del_pos, del_vel, R)
+#define SPH_DENSITY_LAUNCH_E(E)                                                                \
+    if (unit) {                                                                                \
+        if (nbr) SPH_DENSITY_LAUNCH(E, true, true); else SPH_DENSITY_LAUNCH(E, true, false);   \
+    } else {                                                                                   \
+        if (nbr) SPH_DENSITY_LAUNCH(E, false, true); else SPH_DENSITY_LAUNCH(E, false, false); \
     }
+    if (exact) {
+        SPH_DENSITY_LAUNCH_E(true)
+    } else {
+        SPH_DENSITY_LAUNCH_E(false)
+    }
+#undef SPH_DENSITY_LAUNCH_E
 #undef SPH_DENSITY_LAUNCH
 }
 
@@ -134,15 +146,16 @@ void launch_density(const float4* pos_s, const float4* veleval_s, float* density
                     float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
                     cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     idx, vel_u, vel_s, del_pos, del_vel, OneScene{p}, p.unit_scale != 0, grid_items, st);
+                     idx, vel_u, vel_s, del_pos, del_vel, OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items,
+                     st);
 }
 
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                          const ManyScenes& scenes, bool unit, int grid_items, cudaStream_t st) {
+                          const ManyScenes& scenes, bool unit, int exact, int grid_items, cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     nullptr, nullptr, nullptr, nullptr, nullptr, scenes, unit, grid_items, st);
+                     nullptr, nullptr, nullptr, nullptr, nullptr, scenes, unit, exact != 0, grid_items, st);
 }
 
 }  // namespace sphk

@@ -165,7 +165,7 @@ void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_v
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                          const ManyScenes& scenes, bool unit, int grid_items, cudaStream_t st);
+                          const ManyScenes& scenes, bool unit, int exact, int grid_items, cudaStream_t st);
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                         size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                         uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,

@@ -2,8 +2,9 @@
 against the CPU oracle and the golden fixtures of the reference's kernels.
 
 Bit-exact: hash keys and indices, the sorted keys/indices, cell_start/end,
-the permuted arrays, density, collision and leapfrog.  Force is bit-exact in
-exact mode; in the default (fast) mode it must satisfy the FP32 tolerance
+the permuted arrays, collision and leapfrog.  Density and force are
+bit-exact in exact mode; in the default (fast) mode, which forms them with
+fused multiply-adds, they must satisfy the FP32 tolerance
   max_i |f_i - f_ref_i| <= 1e-5 * max_i |f_ref_i|   (per field, norm-wise)
 which is the "1e-5 relative" of the parity contract applied to a field whose
 elements cancel to zero.
@@ -86,8 +87,9 @@ def test_stages_exact_match_reference_golden(name):
 def test_stages_fast_force_within_tolerance(name):
     d, sp, g, gs = golden_io.load(name)
     o = staged_gpu(sp, g, gs, d["in_pos"], d["in_vel"], exact=False)
-    for k in ("sort_hashes", "sort_indices", "cell_start", "cell_end", "pos_s", "density_s"):
+    for k in ("sort_hashes", "sort_indices", "cell_start", "cell_end", "pos_s"):
         np.testing.assert_array_equal(o[k], d["s1_" + k], err_msg=k)
+    assert normwise(o["density_s"], d["s1_density_s"]) <= FORCE_RTOL
     assert normwise(o["force_pre"][:, :3], d["s1_force_pre"][:, :3]) <= FORCE_RTOL
     assert normwise(o["xsph_s"][:, :3], d["s1_xsph_s"][:, :3]) <= FORCE_RTOL
     assert normwise(o["force_s"][:, :3], d["s1_force_s"][:, :3]) <= FORCE_RTOL
