@@ -46,6 +46,11 @@ sys.path.insert(0, ROOT)
 N_DEFAULT = 2097152
 DT = 0.001
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (read + write) of one launch, from an ncu capture of the 2M step
+# (profiles/sph_density_force_2M.md); reported as roofline.traffic for the
+# dominant kernel when it is one of these.
+MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 203.5648e6 + 70.948352e6,
+                    "k_density": 70.404096e6 + 82.43968e6}
 
 
 def parse():
@@ -595,7 +600,8 @@ def main():
                         "%d steps" % args.e2e_steps},
         "gpu_launches": nk.value * steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "frac": achieved / peak,
+                     "traffic": MEASURED_TRAFFIC.get(dom) if n == N_DEFAULT else None, "peak_source": peak_kind,
                      "algorithmic_bytes": ab[dom], "mean_launch_ms": kern_ms[dom]},
         "step_roofline": {"algorithmic_bytes": b_step, "achieved": b_step / (step_ms / 1e3) / 1e9, "peak": peak,
                           "frac": b_step / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s"},
