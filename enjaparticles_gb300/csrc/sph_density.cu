@@ -68,7 +68,11 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
     // candidates are taken in chunks that end at a word boundary
     uint32_t cur = 0, p = 0;
     uint32_t* mrow = mask + i;
+    // walk position of i itself (its bit is cleared when its word is stored,
+    // instead of testing j != i for every candidate)
+    uint32_t pself = 0xffffffffu;
     auto run = [&](uint32_t rs, uint32_t re) {
+        if ((uint32_t)i - rs < re - rs) pself = p + ((uint32_t)i - rs);
         uint32_t j = rs;
         while (j < re) {
             const uint32_t b0 = p & 31u;
@@ -87,12 +91,13 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
                     acc = Exact ? __fadd_rn(acc, __fmul_rn(__fmul_rn(hr2, hr2), hr2))
                                 : __fmaf_rn(__fmul_rn(hr2, hr2), hr2, acc);
                     if (WantCount) ++cnt;
-                    if (j != (uint32_t)i) cur |= bit;
+                    cur |= bit;
                 }
             }
             p += k;
             if ((p & 31u) == 0) {
                 const uint32_t w = (p >> 5) - 1;
+                if (w == (pself >> 5)) cur &= ~(1u << (pself & 31u));
                 if (w < (uint32_t)kMaskWords) mrow[(size_t)w * mstride] = cur;
                 cur = 0;
             }
@@ -103,7 +108,10 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
         walk_rows_fast(P, cs, ce, c, run);
     else
         walk_rows_slow(P, cs, ce, c, run);
-    if ((p & 31u) != 0 && (p >> 5) < (uint32_t)kMaskWords) mrow[(size_t)(p >> 5) * mstride] = cur;
+    if ((p & 31u) != 0 && (p >> 5) < (uint32_t)kMaskWords) {
+        if ((p >> 5) == (pself >> 5)) cur &= ~(1u << (pself & 31u));
+        mrow[(size_t)(p >> 5) * mstride] = cur;
+    }
     const float rho = __fmul_rn(P.dens_coef, acc);
     density[i] = rho;
     const float4 ve = __ldg(veleval_s + i);
