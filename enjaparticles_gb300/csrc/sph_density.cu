@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
             if (k > re - j) k = re - j;
             const uint32_t jend = j + k;
             uint32_t bit = 1u << b0;
-#pragma unroll 2
+#pragma unroll 4
             for (; j < jend; ++j, bit <<= 1) {
                 float4 q = __ldg(pos_s + j);
                 if (!Unit) q = v4scale(q, P.sc);
