@@ -414,6 +414,17 @@ int oracle_sim_upload(void* h, const float* pos, const float* vel, const float* 
     s->num = n;
     return 0;
 }
+// SPH::pushParticles (SPH.cpp:560-602): pos and vel appended after the
+// current particles, veleval left as it is; a push past max_num is dropped
+// (returns -1).
+int oracle_sim_push(void* h, const float* pos, const float* vel, int n) {
+    OracleSim* s = (OracleSim*)h;
+    if (n < 0 || s->num + n > s->max_num) return -1;
+    std::memcpy(s->pos_u.data() + 4 * (size_t)s->num, pos, 16 * (size_t)n);
+    std::memcpy(s->vel_u.data() + 4 * (size_t)s->num, vel, 16 * (size_t)n);
+    s->num += n;
+    return 0;
+}
 void oracle_sim_update(void* h) { sim_update(*(OracleSim*)h); }
 void oracle_sim_integrate(void* h, float dt) { sim_integrate(*(OracleSim*)h, dt); }
 void oracle_sim_step(void* h, float dt, int nsteps) {

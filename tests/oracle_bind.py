@@ -65,6 +65,7 @@ def oracle():
             "oracle_sim_set_integrator": (None, [_P, _I]),
             "oracle_collision_triangles": (None, [_I, _I, _P, _P, _P, _P, _I, _P]),
             "oracle_sim_set_triangles": (None, [_P, _P, _I]),
+            "oracle_sim_push": (_I, [_P, _P, _P, _I]),
             "oracle_colorfield": (None, [_I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_rollout64": (_I, [_P, _P, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_rollout64_jvp": (_I, [_P, _P, C.c_double, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P,
@@ -157,6 +158,12 @@ class OracleSim:
     def set_integrator(self, kind):
         """0: leapfrog, 1: euler."""
         self.lib.oracle_sim_set_integrator(self.h, int(kind))
+
+    def push(self, pos, vel):
+        """SPH::pushParticles; False when past max_num (dropped)."""
+        p = np.ascontiguousarray(pos, np.float32)
+        v = np.ascontiguousarray(vel, np.float32)
+        return self.lib.oracle_sim_push(self.h, ptr(p), ptr(v), p.shape[0]) == 0
 
     def set_triangles(self, tris):
         """(m, 4, 4) or (m, 16) float32 triangles; collision_triangle runs after the walls."""
