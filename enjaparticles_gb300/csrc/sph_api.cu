@@ -298,9 +298,9 @@ void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t 
 
 }  // namespace
 
-// SPH::update as staged launches: hash, sort, cellindices+permute,
-// out-of-grid deletion, density, force, gravity, walls, triangles.
-static int enqueue_update(sph_ctx* c) {
+// SPH::update as staged launches up to the force pass: hash, sort,
+// cellindices+permute, out-of-grid deletion, density, force.
+static int enqueue_to_force(sph_ctx* c) {
     int rc = enqueue_hash(c);
     if (rc) return rc;
     if ((rc = enqueue_sort(c))) return rc;
@@ -310,6 +310,13 @@ static int enqueue_update(sph_ctx* c) {
                                c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
     density_launch(c, c->idx_a, false, c->stream);
     force_launch(c, c->idx_a, false, 0.f, c->stream);
+    return SPH_OK;
+}
+
+// SPH::update as staged launches: up to force, then gravity, walls, triangles.
+static int enqueue_update(sph_ctx* c) {
+    int rc = enqueue_to_force(c);
+    if (rc) return rc;
     sphk::launch_gravity(c->pos_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
     sphk::launch_collision(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
     sphk::launch_triangles(c->pos_s, c->vel_s, c->force_s, c->info, c->P, c->num_hint, c->stream);
@@ -319,16 +326,13 @@ static int enqueue_update(sph_ctx* c) {
 
 int enqueue_fused_step(sph_ctx* c, float dt) {
     if (c->n_tri > 0) {
-        // the triangle stage sits between the walls and the integrator, so
-        // the step runs the staged sequence
-        int rc = enqueue_update(c);
+        // the triangle stage sits between the walls and the integrator: the
+        // staged passes up to force, then one kernel for gravity, walls,
+        // triangles and the integrator
+        int rc = enqueue_to_force(c);
         if (rc) return rc;
-        if (c->integrator == sphk::kIntegratorEuler)
-            sphk::launch_euler(c->pos_s, c->vel_s, c->force_s, c->idx_a, c->pos_u, c->vel_u, c->info, c->P, dt,
-                               c->num_hint, c->stream);
-        else
-            sphk::launch_leapfrog(c->pos_s, c->vel_s, c->force_s, c->xsph_s, c->idx_a, c->pos_u, c->vel_u,
-                                  c->veleval_u, c->info, c->P, dt, c->num_hint, c->stream);
+        sphk::launch_triangles_step(c->pos_s, c->vel_s, c->force_s, c->xsph_s, c->idx_a, c->pos_u, c->vel_u,
+                                    c->veleval_u, c->info, c->P, dt, c->num_hint, c->stream);
         CK_LAUNCH(c);
         return SPH_OK;
     }

@@ -181,6 +181,11 @@ void launch_gravity(const float4* pos_s, float4* force_s, const int* info, const
 // collision_triangle after the walls; no-op without a mesh.
 void launch_triangles(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info, const StepParams& p,
                       int grid_items, cudaStream_t st);
+// The end of the step with a mesh: gravity, walls, triangles and the
+// integrator in one kernel after the (unfused) force pass.
+void launch_triangles_step(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
+                           const uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
+                           const StepParams& p, float dt, int grid_items, cudaStream_t st);
 void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_s, uint32_t* idx, float4* pos_u,
                   float4* vel_u, const int* info, const StepParams& p, float dt, int grid_items, cudaStream_t st);
 void launch_delete_staged(const float4* pos_s, const float4* vel_s, const float4* veleval_s, uint32_t* idx,

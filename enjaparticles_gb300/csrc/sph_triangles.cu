@@ -154,11 +154,30 @@ __device__ __forceinline__ bool box_holds(float4 lo, float4 hi, float4 p) {
     return p.x >= lo.x && p.x <= hi.x && p.y >= lo.y && p.y <= hi.y && p.z >= lo.z && p.z <= hi.z;
 }
 
+// The rest of the step after the force pass, when the kernel ends it (Step):
+// sorted xsph and sort_indices in, the integrated state out.
+struct TriStepTail {
+    const float4* xsph_s;
+    const uint32_t* idx;
+    float4* pos_u;
+    float4* vel_u;
+    float4* veleval_u;
+    float dt;
+};
+
+// Step = false: the stage (force_s holds the force after the walls; it gets
+// the triangle contacts added).  Step = true: the end of the step with a
+// mesh: per particle, the force pass's output plus the point sources and the
+// walls (gravity.cl, collision_wall.cl), the triangle contacts, then the
+// integrator (leapfrog.cl or euler.cl) scattered to the unsorted state: the
+// same operations as those staged kernels, in one pass over the particles.
+template <bool Step, bool Exact>
 __global__ void __launch_bounds__(kTriThreads) k_triangles(const float4* __restrict__ pos_s,
                                                            const float4* __restrict__ vel_s,
                                                            float4* __restrict__ force_s, const int* __restrict__ info,
                                                            const float4* __restrict__ geo,
-                                                           const float4* __restrict__ box, const StepParams P) {
+                                                           const float4* __restrict__ box, const StepParams P,
+                                                           const TriStepTail S) {
     __shared__ int s_cand[kTriThreads];
     __shared__ int s_wcnt[kTriThreads / 32];
     __shared__ float s_red[6][kTriThreads / 32];
@@ -172,9 +191,14 @@ __global__ void __launch_bounds__(kTriThreads) k_triangles(const float4* __restr
     const float bound = P.tri_bound;
     float4 pos = make_float4(0.f, 0.f, 0.f, 0.f), vel = pos, f0 = pos;
     if (valid) {
-        pos = scaled(__ldg(pos_s + i), P);
+        const float4 raw = __ldg(pos_s + i);
+        pos = scaled(raw, P);
         vel = __ldg(vel_s + i);
         f0 = force_s[i];
+        if (Step) {
+            if (P.n_grav > 0) f0 = gravity_add<Exact>(f0, raw, P);
+            f0 = collide_walls(pos, vel, f0, P);
+        }
     }
     // box of the block's particles (NaN coordinates drop out of fminf/fmaxf;
     // such a particle never makes contact)
@@ -244,8 +268,24 @@ __global__ void __launch_bounds__(kTriThreads) k_triangles(const float4* __restr
     rf = v4add(rf, f);
     if (!valid) return;
     // rf.w: each group adds its triangle count, an exact integer sum
-    force_s[i] = make_float4(__fadd_rn(f0.x, rf.x), __fadd_rn(f0.y, rf.y), __fadd_rn(f0.z, rf.z),
-                             __fadd_rn(f0.w, (float)ntri));
+    const float4 ff = make_float4(__fadd_rn(f0.x, rf.x), __fadd_rn(f0.y, rf.y), __fadd_rn(f0.z, rf.z),
+                                  __fadd_rn(f0.w, (float)ntri));
+    if (!Step) {
+        force_s[i] = ff;
+        return;
+    }
+    const uint32_t o = __ldg(S.idx + i);
+    float4 po, vo, eo;
+    if (P.integrator == kIntegratorEuler) {
+        euler_core(pos, vel, ff, S.dt, P, po, vo);
+        S.vel_u[o] = vo;
+        S.pos_u[o] = po;
+        return;
+    }
+    leapfrog_core(pos, vel, ff, __ldg(S.xsph_s + i), S.dt, P, po, vo, eo);
+    S.vel_u[o] = vo;
+    S.veleval_u[o] = eo;
+    S.pos_u[o] = po;
 }
 
 }  // namespace
@@ -256,7 +296,23 @@ void launch_triangles(const float4* pos_s, const float4* vel_s, float4* force_s,
     k_tri_prep<<<(p.n_tri + 255) / 256, 256, 0, st>>>(p.tri_raw, p.n_tri, p.tri_geo, p.tri_box, p);
     int blocks = (grid_items + kTriThreads - 1) / kTriThreads;
     if (blocks < 1) blocks = 1;
-    k_triangles<<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, force_s, info, p.tri_geo, p.tri_box, p);
+    k_triangles<false, false><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, force_s, info, p.tri_geo, p.tri_box, p,
+                                                              TriStepTail{});
+}
+
+void launch_triangles_step(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
+                           const uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
+                           const StepParams& p, float dt, int grid_items, cudaStream_t st) {
+    if (p.n_tri <= 0) return;
+    k_tri_prep<<<(p.n_tri + 255) / 256, 256, 0, st>>>(p.tri_raw, p.n_tri, p.tri_geo, p.tri_box, p);
+    int blocks = (grid_items + kTriThreads - 1) / kTriThreads;
+    if (blocks < 1) blocks = 1;
+    const TriStepTail S{xsph_s, idx, pos_u, vel_u, veleval_u, dt};
+    float4* f = const_cast<float4*>(force_s);  // only read when Step
+    if (p.exact)
+        k_triangles<true, true><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, f, info, p.tri_geo, p.tri_box, p, S);
+    else
+        k_triangles<true, false><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, f, info, p.tri_geo, p.tri_box, p, S);
 }
 
 }  // namespace sphk
