@@ -143,6 +143,7 @@ int sph_make_step_params(const SPHParams& s, const GridParams& gp, const GridPar
     P.tri_raw = nullptr;
     P.tri_geo = nullptr;
     P.tri_box = nullptr;
+    P.tri_tile = nullptr;
     return SPH_OK;
 }
 
@@ -185,6 +186,7 @@ int build_step_params(sph_ctx* c) {
         c->P.tri_raw = c->tri;
         c->P.tri_geo = c->tri + 4 * (size_t)c->tri_cap;
         c->P.tri_box = c->tri + 8 * (size_t)c->tri_cap;
+        c->P.tri_tile = c->tri + 10 * (size_t)c->tri_cap;
     }
     c->params_version++;
     return SPH_OK;
@@ -582,7 +584,7 @@ int sph_load_triangles(sph_ctx* c, const sph_float4* tris, int count) {
         c->tri = nullptr;
         c->tri_cap = 0;
         c->n_tri = 0;
-        CK(c, cudaMalloc(&c->tri, sizeof(float4) * 10 * (size_t)count));
+        CK(c, cudaMalloc(&c->tri, sizeof(float4) * (10 * (size_t)count + 2 * (size_t)((count + 255) / 256))));
         c->tri_cap = count;
     }
     if (count > 0) {

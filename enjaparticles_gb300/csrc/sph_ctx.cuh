@@ -50,6 +50,7 @@ struct sph_ctx {
     int n_grav = 0;
     int integrator = 0;
     // triangle mesh: one allocation of tri_cap * 10 float4 (raw, geo, box)
+    // and 2 float4 per 256 triangles (tile boxes)
     float4* tri = nullptr;
     int n_tri = 0;
     int tri_cap = 0;

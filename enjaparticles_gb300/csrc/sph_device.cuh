@@ -68,6 +68,7 @@ struct StepParams {
     const float4* tri_raw;        // 4 float4 per triangle, as loaded
     float4* tri_geo;              // 4 float4 per triangle (sph_triangles.cu)
     float4* tri_box;              // 2 float4 per triangle
+    float4* tri_tile;             // 2 float4 per 256 triangles
 };
 constexpr int kIntegratorLeapfrog = 0;
 constexpr int kIntegratorEuler = 1;

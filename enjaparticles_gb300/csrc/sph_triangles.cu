@@ -75,6 +75,37 @@ __global__ void __launch_bounds__(256) k_tri_prep(const float4* __restrict__ tri
                                          fmaxf(fmaxf(az, bz), cz) + w, 0.f);
 }
 
+// tile[2t], tile[2t+1]: the union of the widened boxes of triangles
+// [256t, 256t + 256), so that a block can pass over a whole tile.
+__global__ void __launch_bounds__(256) k_tri_tiles(const float4* __restrict__ box, int ntri,
+                                                   float4* __restrict__ tile) {
+    __shared__ float s[6][8];
+    const int j = blockIdx.x * 256 + threadIdx.x;
+    float r[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    if (j < ntri) {
+        const float4 lo = box[2 * (size_t)j], hi = box[2 * (size_t)j + 1];
+        r[0] = lo.x; r[1] = lo.y; r[2] = lo.z; r[3] = hi.x; r[4] = hi.y; r[5] = hi.z;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) r[k] = fminf(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+#pragma unroll
+        for (int k = 3; k < 6; ++k) r[k] = fmaxf(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+    }
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s[k][threadIdx.x >> 5] = r[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s[k][0] = k < 3 ? fminf(s[k][0], s[k][w]) : fmaxf(s[k][0], s[k][w]);
+        tile[2 * (size_t)blockIdx.x] = make_float4(s[0][0], s[1][0], s[2][0], 0.f);
+        tile[2 * (size_t)blockIdx.x + 1] = make_float4(s[3][0], s[4][0], s[5][0], 0.f);
+    }
+}
+
 // Per-particle part of intersect_triangle_segment: the segment
 // p = pos - v_hat d .. q = pos + v_hat d of half-length d = boundary
 // distance along the velocity (collision_tri.cl:218-221).
@@ -176,7 +207,8 @@ __global__ void __launch_bounds__(kTriThreads) k_triangles(const float4* __restr
                                                            const float4* __restrict__ vel_s,
                                                            float4* __restrict__ force_s, const int* __restrict__ info,
                                                            const float4* __restrict__ geo,
-                                                           const float4* __restrict__ box, const StepParams P,
+                                                           const float4* __restrict__ box,
+                                                           const float4* __restrict__ tile_box, const StepParams P,
                                                            const TriStepTail S) {
     __shared__ int s_cand[kTriThreads];
     __shared__ int s_wcnt[kTriThreads / 32];
@@ -229,6 +261,13 @@ __global__ void __launch_bounds__(kTriThreads) k_triangles(const float4* __restr
     float4 f = make_float4(0.f, 0.f, 0.f, 0.f), rf = f;
     int chunk = 0;
     for (int t0 = 0; t0 < ntri; t0 += kTriThreads) {
+        {  // a tile whose union box misses the block's box has no candidate
+            const float4 lo = __ldg(tile_box + 2 * (size_t)(t0 / kTriThreads));
+            const float4 hi = __ldg(tile_box + 2 * (size_t)(t0 / kTriThreads) + 1);
+            if (!(lo.x <= bhi.x && hi.x >= blo.x && lo.y <= bhi.y && hi.y >= blo.y && lo.z <= bhi.z &&
+                  hi.z >= blo.z))
+                continue;  // the same for every thread of the block
+        }
         // candidates of this tile, in triangle order
         const int j = t0 + tid;
         bool cand = false;
@@ -294,10 +333,11 @@ void launch_triangles(const float4* pos_s, const float4* vel_s, float4* force_s,
                       int grid_items, cudaStream_t st) {
     if (p.n_tri <= 0) return;
     k_tri_prep<<<(p.n_tri + 255) / 256, 256, 0, st>>>(p.tri_raw, p.n_tri, p.tri_geo, p.tri_box, p);
+    k_tri_tiles<<<(p.n_tri + 255) / 256, 256, 0, st>>>(p.tri_box, p.n_tri, p.tri_tile);
     int blocks = (grid_items + kTriThreads - 1) / kTriThreads;
     if (blocks < 1) blocks = 1;
-    k_triangles<false, false><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, force_s, info, p.tri_geo, p.tri_box, p,
-                                                              TriStepTail{});
+    k_triangles<false, false><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, force_s, info, p.tri_geo, p.tri_box,
+                                                              p.tri_tile, p, TriStepTail{});
 }
 
 void launch_triangles_step(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
@@ -305,14 +345,17 @@ void launch_triangles_step(const float4* pos_s, const float4* vel_s, const float
                            const StepParams& p, float dt, int grid_items, cudaStream_t st) {
     if (p.n_tri <= 0) return;
     k_tri_prep<<<(p.n_tri + 255) / 256, 256, 0, st>>>(p.tri_raw, p.n_tri, p.tri_geo, p.tri_box, p);
+    k_tri_tiles<<<(p.n_tri + 255) / 256, 256, 0, st>>>(p.tri_box, p.n_tri, p.tri_tile);
     int blocks = (grid_items + kTriThreads - 1) / kTriThreads;
     if (blocks < 1) blocks = 1;
     const TriStepTail S{xsph_s, idx, pos_u, vel_u, veleval_u, dt};
     float4* f = const_cast<float4*>(force_s);  // only read when Step
     if (p.exact)
-        k_triangles<true, true><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, f, info, p.tri_geo, p.tri_box, p, S);
+        k_triangles<true, true><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, f, info, p.tri_geo, p.tri_box,
+                                                                p.tri_tile, p, S);
     else
-        k_triangles<true, false><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, f, info, p.tri_geo, p.tri_box, p, S);
+        k_triangles<true, false><<<blocks, kTriThreads, 0, st>>>(pos_s, vel_s, f, info, p.tri_geo, p.tri_box,
+                                                                 p.tri_tile, p, S);
 }
 
 }  // namespace sphk
