@@ -8,9 +8,13 @@
 // line: particle-updates/s and an FP64 checksum of the final positions.
 //
 //   sph_bench [--n N] [--steps S] [--warmup W] [--dt DT] [--viscosity MU]
-//             [--frames] [--exact]
+//             [--frames] [--exact] [--mesh] [--post-process RES]
 //   --frames: one update()+integrate() pair per step (the reference's frame
 //             loop, staged kernels) instead of the fused graph-replayed step.
+//   --mesh: load the 524-triangle ramp-and-box mesh (scenes.ramp_and_box_mesh,
+//             same vertex bits) with SPH::loadTriangles.
+//   --post-process RES: SPH::postProcess with the colour field at RES after
+//             the run (every frame with --frames); prints the mesh's triangles.
 //   sph_bench --n N --dump-scene FILE: write the scene's positions (N x 4
 //             float32) to FILE and exit (no GPU needed).
 #include <chrono>
@@ -56,10 +60,46 @@ std::vector<rtps::float4> dambreak_positions(int n, uint64_t seed) {
     return pos;
 }
 
+// scenes.ramp_mesh() + scenes.box_mesh((0.6, 0.3, 0), (0.75, 0.6, 0.3)): the
+// vertices from the same double expressions, rounded to float (the stored
+// normal is not read by the kernel and is left zero).
+std::vector<rtps::Triangle> ramp_and_box_mesh() {
+    std::vector<rtps::Triangle> t;
+    auto tri = [&](const double* a, const double* b, const double* c) {
+        rtps::Triangle x;
+        const double* v[3] = {a, b, c};
+        for (int k = 0; k < 3; ++k) x.verts[k] = rtps::make_float4((float)v[k][0], (float)v[k][1], (float)v[k][2], 1.f);
+        x.normal = rtps::make_float4(0, 0, 0, 0);
+        t.push_back(x);
+    };
+    const int nx = 16, ny = 16;
+    const double z0 = 0.12, z1 = 0.22;
+    auto z = [&](double x) { return z0 + (z1 - z0) * x; };
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const double x0 = i * (1.0 / nx), x1 = (i + 1) * (1.0 / nx), y0 = j * (1.0 / ny), y1 = (j + 1) * (1.0 / ny);
+            const double a[3] = {x0, y0, z(x0)}, b[3] = {x1, y0, z(x1)}, c[3] = {x1, y1, z(x1)}, d[3] = {x0, y1, z(x0)};
+            tri(a, b, c);
+            tri(a, c, d);
+        }
+    const double lo[3] = {0.6, 0.3, 0.0}, hi[3] = {0.75, 0.6, 0.3};
+    double cn[8][3];
+    for (int k = 0; k < 8; ++k) {
+        static const int sel[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+        for (int a = 0; a < 3; ++a) cn[k][a] = sel[k][a] ? hi[a] : lo[a];
+    }
+    static const int quads[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {2, 3, 7, 6}, {1, 2, 6, 5}, {3, 0, 4, 7}};
+    for (const auto& q : quads) {
+        tri(cn[q[0]], cn[q[1]], cn[q[2]]);
+        tri(cn[q[0]], cn[q[2]], cn[q[3]]);
+    }
+    return t;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
-    int n = 262144, steps = 200, warmup = 10, frames = 0, exact = 0;
+    int n = 262144, steps = 200, warmup = 10, frames = 0, exact = 0, mesh = 0, post_res = 0;
     float dt = 0.001f, mu = 0.01f;
     std::string dump;
     for (int i = 1; i < argc; ++i) {
@@ -79,6 +119,8 @@ int main(int argc, char** argv) {
         else if (a == "--frames") frames = 1;
         else if (a == "--exact") exact = 1;
         else if (a == "--dump-scene") dump = next();
+        else if (a == "--mesh") mesh = 1;
+        else if (a == "--post-process") post_res = std::atoi(next());
         else {
             std::fprintf(stderr, "unknown argument %s\n", a.c_str());
             return 2;
@@ -100,6 +142,11 @@ int main(int argc, char** argv) {
     try {
         rtps::SPH sph(sp, g, n, &gs, dt);
         if (exact) sph_set_exact(sph.handle(), 1);
+        if (mesh) {
+            std::vector<rtps::Triangle> tris = ramp_and_box_mesh();
+            sph.loadTriangles(tris);
+        }
+        if (post_res > 0) sph.useColorField(true, post_res);
         sph.pushParticles(dambreak_positions(n, 20250101ull), rtps::make_float4(0, 0, 0, 0));
         auto frame = [&](int k) {
             if (frames) {
@@ -121,14 +168,19 @@ int main(int argc, char** argv) {
         frame(steps);
         sph.sync();
         const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        int ntri = -1;
+        if (post_res > 0) {
+            if (!frames) sph.postProcess();
+            ntri = sph.getMesh(nullptr, nullptr);
+        }
         const std::vector<rtps::float4> p = sph.getPositions();
         double sum = 0.0;
         for (const rtps::float4& q : p) sum += (double)q.x + 2.0 * q.y + 3.0 * q.z;
         std::printf("{\"metric\": \"particle-updates/s\", \"value\": %.6g, \"n\": %d, \"steps\": %d, \"warmup\": %d, "
                     "\"seconds\": %.6g, \"mode\": \"%s\", \"exact\": %d, \"num_after\": %d, "
-                    "\"checksum\": %.17g, \"build\": \"%s\"}\n",
+                    "\"checksum\": %.17g, \"mesh\": %d, \"triangles\": %d, \"build\": \"%s\"}\n",
                     steps > 0 && el > 0 ? (double)n * steps / el : 0.0, n, steps, warmup, el,
-                    frames ? "frames" : "fused", exact, sph.getNum(), sum, sph_build_info());
+                    frames ? "frames" : "fused", exact, sph.getNum(), sum, mesh, ntri, sph_build_info());
     } catch (const rtps::SPHError& e) {
         std::fprintf(stderr, "error %d: %s\n", e.code(), e.what());
         return 1;

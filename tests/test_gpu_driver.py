@@ -36,3 +36,22 @@ def test_driver_matches_python_exact():
 def test_driver_throughput_line():
     d = _run("--n", 262144, "--steps", 100, "--warmup", 5)
     assert d["metric"] == "particle-updates/s" and d["mode"] == "fused" and d["value"] > 1e8
+
+
+def test_driver_mesh_and_post_process_match_python():
+    """--mesh loads the ramp-and-box mesh through rtps::SPH::loadTriangles and
+    --post-process runs SPH::postProcess: the same bits and the same surface
+    as the Python harness with scenes.ramp_and_box_mesh and postProcess."""
+    from enjaparticles_gb300.scenes import ramp_and_box_mesh
+    n, steps, warm, res = 16384, 20, 3, 32
+    d = _run("--n", n, "--steps", steps, "--warmup", warm, "--exact", "--mesh", "--post-process", res)
+    s, _, _ = dambreak_system(n, exact=True)
+    s.loadTriangles(ramp_and_box_mesh())
+    s.step(0.001, warm + steps)
+    p = s.get("pos_u", n).astype(np.float64)
+    want = 0.0
+    for q in p:
+        want += q[0] + 2.0 * q[1] + 3.0 * q[2]
+    v, _ = s.postProcess(res)
+    assert d["mesh"] == 1 and d["checksum"] == want
+    assert d["triangles"] == len(v) > 0
