@@ -240,6 +240,9 @@ void free_all(sph_ctx* c) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
+    if (c->up_done) cudaEventDestroy(c->up_done);
+    if (c->up_start) cudaEventDestroy(c->up_start);
+    if (c->up_stream) cudaStreamDestroy(c->up_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
 
@@ -306,6 +309,7 @@ static int enqueue_to_force(sph_ctx* c) {
     int rc = enqueue_hash(c);
     if (rc) return rc;
     if ((rc = enqueue_sort(c))) return rc;
+    if ((rc = join_upload(c))) return rc;
     sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
                                c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 2, c->stream);
     sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
@@ -342,6 +346,7 @@ int enqueue_fused_step(sph_ctx* c, float dt) {
     if (rc) return rc;
     rc = enqueue_sort(c);
     if (rc) return rc;
+    if ((rc = join_upload(c))) return rc;
     sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
                                c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 1, c->stream);
     density_launch(c, c->idx_a, true, c->stream);
@@ -359,10 +364,27 @@ int read_info(sph_ctx* c) {
     return SPH_OK;
 }
 
-int check_ctx(sph_ctx* c) {
+int check_ctx(sph_ctx* c, bool join) {
     if (!c) return SPH_EINVAL;
     int dev = -1;
     if (cudaGetDevice(&dev) == cudaSuccess && dev != c->device) CK(c, cudaSetDevice(c->device));
+    if (join && c->up_pending) {
+        CK(c, cudaStreamWaitEvent(c->stream, c->up_done, 0));
+        c->up_pending = false;
+    }
+    return SPH_OK;
+}
+
+int join_upload(sph_ctx* c) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(c, cudaStreamIsCapturing(c->stream, &cs));
+    if (cs == cudaStreamCaptureStatusActive) {
+        // in the step graph for good: every replay waits for the latest upload
+        CK(c, cudaStreamWaitEvent(c->stream, c->up_done, cudaEventWaitExternal));
+    } else if (c->up_pending) {
+        CK(c, cudaStreamWaitEvent(c->stream, c->up_done, 0));
+        c->up_pending = false;
+    }
     return SPH_OK;
 }
 
@@ -449,8 +471,11 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
 #undef ALLOC
     if (rc == SPH_OK && cudaMallocHost((void**)&c->host_info, sizeof(int) * sphk::kInfoSlots) != cudaSuccess)
         rc = set_err(nullptr, SPH_ENOMEM, "cudaMallocHost failed");
-    if (rc == SPH_OK && cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
-        rc = set_err(nullptr, SPH_ECUDA, "cudaStreamCreate failed");
+    if (rc == SPH_OK && (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+                         cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking) != cudaSuccess ||
+                         cudaEventCreateWithFlags(&c->up_start, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaEventCreateWithFlags(&c->up_done, cudaEventDisableTiming) != cudaSuccess))
+        rc = set_err(nullptr, SPH_ECUDA, "cudaStreamCreate / cudaEventCreate failed");
     if (rc != SPH_OK) {
         free_all(c);
         delete c;
@@ -495,6 +520,7 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
 int sph_destroy(sph_ctx* c) {
     if (!c) return SPH_EINVAL;
     cudaSetDevice(c->device);
+    if (c->up_stream) cudaStreamSynchronize(c->up_stream);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (sph_hose* h : c->hoses) sph_hose_destroy(h);
     free_all(c);
@@ -610,11 +636,18 @@ int sph_upload(sph_ctx* c, const sph_float4* pos, const sph_float4* vel, const s
     const size_t b = (size_t)n * 16;
     if (n > 0) {
         CK(c, cudaMemcpyAsync(c->pos_u, pos, b, cudaMemcpyHostToDevice, c->stream));
-        CK(c, cudaMemcpyAsync(c->vel_u, vel, b, cudaMemcpyHostToDevice, c->stream));
+        // vel and veleval follow on the side stream once pos is in (the link
+        // is not shared with it): the next step's hash and sort, which read
+        // only pos, run meanwhile
+        CK(c, cudaEventRecord(c->up_start, c->stream));
+        CK(c, cudaStreamWaitEvent(c->up_stream, c->up_start, 0));
+        CK(c, cudaMemcpyAsync(c->vel_u, vel, b, cudaMemcpyHostToDevice, c->up_stream));
         if (veleval)
-            CK(c, cudaMemcpyAsync(c->veleval_u, veleval, b, cudaMemcpyHostToDevice, c->stream));
+            CK(c, cudaMemcpyAsync(c->veleval_u, veleval, b, cudaMemcpyHostToDevice, c->up_stream));
         else
-            CK(c, cudaMemsetAsync(c->veleval_u, 0, b, c->stream));
+            CK(c, cudaMemsetAsync(c->veleval_u, 0, b, c->up_stream));
+        CK(c, cudaEventRecord(c->up_done, c->up_stream));
+        c->up_pending = true;
     }
     k_set_num<<<1, 1, 0, c->stream>>>(c->info, n);
     CK_LAUNCH(c);
@@ -801,7 +834,7 @@ int sph_stage_leapfrog(sph_ctx* c, float dt) {
 }
 
 int sph_update(sph_ctx* c) {
-    int rc = check_ctx(c);
+    int rc = check_ctx(c, false);  // the upload is joined before cells+permute
     if (rc) return rc;
     if (!c->hoses.empty() && (rc = sph_spray_hoses(c, nullptr))) return rc;
     return enqueue_update(c);
@@ -887,7 +920,7 @@ int sph_integrate(sph_ctx* c, float dt) {
 static int ensure_step_graph(sph_ctx* c, float dt);
 
 int sph_step(sph_ctx* c, float dt, int nsteps) {
-    int rc = check_ctx(c);
+    int rc = check_ctx(c, false);  // the upload is joined inside the step, before cells+permute
     if (rc) return rc;
     if (nsteps < 0 || !std::isfinite(dt)) return set_err(c, SPH_EINVAL, "sph_step: bad arguments");
     if (!c->hoses.empty()) {
@@ -897,11 +930,13 @@ int sph_step(sph_ctx* c, float dt, int nsteps) {
             if (c->num_hint == 0) continue;
             if ((rc = ensure_step_graph(c, dt))) return rc;
             CK(c, cudaGraphLaunch(c->graph, c->stream));
+            c->up_pending = false;  // the graph waited for it
         }
     } else {
         if (nsteps == 0 || c->num_hint == 0) return SPH_OK;
         if ((rc = ensure_step_graph(c, dt))) return rc;
         for (int k = 0; k < nsteps; ++k) CK(c, cudaGraphLaunch(c->graph, c->stream));
+        c->up_pending = false;  // the graph waited for it
     }
     c->keys_cur = c->keys_a;
     c->idx_cur = c->idx_a;
@@ -943,7 +978,7 @@ static int ensure_step_graph(sph_ctx* c, float dt) {
 }
 
 int sph_step_eager(sph_ctx* c, float dt, int nsteps) {
-    int rc = check_ctx(c);
+    int rc = check_ctx(c, false);
     if (rc) return rc;
     if (nsteps < 0 || !std::isfinite(dt)) return set_err(c, SPH_EINVAL, "sph_step_eager: bad arguments");
     for (int k = 0; k < nsteps; ++k) {

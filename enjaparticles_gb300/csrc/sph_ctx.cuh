@@ -15,6 +15,12 @@ struct sph_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
+    // sph_upload copies vel/veleval on up_stream after the position copy, so
+    // that they overlap hash and sort; up_done marks their end, and the step
+    // waits for it before cells+permute (every other call waits on entry).
+    cudaStream_t up_stream = nullptr;
+    cudaEvent_t up_start = nullptr, up_done = nullptr;
+    bool up_pending = false;
     SPHParams sp;
     GridParams gp, gps;
     sphk::StepParams P;
@@ -83,8 +89,12 @@ struct sph_ctx {
 // Records the message (on the context, or as the last creation error when c
 // is null) and returns code.
 int set_err(sph_ctx* c, int code, const char* fmt, ...);
-// Makes the context's device current.
-int check_ctx(sph_ctx* c);
+// Makes the context's device current and, unless join is false, orders
+// the context stream after a pending upload's side-stream copies.
+int check_ctx(sph_ctx* c, bool join = true);
+// The step's wait for a pending upload, enqueued right before cells+permute
+// (an external event wait node when the stream is being captured).
+int join_upload(sph_ctx* c);
 // Enqueues one fused step (hash .. leapfrog) on c->stream.
 int enqueue_fused_step(sph_ctx* c, float dt);
 // Reads the device counters into c->host_info (synchronises the stream).
