@@ -26,7 +26,7 @@ def test_driver_matches_python_exact():
     s.step(0.001, warm + steps)
     p = s.get("pos_u", n).astype(np.float64)
     want = 0.0
-    for q in p:  # the driver's summation order
+    for q in p:  # sph_bench's summation order
         want += q[0] + 2.0 * q[1] + 3.0 * q[2]
     assert fused["checksum"] == want
     assert frames["checksum"] == want
