@@ -49,8 +49,8 @@ FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) of one launch, from an ncu capture of the 2M step
 # (profiles/sph_density_force_2M.md); reported as roofline.traffic for the
 # dominant kernel when it is one of these.
-MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 203.5648e6 + 70.948352e6,
-                    "k_density": 70.404096e6 + 82.43968e6}
+MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 203.652864e6 + 70.948864e6,
+                    "k_density": 70.441472e6 + 82.293248e6}
 
 
 def parse():
