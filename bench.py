@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark: particle-updates/s of the 2,097,152-particle SPH dam break on GB300.
 
-One step = hash -> LSD radix sort -> cellindices+permute -> density ->
+One step = hash+count -> cell scan -> place -> rank+permute -> density ->
 force+collision+leapfrog over all particles (the fused path of sph_step,
 replayed from a CUDA graph).  The workload is the 2M-particle configuration:
 unit box, lattice spacing 2^-8, h = 2s, dt = 0.001, 1000-step rollout, seeded
@@ -147,19 +147,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def algorithmic_bytes(n, c, passes):
+def algorithmic_bytes(n, c):
     """Compulsory bytes per launch of each kernel of the step (one read of each
     input and one write of each output, physics fields only):
-      hash 24N (+4C: cell_start reset), sort 16N in all passes,
-      cellindices 4N+4C + permute 100N, density 20N+8C,
-      force 68N+8C + collision 64N + leapfrog 116N; total 412N + 24C."""
-    b = {"k_prologue": 0.0, "k_hash": 24.0 * n + 4.0 * c, "k_sort_reset": 0.0}
-    for p in range(passes):
-        b["k_radix_pass[%d]" % p] = 16.0 * n / passes
-    b["k_cells_permute"] = 104.0 * n + 4.0 * c
-    b["k_density"] = 20.0 * n + 8.0 * c
-    b["k_force(fused collision+leapfrog)"] = 248.0 * n + 8.0 * c
-    return b
+      count 24N (pos in; key, slot out), scan 12C (counts in, cell_start out,
+      counts zeroed; cell_end of the occupied cells not counted), place 16N,
+      permute 8N in + 8N (keys, indices) + 64N (pos, veleval gathered and
+      written), density 20N+8C, force 68N+8C + collision 64N + leapfrog 116N;
+      total 416N + 28C."""
+    return {"k_cell_prologue": 0.0, "k_cell_count": 24.0 * n, "k_cell_scan": 12.0 * c,
+            "k_cell_place": 16.0 * n, "k_cell_permute": 80.0 * n,
+            "k_density": 20.0 * n + 8.0 * c, "k_force(fused collision+leapfrog)": 248.0 * n + 8.0 * c}
 
 
 def cpu_baseline_port(n, seconds):
@@ -581,9 +579,8 @@ def main():
 
     steps = args.steps
     value = n * steps * world / (t_ms / 1e3)
-    passes = nk.value - 6
     c = g.nb_cells
-    ab = algorithmic_bytes(n, c, passes)
+    ab = algorithmic_bytes(n, c)
     dom = max(kern_ms, key=lambda k: kern_ms[k])
     peak, peak_kind = measured_hbm()
     achieved = ab[dom] / (kern_ms[dom] / 1e3) / 1e9

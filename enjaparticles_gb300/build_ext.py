@@ -16,7 +16,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librtps_sph.so")
 DRIVER = os.path.join(PKG, "sph_bench")
 
-SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cells.cu", "sph_density.cu", "sph_force.cu", "sph_integrate.cu",
+SOURCES = ["sph_api.cu", "sph_sort.cu", "sph_cellsort.cu", "sph_cells.cu", "sph_density.cu", "sph_force.cu", "sph_integrate.cu",
            "sph_triangles.cu", "sph_surface.cu", "sph_batch.cu", "sph_noalloc.cu", "sph_adjoint.cu", "sph_params.cpp",
            "sph_hose.cpp"]
 # Per-file flags: the density pass and the hose's host arithmetic rely on

@@ -236,7 +236,7 @@ void free_all(sph_ctx* c) {
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
                     c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
                     c->cell_start, c->cell_end, c->info, c->scratch, c->grav, c->tri, c->cf, c->cf_inv,
-                    c->mc_scan, c->mc_table, c->mesh};
+                    c->mc_scan, c->mc_table, c->mesh, c->cell_count, c->cell_status, c->cell_entries};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
@@ -284,6 +284,24 @@ int enqueue_sort(sph_ctx* c) {
     return SPH_OK;
 }
 
+// The step's sort: counting sort on the cell key up to the sorted arrays,
+// cell ranges and the gather (gather 1: pos/veleval, 2: + vel).
+int enqueue_cell_sort(sph_ctx* c, int gather) {
+    cudaStream_t st = c->stream;
+    sphk::launch_cell_prologue(c->cell_status, c->gp.nb_cells, c->info, st);
+    sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
+    sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_status, c->info, c->gp.nb_cells, st);
+    sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
+    int rc = join_upload(c);
+    if (rc) return rc;
+    sphk::launch_cell_permute(c->cell_entries, c->cell_start, c->cell_end, c->keys_a, c->idx_a, c->pos_u, c->vel_u,
+                              c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, gather, st);
+    c->keys_cur = c->keys_a;
+    c->idx_cur = c->idx_a;
+    CK_LAUNCH(c);
+    return SPH_OK;
+}
+
 // Density over the sorted arrays; with_deletion: also the fused step's
 // out-of-grid bookkeeping.
 void density_launch(sph_ctx* c, const uint32_t* idx, bool with_deletion, cudaStream_t st) {
@@ -306,12 +324,8 @@ void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t 
 // SPH::update as staged launches up to the force pass: hash, sort,
 // cellindices+permute, out-of-grid deletion, density, force.
 static int enqueue_to_force(sph_ctx* c) {
-    int rc = enqueue_hash(c);
+    int rc = enqueue_cell_sort(c, 2);
     if (rc) return rc;
-    if ((rc = enqueue_sort(c))) return rc;
-    if ((rc = join_upload(c))) return rc;
-    sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
-                               c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 2, c->stream);
     sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
                                c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
     density_launch(c, c->idx_a, false, c->stream);
@@ -342,13 +356,8 @@ int enqueue_fused_step(sph_ctx* c, float dt) {
         CK_LAUNCH(c);
         return SPH_OK;
     }
-    int rc = enqueue_hash(c);
+    int rc = enqueue_cell_sort(c, 1);
     if (rc) return rc;
-    rc = enqueue_sort(c);
-    if (rc) return rc;
-    if ((rc = join_upload(c))) return rc;
-    sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
-                               c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 1, c->stream);
     density_launch(c, c->idx_a, true, c->stream);
     force_launch(c, c->idx_a, true, dt, c->stream);
     CK_LAUNCH(c);
@@ -359,7 +368,10 @@ int read_info(sph_ctx* c) {
     CK(c, cudaMemcpyAsync(c->host_info, c->info, sizeof(int) * sphk::kInfoSlots, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     if (c->host_info[sphk::kError] & sphk::kErrLookbackTimeout) {
-        return set_err(c, SPH_ETIMEOUT, "radix sort look-back wait expired; the step result is invalid");
+        // a scan tile that gave up may have left its cell counts behind
+        CK(c, cudaMemsetAsync(c->cell_count, 0, ((size_t)c->gp.nb_cells + 1) * 4, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        return set_err(c, SPH_ETIMEOUT, "sort look-back wait expired; the step result is invalid");
     }
     return SPH_OK;
 }
@@ -463,6 +475,9 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->idx_b, N * 4);
     ALLOC(c->cell_start, C1 * 4);
     ALLOC(c->cell_end, C1 * 4);
+    ALLOC(c->cell_count, C1 * 4);
+    ALLOC(c->cell_status, (size_t)sphk::cell_scan_tiles((int)C1) * 4);
+    ALLOC(c->cell_entries, N * 8);
     ALLOC(c->info, sizeof(int) * sphk::kInfoSlots);
     // point sources: kMaxGravitySources float4 positions, then masses, then alphas
     ALLOC(c->grav, sizeof(float4) * sphk::kMaxGravitySources + 2 * sizeof(float) * sphk::kMaxGravitySources);
@@ -504,6 +519,8 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     fill_u32(c->idx_b, N, 0x7fffffffu, st);
     fill_u32(c->cell_start, C1, 666u, st);
     fill_u32(c->cell_end, C1, 666u, st);
+    cudaMemsetAsync(c->cell_count, 0, C1 * 4, st);
+    cudaMemsetAsync(c->cell_entries, 0, N * 8, st);
     cudaMemsetAsync(c->scratch, 0, c->scratch_words * 4, st);
     e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -997,39 +1014,29 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
     if (c->n_tri > 0)
         return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step; with a triangle mesh the step is staged");
     if (!c->hoses.empty()) return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step without hoses");
-    // Launches of one fused step: prologue, hash, sort reset, radix passes,
-    // cells+permute, density, force+collision+leapfrog.
-    const int nk = 6 + c->passes;
+    // Launches of one fused step: prologue, count, scan, place, permute,
+    // density, force+collision+leapfrog.
+    const int nk = 7;
     if (nkernels) *nkernels = nk;
     for (int k = 0; k < cap; ++k) kernel_ms[k] = 0.f;
-    cudaEvent_t ev[24];
+    cudaEvent_t ev[nk + 1];
     for (int k = 0; k <= nk; ++k) CK(c, cudaEventCreate(&ev[k]));
     cudaStream_t st = c->stream;
     for (int step = 0; step < nsteps && c->num_hint > 0; ++step) {
         int e = 0;
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_prologue(c->hist, c->info, st);
+        sphk::launch_cell_prologue(c->cell_status, c->gp.nb_cells, c->info, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_hash(c->pos_u, hash_keys(c), hash_idx(c), c->cell_start, c->hist, c->info, c->P, c->num_hint,
-                          c->passes, 1, st);
+        sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_sort_reset(c->status, (size_t)c->passes * c->tiles_cap * 256, c->info + sphk::kSortTiles, st);
+        sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_status, c->info, c->gp.nb_cells,
+                               st);
         CK(c, cudaEventRecord(ev[e++], st));
-        uint32_t *kin = hash_keys(c), *vin = hash_idx(c);
-        uint32_t *kout = (kin == c->keys_a) ? c->keys_b : c->keys_a, *vout = (vin == c->idx_a) ? c->idx_b : c->idx_a;
-        const int total_bits = bit_width((uint32_t)c->gp.nb_cells);
-        for (int ps = 0; ps < c->passes; ++ps) {
-            int bits = total_bits - ps * 8;
-            bits = bits > 8 ? 8 : (bits < 1 ? 1 : bits);
-            sphk::launch_radix_pass(kin, vin, kout, vout, c->info, c->hist + ps * 256,
-                                    c->status + (size_t)ps * c->tiles_cap * 256, c->info + sphk::kSortTiles + ps,
-                                    c->info + sphk::kError, ps * 8, bits, c->num_hint, st);
-            std::swap(kin, kout);
-            std::swap(vin, vout);
-            CK(c, cudaEventRecord(ev[e++], st));
-        }
-        sphk::launch_cells_permute(c->keys_a, c->idx_a, c->cell_start, c->cell_end, c->pos_u, c->vel_u, c->veleval_u,
-                                   c->pos_s, c->vel_s, c->veleval_s, c->info, c->gp.nb_cells, c->num_hint, 1, st);
+        sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        sphk::launch_cell_permute(c->cell_entries, c->cell_start, c->cell_end, c->keys_a, c->idx_a, c->pos_u,
+                                  c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, 1,
+                                  st);
         CK(c, cudaEventRecord(ev[e++], st));
         density_launch(c, c->idx_a, true, st);
         CK(c, cudaEventRecord(ev[e++], st));
@@ -1050,14 +1057,10 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
 }
 
 const char* sph_profile_kernel_name(sph_ctx* c, int k) {
-    static const char* fixed[] = {"k_prologue", "k_hash", "k_sort_reset"};
-    static const char* tail[] = {"k_cells_permute", "k_density", "k_force(fused collision+leapfrog)"};
-    static const char* pass[] = {"k_radix_pass[0]", "k_radix_pass[1]", "k_radix_pass[2]", "k_radix_pass[3]"};
-    if (!c || k < 0) return "";
-    if (k < 3) return fixed[k];
-    if (k < 3 + c->passes) return pass[k - 3];
-    k -= 3 + c->passes;
-    return k < 3 ? tail[k] : "";
+    static const char* names[] = {"k_cell_prologue", "k_cell_count", "k_cell_scan", "k_cell_place",
+                                  "k_cell_permute", "k_density", "k_force(fused collision+leapfrog)"};
+    if (!c || k < 0 || k >= 7) return "";
+    return names[k];
 }
 
 int sph_sync(sph_ctx* c) {

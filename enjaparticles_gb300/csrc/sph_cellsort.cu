@@ -1,0 +1,315 @@
+// sph_cellsort.cu — the step's sort as a counting sort on the cell key.
+//
+// The reference hashes (hash.cl:50-157), sorts the (hash, index) pairs with
+// System::bitonic_sort (System.cpp:407-480, bitonic.cl:54-258), finds the
+// cell ranges (cellindices.cl:12-107 after the cell_start reset of
+// CellIndices.cpp:58-62) and gathers the sorted arrays (permute.cl:10-46).
+// The step produces what those stages leave, in the canonical order the
+// stable radix sort of sph_sort.cu also gives (key ascending, equal keys by
+// ascending particle index), in four passes:
+//
+//   count    the cell key of each particle (hash.cl, clamped to nb_cells like
+//            k_hash) and an atomic count per cell; the count a particle's
+//            warp finds is the base of its slot in the cell.
+//   scan     an exclusive scan of the counts (one pass, decoupled look-back)
+//            writes cell_start (kEmpty for an empty cell) and cell_end of the
+//            non-empty cells, records where the out-of-grid key nb_cells
+//            starts, and zeroes the counts for the next step.
+//   place    each particle's (index, key) at cell_start[key] + slot.
+//   permute  slots within a cell come in atomic order, so each sorted
+//            position ranks its particle index among the entries of its cell
+//            and writes index, key and the gathered pos/veleval(/vel) at
+//            cell_start + rank.
+//
+// The ranking reads every entry of a cell once per entry: quadratic in the
+// occupancy of one cell, as the neighbour passes are (they walk every entry of
+// the 27 cells around a particle).  The out-of-grid key nb_cells is the one
+// cell they do not walk; a step in which k particles leave the grid together
+// spends ~k^2/32 warp iterations here.
+//
+// Counts must be zero when a step starts: zeroed at allocation, re-zeroed by
+// the scan of every step (and by the host after a look-back timeout).
+#include "sph_device.cuh"
+
+namespace sphk {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 cells per tile
+constexpr uint32_t kAgg = 1u << 30;
+constexpr uint32_t kInc = 2u << 30;
+constexpr uint32_t kVal = (1u << 30) - 1;
+constexpr int kSpinLimit = 1 << 22;
+
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+}  // namespace
+
+int cell_scan_tiles(int cells) { return (cells + kScanTile - 1) / kScanTile; }
+
+// ---------------------------------------------------------------------------
+// Prologue: apply the previous step's out-of-grid deletion to the particle
+// count; zero the scan's look-back words and its tile counter.
+__global__ void k_cell_prologue(uint32_t* __restrict__ status, int words, int* __restrict__ info) {
+    if (threadIdx.x == 0) {
+        const int out = info[kOutStart];
+        if (out >= 0) info[kNum] = out;
+        info[kOutStart] = -1;
+        info[kCellScanTile] = 0;
+    }
+    for (int k = threadIdx.x; k < words; k += blockDim.x) status[k] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Count: key and slot of every particle (original order).  Lanes of a warp
+// with the same key take consecutive slots after one atomic.
+__global__ void __launch_bounds__(256) k_cell_count(const float4* __restrict__ pos_u, uint32_t* __restrict__ key_of,
+                                                    uint32_t* __restrict__ slot_of, uint32_t* __restrict__ count,
+                                                    const int* __restrict__ info, StepParams p) {
+    const int n = info[kNum];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i & ~31) >= n) return;  // whole warps only: the match below sees 32 lanes
+    const unsigned lane = threadIdx.x & 31;
+    const bool valid = i < n;
+    uint32_t key = 0xffffffffu;  // no valid key takes this value
+    if (valid) {
+        const float4 q = ldg4(pos_u + i);
+        const int3 c = grid_cell(q.x, q.y, q.z, p.g_min, p.g_delta);
+        int h = grid_hash_f(c.x, c.y, c.z, p.g_res);
+        h = h > p.nb_cells ? p.nb_cells : h;
+        h = h < 0 ? p.nb_cells : h;
+        key = (uint32_t)h;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (valid && (int)lane == leader) base = atomicAdd(count + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (valid) {
+        key_of[i] = key;
+        slot_of[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Scan over cells [0, cells): 16 consecutive cells per thread, tiles taken in
+// launch order from a counter, warp 0 looks back 32 tiles at a time.
+__global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict__ count,
+                                                            uint32_t* __restrict__ cell_start,
+                                                            uint32_t* __restrict__ cell_end,
+                                                            uint32_t* __restrict__ status, int* __restrict__ info,
+                                                            uint32_t cells) {
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    __shared__ uint32_t s_excl;
+    __shared__ int s_tile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(info + kCellScanTile, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= (int)gridDim.x) {  // counter not reset: never index past the status words
+        if (tid == 0) atomicOr(info + kError, kErrLookbackTimeout);
+        return;
+    }
+    const uint32_t c0 = (uint32_t)tile * kScanTile + (uint32_t)tid * kScanItems;
+    // 128-bit accesses when the 16 cells are in range and both arrays are
+    // 16-byte aligned (c0 is a multiple of 16 cells; a recorded rollout's
+    // cell arrays are packed at a stride of nb_cells + 1 words, so their base
+    // need not be)
+    const bool vec = c0 + kScanItems <= cells &&
+                     ((reinterpret_cast<uintptr_t>(count) | reinterpret_cast<uintptr_t>(cell_start)) & 15u) == 0;
+    uint32_t v[kScanItems];
+    if (vec) {
+        const uint4* q = reinterpret_cast<const uint4*>(count + c0);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            const uint4 w = q[k];
+            v[4 * k] = w.x;
+            v[4 * k + 1] = w.y;
+            v[4 * k + 2] = w.z;
+            v[4 * k + 3] = w.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = c0 + k < cells ? count[c0 + k] : 0u;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    // block-wide exclusive scan of the thread sums
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t wbefore = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) {
+        const uint32_t t = s_warp[w];
+        wbefore += w < warp ? t : 0u;
+        total += t;
+    }
+    const uint32_t texcl = wbefore + x - sum;
+    // decoupled look-back (bounded spin)
+    if (warp == 0) {
+        uint32_t excl = 0;
+        if (tile == 0) {
+            if (lane == 0) st_relaxed_u32(status, kInc | total);
+        } else {
+            if (lane == 0) st_relaxed_u32(status + tile, kAgg | total);
+            int top = tile - 1;
+            int spins = 0;
+            while (true) {
+                const int t = top - lane;
+                const uint32_t s = t >= 0 ? ld_relaxed_u32(status + t) : kInc;
+                const uint32_t flag = s & ~kVal;
+                const unsigned inc = __ballot_sync(0xffffffffu, flag == kInc);
+                const unsigned none = __ballot_sync(0xffffffffu, flag == 0);
+                const int first = inc ? __ffs(inc) - 1 : 31;  // the lanes that count: 0..first
+                const unsigned upto = first == 31 ? 0xffffffffu : ((2u << first) - 1u);
+                if (none & upto) {
+                    if (++spins > kSpinLimit) {
+                        if (lane == 0) atomicOr(info + kError, kErrLookbackTimeout);
+                        break;
+                    }
+                    continue;
+                }
+                uint32_t a = (unsigned)lane <= (unsigned)first ? (s & kVal) : 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+                excl += a;
+                if (inc) break;
+                top -= 32;
+            }
+            if (lane == 0) st_relaxed_u32(status + tile, kInc | (excl + total));
+        }
+        if (lane == 0) s_excl = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_excl + texcl;
+    uint32_t st[kScanItems];
+    const uint32_t last = cells - 1;  // the out-of-grid key
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        st[k] = v[k] ? run : kEmpty;
+        if (v[k]) {
+            cell_end[c0 + k] = run + v[k];
+            if (c0 + k == last) info[kOutStart] = (int)run;
+        }
+        run += v[k];
+    }
+    if (vec) {
+        uint4* s4 = reinterpret_cast<uint4*>(cell_start + c0);
+        uint4* z4 = reinterpret_cast<uint4*>(count + c0);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            s4[k] = make_uint4(st[4 * k], st[4 * k + 1], st[4 * k + 2], st[4 * k + 3]);
+            z4[k] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            if (c0 + k < cells) {
+                cell_start[c0 + k] = st[k];
+                count[c0 + k] = 0u;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Place: (index, key) of particle i at its cell's start + its slot.
+__global__ void __launch_bounds__(256) k_cell_place(const uint32_t* __restrict__ key_of,
+                                                    const uint32_t* __restrict__ slot_of,
+                                                    const uint32_t* __restrict__ cell_start,
+                                                    uint2* __restrict__ entries, const int* __restrict__ info) {
+    const int n = info[kNum];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t key = __ldg(key_of + i);
+    entries[__ldg(cell_start + key) + __ldg(slot_of + i)] = make_uint2((uint32_t)i, key);
+}
+
+// ---------------------------------------------------------------------------
+// Permute: rank within the cell, then the sorted arrays.
+// Gather: 1 = pos/veleval, 2 = pos/vel/veleval.
+template <int Gather>
+__global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ entries,
+                                                      const uint32_t* __restrict__ cell_start,
+                                                      const uint32_t* __restrict__ cell_end,
+                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ idx,
+                                                      const float4* __restrict__ pos_u,
+                                                      const float4* __restrict__ vel_u,
+                                                      const float4* __restrict__ veleval_u,
+                                                      float4* __restrict__ pos_s, float4* __restrict__ vel_s,
+                                                      float4* __restrict__ veleval_s, const int* __restrict__ info) {
+    const int n = info[kNum];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint2 e = __ldg(entries + s);
+    const uint32_t id = e.x, key = e.y;
+    const uint32_t cs = __ldg(cell_start + key), ce = __ldg(cell_end + key);
+    // every entry lies in a cell of [cs, ce) within [0, n) unless a scan tile
+    // gave up its look-back (flagged in info): then write nothing
+    if (cs >= ce || ce > (uint32_t)n) return;
+    const uint32_t* ids = reinterpret_cast<const uint32_t*>(entries);
+    uint32_t rank = 0;
+    for (uint32_t t = cs; t < ce; ++t) rank += __ldg(ids + 2 * t) < id ? 1u : 0u;
+    const uint32_t p = cs + rank;
+    keys[s] = key;  // one key over the whole cell
+    idx[p] = id;
+    pos_s[p] = __ldg(pos_u + id);
+    veleval_s[p] = __ldg(veleval_u + id);
+    if (Gather == 2) vel_s[p] = __ldg(vel_u + id);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers, one per pass (the step profile times each).
+void launch_cell_prologue(uint32_t* status, int nb_cells, int* info, cudaStream_t st) {
+    k_cell_prologue<<<1, 256, 0, st>>>(status, cell_scan_tiles(nb_cells + 1), info);
+}
+
+void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of, uint32_t* count, const int* info,
+                       const StepParams& p, int grid_items, cudaStream_t st) {
+    const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
+    k_cell_count<<<blocks, 256, 0, st>>>(pos_u, key_of, slot_of, count, info, p);
+}
+
+void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* status, int* info,
+                      int nb_cells, cudaStream_t st) {
+    const uint32_t cells = (uint32_t)nb_cells + 1u;
+    k_cell_scan<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, cell_start, cell_end, status, info,
+                                                                       cells);
+}
+
+void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
+                       const int* info, int grid_items, cudaStream_t st) {
+    const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
+    k_cell_place<<<blocks, 256, 0, st>>>(key_of, slot_of, cell_start, entries, info);
+}
+
+void launch_cell_permute(const uint2* entries, const uint32_t* cell_start, const uint32_t* cell_end, uint32_t* keys,
+                         uint32_t* idx, const float4* pos_u, const float4* vel_u, const float4* veleval_u,
+                         float4* pos_s, float4* vel_s, float4* veleval_s, const int* info, int grid_items, int gather,
+                         cudaStream_t st) {
+    const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
+    if (gather == 2)
+        k_cell_permute<2><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
+                                                  pos_s, vel_s, veleval_s, info);
+    else
+        k_cell_permute<1><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
+                                                  pos_s, vel_s, veleval_s, info);
+}
+
+}  // namespace sphk

@@ -46,6 +46,11 @@ struct sph_ctx {
     uint32_t* hist = nullptr;    // [4][256]
     uint32_t* status = nullptr;  // [passes][tiles][256]
     int tiles_cap = 0;
+    // counting sort of the step (sph_cellsort.cu): particles per cell (zero
+    // between steps), the scan's look-back words, (index, key) per slot
+    uint32_t* cell_count = nullptr;
+    uint32_t* cell_status = nullptr;
+    uint2* cell_entries = nullptr;
     int* host_info = nullptr;  // pinned
     // When set, the fused step also stores, per sorted particle, the SPH
     // force before the walls (keep_f) and the step's input velocity (keep_v):

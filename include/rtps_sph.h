@@ -381,9 +381,10 @@ int sph_update(sph_ctx* ctx);
 /* SPH::integrate (SPH.cpp:389-441): the integrator sph_set_integrator chose. */
 int sph_integrate(sph_ctx* ctx, float dt);
 
-/* nsteps x (update + integrate) on the fused path: hash -> sort ->
- * cellindices+permute -> density -> force+gravity+collision+integrator, replayed from a
- * captured CUDA graph.  With a triangle mesh loaded the graph holds the
+/* nsteps x (update + integrate) on the fused path: hash and sort (a counting
+ * sort on the cell key, with the same canonical order as sph_stage_sort) ->
+ * cellindices+permute -> density -> force+gravity+collision+integrator,
+ * replayed from a captured CUDA graph.  With a triangle mesh loaded the graph holds the
  * staged launches of update + integrate instead.  Results equal nsteps staged
  * update()+integrate() calls.  Asynchronous. */
 int sph_step(sph_ctx* ctx, float dt, int nsteps);
