@@ -236,7 +236,7 @@ void free_all(sph_ctx* c) {
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
                     c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
                     c->cell_start, c->cell_end, c->info, c->scratch, c->grav, c->tri, c->cf, c->cf_inv,
-                    c->mc_scan, c->mc_table, c->mesh, c->cell_count, c->cell_status, c->cell_entries};
+                    c->mc_scan, c->mc_table, c->mesh, c->cell_count, c->cell_tile_total, c->cell_entries};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
@@ -288,9 +288,9 @@ int enqueue_sort(sph_ctx* c) {
 // cell ranges and the gather (gather 1: pos/veleval, 2: + vel).
 int enqueue_cell_sort(sph_ctx* c, int gather) {
     cudaStream_t st = c->stream;
-    sphk::launch_cell_prologue(c->cell_status, c->gp.nb_cells, c->info, st);
+    sphk::launch_cell_prologue(c->cell_tile_total, c->gp.nb_cells, c->info, st);
     sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
-    sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_status, c->info, c->gp.nb_cells, st);
+    sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, c->gp.nb_cells, st);
     sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
     int rc = join_upload(c);
     if (rc) return rc;
@@ -368,9 +368,6 @@ int read_info(sph_ctx* c) {
     CK(c, cudaMemcpyAsync(c->host_info, c->info, sizeof(int) * sphk::kInfoSlots, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     if (c->host_info[sphk::kError] & sphk::kErrLookbackTimeout) {
-        // a scan tile that gave up may have left its cell counts behind
-        CK(c, cudaMemsetAsync(c->cell_count, 0, ((size_t)c->gp.nb_cells + 1) * 4, c->stream));
-        CK(c, cudaStreamSynchronize(c->stream));
         return set_err(c, SPH_ETIMEOUT, "sort look-back wait expired; the step result is invalid");
     }
     return SPH_OK;
@@ -476,7 +473,7 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->cell_start, C1 * 4);
     ALLOC(c->cell_end, C1 * 4);
     ALLOC(c->cell_count, C1 * 4);
-    ALLOC(c->cell_status, (size_t)sphk::cell_scan_tiles((int)C1) * 4);
+    ALLOC(c->cell_tile_total, (size_t)sphk::cell_scan_tiles((int)C1) * 4);
     ALLOC(c->cell_entries, N * 8);
     ALLOC(c->info, sizeof(int) * sphk::kInfoSlots);
     // point sources: kMaxGravitySources float4 positions, then masses, then alphas
@@ -1025,11 +1022,11 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
     for (int step = 0; step < nsteps && c->num_hint > 0; ++step) {
         int e = 0;
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_cell_prologue(c->cell_status, c->gp.nb_cells, c->info, st);
+        sphk::launch_cell_prologue(c->cell_tile_total, c->gp.nb_cells, c->info, st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_status, c->info, c->gp.nb_cells,
+        sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, c->gp.nb_cells,
                                st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);

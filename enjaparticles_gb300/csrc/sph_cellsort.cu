@@ -11,8 +11,11 @@
 //   count    the cell key of each particle (hash.cl, clamped to nb_cells like
 //            k_hash) and an atomic count per cell; the count a particle's
 //            warp finds is the base of its slot in the cell.
-//   scan     an exclusive scan of the counts (one pass, decoupled look-back)
-//            writes cell_start (kEmpty for an empty cell) and cell_end of the
+//   scan     an exclusive scan of the counts in tiles of 4096 cells, taken in
+//            launch order: a block publishes its tile's total, reads the
+//            totals of all earlier tiles at once (each published by a block
+//            that is already running and waits on nobody), and writes
+//            cell_start (kEmpty for an empty cell) and cell_end of the
 //            non-empty cells, records where the out-of-grid key nb_cells
 //            starts, and zeroes the counts for the next step.
 //   place    each particle's (index, key) at cell_start[key] + slot.
@@ -27,8 +30,10 @@
 // cell they do not walk; a step in which k particles leave the grid together
 // spends ~k^2/32 warp iterations here.
 //
-// Counts must be zero when a step starts: zeroed at allocation, re-zeroed by
-// the scan of every step (and by the host after a look-back timeout).
+// Counts must be zero when a step starts: zeroed at allocation and re-zeroed
+// by the scan of every step; the prologue zeroes the tile totals.  A wait for
+// a tile total is bounded: when it runs out the step sets
+// kErrLookbackTimeout and the permute writes nothing outside a cell.
 #include "sph_device.cuh"
 
 namespace sphk {
@@ -38,10 +43,9 @@ namespace {
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 cells per tile
-constexpr uint32_t kAgg = 1u << 30;
-constexpr uint32_t kInc = 2u << 30;
-constexpr uint32_t kVal = (1u << 30) - 1;
-constexpr int kSpinLimit = 1 << 22;
+constexpr int kItems = 4;                               // particles per thread in count and place
+constexpr uint32_t kPublished = 1u << 31;               // tile total word: flag | total
+constexpr int kSpinLimit = 1 << 20;
 
 __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
     uint32_t v;
@@ -58,64 +62,83 @@ int cell_scan_tiles(int cells) { return (cells + kScanTile - 1) / kScanTile; }
 
 // ---------------------------------------------------------------------------
 // Prologue: apply the previous step's out-of-grid deletion to the particle
-// count; zero the scan's look-back words and its tile counter.
-__global__ void k_cell_prologue(uint32_t* __restrict__ status, int words, int* __restrict__ info) {
+// count; zero the tile totals and the scan's tile counter.
+__global__ void k_cell_prologue(uint32_t* __restrict__ tile_total, int tiles, int* __restrict__ info) {
     if (threadIdx.x == 0) {
         const int out = info[kOutStart];
         if (out >= 0) info[kNum] = out;
         info[kOutStart] = -1;
         info[kCellScanTile] = 0;
     }
-    for (int k = threadIdx.x; k < words; k += blockDim.x) status[k] = 0;
+    for (int k = threadIdx.x; k < tiles; k += blockDim.x) tile_total[k] = 0;
 }
 
 // ---------------------------------------------------------------------------
-// Count: key and slot of every particle (original order).  Lanes of a warp
-// with the same key take consecutive slots after one atomic.
+// Count: key and slot of every particle (original order).  A warp takes 4
+// runs of 32 consecutive particles, all loads and atomics of the 4 in flight
+// together.  Lanes with the same key take consecutive slots after one atomic.
 __global__ void __launch_bounds__(256) k_cell_count(const float4* __restrict__ pos_u, uint32_t* __restrict__ key_of,
                                                     uint32_t* __restrict__ slot_of, uint32_t* __restrict__ count,
                                                     const int* __restrict__ info, StepParams p) {
     const int n = info[kNum];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if ((i & ~31) >= n) return;  // whole warps only: the match below sees 32 lanes
     const unsigned lane = threadIdx.x & 31;
-    const bool valid = i < n;
-    uint32_t key = 0xffffffffu;  // no valid key takes this value
-    if (valid) {
-        const float4 q = ldg4(pos_u + i);
-        const int3 c = grid_cell(q.x, q.y, q.z, p.g_min, p.g_delta);
-        int h = grid_hash_f(c.x, c.y, c.z, p.g_res);
-        h = h > p.nb_cells ? p.nb_cells : h;
-        h = h < 0 ? p.nb_cells : h;
-        key = (uint32_t)h;
+    const int wb = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) * kItems;  // first particle of the warp
+    if (wb >= n) return;
+    uint32_t key[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int i = wb + 32 * k + (int)lane;
+        key[k] = 0xffffffffu;  // no valid key takes this value
+        if (i < n) {
+            const float4 q = ldg4(pos_u + i);
+            const int3 c = grid_cell(q.x, q.y, q.z, p.g_min, p.g_delta);
+            int h = grid_hash_f(c.x, c.y, c.z, p.g_res);
+            h = h > p.nb_cells ? p.nb_cells : h;
+            h = h < 0 ? p.nb_cells : h;
+            key[k] = (uint32_t)h;
+        }
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    const int leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (valid && (int)lane == leader) base = atomicAdd(count + key, (uint32_t)__popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (valid) {
-        key_of[i] = key;
-        slot_of[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    uint32_t base[kItems];
+    unsigned peers[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        base[k] = 0;
+        peers[k] = 0;
+        if (wb + 32 * k < n) {  // warp-uniform: every lane takes part in the matches
+            const bool valid = key[k] != 0xffffffffu;
+            peers[k] = __match_any_sync(0xffffffffu, key[k]);
+            if (valid && (int)lane == __ffs(peers[k]) - 1)
+                base[k] = atomicAdd(count + key[k], (uint32_t)__popc(peers[k]));
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        if (wb + 32 * k < n) {
+            const uint32_t b = __shfl_sync(0xffffffffu, base[k], __ffs(peers[k]) - 1);
+            const int i = wb + 32 * k + (int)lane;
+            if (i < n) {
+                key_of[i] = key[k];
+                slot_of[i] = b + (uint32_t)__popc(peers[k] & ((1u << lane) - 1u));
+            }
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Scan over cells [0, cells): 16 consecutive cells per thread, tiles taken in
-// launch order from a counter, warp 0 looks back 32 tiles at a time.
+// Scan over cells [0, cells): 16 consecutive cells per thread.
 __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict__ count,
                                                             uint32_t* __restrict__ cell_start,
                                                             uint32_t* __restrict__ cell_end,
-                                                            uint32_t* __restrict__ status, int* __restrict__ info,
-                                                            uint32_t cells) {
+                                                            uint32_t* __restrict__ tile_total,
+                                                            int* __restrict__ info, uint32_t cells) {
     __shared__ uint32_t s_warp[kScanThreads / 32];
-    __shared__ uint32_t s_excl;
+    __shared__ uint32_t s_base[kScanThreads / 32];
     __shared__ int s_tile;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(info + kCellScanTile, 1);
     __syncthreads();
     const int tile = s_tile;
-    if (tile >= (int)gridDim.x) {  // counter not reset: never index past the status words
+    if (tile >= (int)gridDim.x) {  // counter not reset: never index past the tile totals
         if (tid == 0) atomicOr(info + kError, kErrLookbackTimeout);
         return;
     }
@@ -161,43 +184,25 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict
         total += t;
     }
     const uint32_t texcl = wbefore + x - sum;
-    // decoupled look-back (bounded spin)
-    if (warp == 0) {
-        uint32_t excl = 0;
-        if (tile == 0) {
-            if (lane == 0) st_relaxed_u32(status, kInc | total);
-        } else {
-            if (lane == 0) st_relaxed_u32(status + tile, kAgg | total);
-            int top = tile - 1;
-            int spins = 0;
-            while (true) {
-                const int t = top - lane;
-                const uint32_t s = t >= 0 ? ld_relaxed_u32(status + t) : kInc;
-                const uint32_t flag = s & ~kVal;
-                const unsigned inc = __ballot_sync(0xffffffffu, flag == kInc);
-                const unsigned none = __ballot_sync(0xffffffffu, flag == 0);
-                const int first = inc ? __ffs(inc) - 1 : 31;  // the lanes that count: 0..first
-                const unsigned upto = first == 31 ? 0xffffffffu : ((2u << first) - 1u);
-                if (none & upto) {
-                    if (++spins > kSpinLimit) {
-                        if (lane == 0) atomicOr(info + kError, kErrLookbackTimeout);
-                        break;
-                    }
-                    continue;
-                }
-                uint32_t a = (unsigned)lane <= (unsigned)first ? (s & kVal) : 0u;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-                excl += a;
-                if (inc) break;
-                top -= 32;
-            }
-            if (lane == 0) st_relaxed_u32(status + tile, kInc | (excl + total));
-        }
-        if (lane == 0) s_excl = excl;
+    if (tid == 0) st_relaxed_u32(tile_total + tile, kPublished | total);
+    // the totals of tiles 0..tile-1, all read at once (bounded waits)
+    uint32_t before = 0;
+    bool late = false;
+    for (int t = tid; t < tile; t += kScanThreads) {
+        uint32_t w = ld_relaxed_u32(tile_total + t);
+        for (int spins = 0; !(w & kPublished) && spins < kSpinLimit; ++spins) w = ld_relaxed_u32(tile_total + t);
+        late |= !(w & kPublished);
+        before += w & ~kPublished;
     }
+    if (late) atomicOr(info + kError, kErrLookbackTimeout);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    if (lane == 0) s_base[warp] = before;
     __syncthreads();
-    uint32_t run = s_excl + texcl;
+    uint32_t tbase = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) tbase += s_base[w];
+    uint32_t run = tbase + texcl;
     uint32_t st[kScanItems];
     const uint32_t last = cells - 1;  // the out-of-grid key
 #pragma unroll
@@ -229,16 +234,28 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Place: (index, key) of particle i at its cell's start + its slot.
+// Place: (index, key) of particle i at its cell's start + its slot; 4
+// particles per thread, loads in flight together.
 __global__ void __launch_bounds__(256) k_cell_place(const uint32_t* __restrict__ key_of,
                                                     const uint32_t* __restrict__ slot_of,
                                                     const uint32_t* __restrict__ cell_start,
                                                     uint2* __restrict__ entries, const int* __restrict__ info) {
     const int n = info[kNum];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t key = __ldg(key_of + i);
-    entries[__ldg(cell_start + key) + __ldg(slot_of + i)] = make_uint2((uint32_t)i, key);
+    const int i0 = blockIdx.x * (blockDim.x * kItems) + threadIdx.x;
+    uint32_t key[kItems], slot[kItems], cs[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int i = i0 + k * (int)blockDim.x;
+        key[k] = i < n ? __ldg(key_of + i) : 0u;
+        slot[k] = i < n ? __ldg(slot_of + i) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) cs[k] = i0 + k * (int)blockDim.x < n ? __ldg(cell_start + key[k]) : 0u;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int i = i0 + k * (int)blockDim.x;
+        if (i < n) entries[cs[k] + slot[k]] = make_uint2((uint32_t)i, key[k]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -259,9 +276,14 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
     if (s >= n) return;
     const uint2 e = __ldg(entries + s);
     const uint32_t id = e.x, key = e.y;
+    // the gathers do not depend on the rank: in flight during the ranking
+    const float4 pq = __ldg(pos_u + id);
+    const float4 vq = __ldg(veleval_u + id);
+    float4 wq = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (Gather == 2) wq = __ldg(vel_u + id);
     const uint32_t cs = __ldg(cell_start + key), ce = __ldg(cell_end + key);
-    // every entry lies in a cell of [cs, ce) within [0, n) unless a scan tile
-    // gave up its look-back (flagged in info): then write nothing
+    // every entry lies in a cell of [cs, ce) within [0, n) when the counts
+    // were zero at the start of the step; never write outside it
     if (cs >= ce || ce > (uint32_t)n) return;
     const uint32_t* ids = reinterpret_cast<const uint32_t*>(entries);
     uint32_t rank = 0;
@@ -269,33 +291,35 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
     const uint32_t p = cs + rank;
     keys[s] = key;  // one key over the whole cell
     idx[p] = id;
-    pos_s[p] = __ldg(pos_u + id);
-    veleval_s[p] = __ldg(veleval_u + id);
-    if (Gather == 2) vel_s[p] = __ldg(vel_u + id);
+    pos_s[p] = pq;
+    veleval_s[p] = vq;
+    if (Gather == 2) vel_s[p] = wq;
 }
 
 // ---------------------------------------------------------------------------
 // Launchers, one per pass (the step profile times each).
-void launch_cell_prologue(uint32_t* status, int nb_cells, int* info, cudaStream_t st) {
-    k_cell_prologue<<<1, 256, 0, st>>>(status, cell_scan_tiles(nb_cells + 1), info);
+void launch_cell_prologue(uint32_t* tile_total, int nb_cells, int* info, cudaStream_t st) {
+    k_cell_prologue<<<1, 256, 0, st>>>(tile_total, cell_scan_tiles(nb_cells + 1), info);
 }
 
 void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of, uint32_t* count, const int* info,
                        const StepParams& p, int grid_items, cudaStream_t st) {
-    const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
+    const int per = 256 * kItems;
+    const int blocks = grid_items > 0 ? (grid_items + per - 1) / per : 1;
     k_cell_count<<<blocks, 256, 0, st>>>(pos_u, key_of, slot_of, count, info, p);
 }
 
-void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* status, int* info,
-                      int nb_cells, cudaStream_t st) {
+void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total,
+                      int* info, int nb_cells, cudaStream_t st) {
     const uint32_t cells = (uint32_t)nb_cells + 1u;
-    k_cell_scan<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, cell_start, cell_end, status, info,
+    k_cell_scan<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, cell_start, cell_end, tile_total, info,
                                                                        cells);
 }
 
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
                        const int* info, int grid_items, cudaStream_t st) {
-    const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
+    const int per = 256 * kItems;
+    const int blocks = grid_items > 0 ? (grid_items + per - 1) / per : 1;
     k_cell_place<<<blocks, 256, 0, st>>>(key_of, slot_of, cell_start, entries, info);
 }
 

@@ -47,9 +47,9 @@ struct sph_ctx {
     uint32_t* status = nullptr;  // [passes][tiles][256]
     int tiles_cap = 0;
     // counting sort of the step (sph_cellsort.cu): particles per cell (zero
-    // between steps), the scan's look-back words, (index, key) per slot
+    // between steps), particles per tile of 4096 cells, (index, key) per slot
     uint32_t* cell_count = nullptr;
-    uint32_t* cell_status = nullptr;
+    uint32_t* cell_tile_total = nullptr;
     uint2* cell_entries = nullptr;
     int* host_info = nullptr;  // pinned
     // When set, the fused step also stores, per sorted particle, the SPH

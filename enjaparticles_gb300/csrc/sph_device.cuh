@@ -150,10 +150,10 @@ int radix_tiles(int n);
 // Counting sort on the cell key (sph_cellsort.cu): prologue, count, scan,
 // place, then permute (which reads veleval_u/vel_u: after any upload join).
 int cell_scan_tiles(int cells);
-void launch_cell_prologue(uint32_t* status, int nb_cells, int* info, cudaStream_t st);
+void launch_cell_prologue(uint32_t* tile_total, int nb_cells, int* info, cudaStream_t st);
 void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of, uint32_t* count, const int* info,
                        const StepParams& p, int grid_items, cudaStream_t st);
-void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* status, int* info,
+void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
                       int nb_cells, cudaStream_t st);
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
                        const int* info, int grid_items, cudaStream_t st);
