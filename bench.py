@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark: particle-updates/s of the 2,097,152-particle SPH dam break on GB300.
 
-One step = hash+count -> cell scan -> place -> rank+permute -> density ->
+One step = hash+count -> tile totals -> cell scan -> place -> rank+permute -> density ->
 force+collision+leapfrog over all particles (the fused path of sph_step,
 replayed from a CUDA graph).  The workload is the 2M-particle configuration:
 unit box, lattice spacing 2^-8, h = 2s, dt = 0.001, 1000-step rollout, seeded
@@ -150,12 +150,13 @@ class ClockSampler:
 def algorithmic_bytes(n, c):
     """Compulsory bytes per launch of each kernel of the step (one read of each
     input and one write of each output, physics fields only):
-      count 24N (pos in; key, slot out), scan 12C (counts in, cell_start out,
-      counts zeroed; cell_end of the occupied cells not counted), place 16N,
+      count 24N (pos in; key, slot out), totals 4C, scan 12C (counts in,
+      cell_start out, counts zeroed; cell_end of the occupied cells not
+      counted), place 16N,
       permute 8N in + 8N (keys, indices) + 64N (pos, veleval gathered and
       written), density 20N+8C, force 68N+8C + collision 64N + leapfrog 116N;
-      total 416N + 28C."""
-    return {"k_cell_prologue": 0.0, "k_cell_count": 24.0 * n, "k_cell_scan": 12.0 * c,
+      total 416N + 32C."""
+    return {"k_cell_count": 24.0 * n, "k_cell_totals": 4.0 * c, "k_cell_scan": 12.0 * c,
             "k_cell_place": 16.0 * n, "k_cell_permute": 80.0 * n,
             "k_density": 20.0 * n + 8.0 * c, "k_force(fused collision+leapfrog)": 248.0 * n + 8.0 * c}
 

@@ -288,8 +288,8 @@ int enqueue_sort(sph_ctx* c) {
 // cell ranges and the gather (gather 1: pos/veleval, 2: + vel).
 int enqueue_cell_sort(sph_ctx* c, int gather) {
     cudaStream_t st = c->stream;
-    sphk::launch_cell_prologue(c->cell_tile_total, c->gp.nb_cells, c->info, st);
     sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
+    sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, c->gp.nb_cells, st);
     sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, c->gp.nb_cells, st);
     sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
     int rc = join_upload(c);
@@ -1011,7 +1011,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
     if (c->n_tri > 0)
         return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step; with a triangle mesh the step is staged");
     if (!c->hoses.empty()) return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step without hoses");
-    // Launches of one fused step: prologue, count, scan, place, permute,
+    // Launches of one fused step: count, totals, scan, place, permute,
     // density, force+collision+leapfrog.
     const int nk = 7;
     if (nkernels) *nkernels = nk;
@@ -1022,9 +1022,9 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
     for (int step = 0; step < nsteps && c->num_hint > 0; ++step) {
         int e = 0;
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_cell_prologue(c->cell_tile_total, c->gp.nb_cells, c->info, st);
-        CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, c->gp.nb_cells, st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, c->gp.nb_cells,
                                st);
@@ -1054,7 +1054,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
 }
 
 const char* sph_profile_kernel_name(sph_ctx* c, int k) {
-    static const char* names[] = {"k_cell_prologue", "k_cell_count", "k_cell_scan", "k_cell_place",
+    static const char* names[] = {"k_cell_count", "k_cell_totals", "k_cell_scan", "k_cell_place",
                                   "k_cell_permute", "k_density", "k_force(fused collision+leapfrog)"};
     if (!c || k < 0 || k >= 7) return "";
     return names[k];

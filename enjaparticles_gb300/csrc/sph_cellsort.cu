@@ -6,18 +6,19 @@
 // CellIndices.cpp:58-62) and gathers the sorted arrays (permute.cl:10-46).
 // The step produces what those stages leave, in the canonical order the
 // stable radix sort of sph_sort.cu also gives (key ascending, equal keys by
-// ascending particle index), in four passes:
+// ascending particle index), in five passes:
 //
 //   count    the cell key of each particle (hash.cl, clamped to nb_cells like
-//            k_hash) and an atomic count per cell; the count a particle's
-//            warp finds is the base of its slot in the cell.
-//   scan     an exclusive scan of the counts in tiles of 4096 cells, taken in
-//            launch order: a block publishes its tile's total, reads the
-//            totals of all earlier tiles at once (each published by a block
-//            that is already running and waits on nobody), and writes
-//            cell_start (kEmpty for an empty cell) and cell_end of the
-//            non-empty cells, records where the out-of-grid key nb_cells
-//            starts, and zeroes the counts for the next step.
+//            k_hash) and an atomic count per cell; the count a particle finds
+//            is its slot in the cell.
+//   totals   the number of particles in each tile of 4096 cells; the first
+//            thread also applies the previous step's out-of-grid deletion to
+//            the particle count (count derives the same number on its own).
+//   scan     an exclusive scan of the counts, one block per tile, its base the
+//            sum of the totals of the tiles before it (no block waits on
+//            another), writes cell_start (kEmpty for an empty cell) and
+//            cell_end of the non-empty cells, records where the out-of-grid
+//            key nb_cells starts, and zeroes the counts for the next step.
 //   place    each particle's (index, key) at cell_start[key] + slot.
 //   permute  slots within a cell come in atomic order, so each sorted
 //            position ranks its particle index among the entries of its cell
@@ -31,9 +32,7 @@
 // spends ~k^2/32 warp iterations here.
 //
 // Counts must be zero when a step starts: zeroed at allocation and re-zeroed
-// by the scan of every step; the prologue zeroes the tile totals.  A wait for
-// a tile total is bounded: when it runs out the step sets
-// kErrLookbackTimeout and the permute writes nothing outside a cell.
+// by the scan of every step.
 #include "sph_device.cuh"
 
 namespace sphk {
@@ -44,46 +43,23 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 cells per tile
 constexpr int kItems = 4;                               // particles per thread in count and place
-constexpr uint32_t kPublished = 1u << 31;               // tile total word: flag | total
-constexpr int kSpinLimit = 1 << 20;
-
-__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
-    uint32_t v;
-    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
-    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 }  // namespace
 
 int cell_scan_tiles(int cells) { return (cells + kScanTile - 1) / kScanTile; }
 
 // ---------------------------------------------------------------------------
-// Prologue: apply the previous step's out-of-grid deletion to the particle
-// count; zero the tile totals and the scan's tile counter.
-__global__ void k_cell_prologue(uint32_t* __restrict__ tile_total, int tiles, int* __restrict__ info) {
-    if (threadIdx.x == 0) {
-        const int out = info[kOutStart];
-        if (out >= 0) info[kNum] = out;
-        info[kOutStart] = -1;
-        info[kCellScanTile] = 0;
-    }
-    for (int k = threadIdx.x; k < tiles; k += blockDim.x) tile_total[k] = 0;
-}
-
-// ---------------------------------------------------------------------------
 // Count: key and slot of every particle (original order).  A warp takes 4
 // runs of 32 consecutive particles, all loads and atomics of the 4 in flight
-// together.  Lanes with the same key take consecutive slots after one atomic.
+// together.  The particle count is the previous step's after its out-of-grid
+// deletion (k_cell_totals stores it once this pass is done).
 __global__ void __launch_bounds__(256) k_cell_count(const float4* __restrict__ pos_u, uint32_t* __restrict__ key_of,
                                                     uint32_t* __restrict__ slot_of, uint32_t* __restrict__ count,
                                                     const int* __restrict__ info, StepParams p) {
-    const int n = info[kNum];
+    const int out = info[kOutStart];
+    const int n = out >= 0 ? out : info[kNum];
     const unsigned lane = threadIdx.x & 31;
     const int wb = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) * kItems;  // first particle of the warp
-    if (wb >= n) return;
     uint32_t key[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
@@ -98,58 +74,24 @@ __global__ void __launch_bounds__(256) k_cell_count(const float4* __restrict__ p
             key[k] = (uint32_t)h;
         }
     }
-    uint32_t base[kItems];
-    unsigned peers[kItems];
+    uint32_t slot[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) slot[k] = key[k] != 0xffffffffu ? atomicAdd(count + key[k], 1u) : 0u;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        base[k] = 0;
-        peers[k] = 0;
-        if (wb + 32 * k < n) {  // warp-uniform: every lane takes part in the matches
-            const bool valid = key[k] != 0xffffffffu;
-            peers[k] = __match_any_sync(0xffffffffu, key[k]);
-            if (valid && (int)lane == __ffs(peers[k]) - 1)
-                base[k] = atomicAdd(count + key[k], (uint32_t)__popc(peers[k]));
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < kItems; ++k) {
-        if (wb + 32 * k < n) {
-            const uint32_t b = __shfl_sync(0xffffffffu, base[k], __ffs(peers[k]) - 1);
-            const int i = wb + 32 * k + (int)lane;
-            if (i < n) {
-                key_of[i] = key[k];
-                slot_of[i] = b + (uint32_t)__popc(peers[k] & ((1u << lane) - 1u));
-            }
+        const int i = wb + 32 * k + (int)lane;
+        if (i < n) {
+            key_of[i] = key[k];
+            slot_of[i] = slot[k];
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Scan over cells [0, cells): 16 consecutive cells per thread.
-__global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict__ count,
-                                                            uint32_t* __restrict__ cell_start,
-                                                            uint32_t* __restrict__ cell_end,
-                                                            uint32_t* __restrict__ tile_total,
-                                                            int* __restrict__ info, uint32_t cells) {
-    __shared__ uint32_t s_warp[kScanThreads / 32];
-    __shared__ uint32_t s_base[kScanThreads / 32];
-    __shared__ int s_tile;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_tile = atomicAdd(info + kCellScanTile, 1);
-    __syncthreads();
-    const int tile = s_tile;
-    if (tile >= (int)gridDim.x) {  // counter not reset: never index past the tile totals
-        if (tid == 0) atomicOr(info + kError, kErrLookbackTimeout);
-        return;
-    }
-    const uint32_t c0 = (uint32_t)tile * kScanTile + (uint32_t)tid * kScanItems;
-    // 128-bit accesses when the 16 cells are in range and both arrays are
-    // 16-byte aligned (c0 is a multiple of 16 cells; a recorded rollout's
-    // cell arrays are packed at a stride of nb_cells + 1 words, so their base
-    // need not be)
-    const bool vec = c0 + kScanItems <= cells &&
-                     ((reinterpret_cast<uintptr_t>(count) | reinterpret_cast<uintptr_t>(cell_start)) & 15u) == 0;
-    uint32_t v[kScanItems];
+// The 16 counts of cells [c0, c0 + 16): 128-bit loads when in range and the
+// array is 16-byte aligned (c0 is a multiple of 16 cells).
+__device__ __forceinline__ void load_counts(const uint32_t* __restrict__ count, uint32_t c0, uint32_t cells, bool vec,
+                                            uint32_t (&v)[kScanItems]) {
     if (vec) {
         const uint4* q = reinterpret_cast<const uint4*>(count + c0);
 #pragma unroll
@@ -164,6 +106,61 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) v[k] = c0 + k < cells ? count[c0 + k] : 0u;
     }
+}
+
+// Totals: block b sums the counts of tile b.
+__global__ void __launch_bounds__(kScanThreads) k_cell_totals(const uint32_t* __restrict__ count,
+                                                              uint32_t* __restrict__ tile_total,
+                                                              int* __restrict__ info, uint32_t cells) {
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (blockIdx.x == 0 && tid == 0) {  // the step's particle count; the scan sets kOutStart anew
+        const int out = info[kOutStart];
+        if (out >= 0) info[kNum] = out;
+        info[kOutStart] = -1;
+    }
+    const uint32_t c0 = (uint32_t)blockIdx.x * kScanTile + (uint32_t)tid * kScanItems;
+    const bool vec = c0 + kScanItems <= cells && (reinterpret_cast<uintptr_t>(count) & 15u) == 0;
+    uint32_t v[kScanItems];
+    load_counts(count, c0, cells, vec, v);
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) s_warp[warp] = sum;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int w = 0; w < kScanThreads / 32; ++w) t += s_warp[w];
+        tile_total[blockIdx.x] = t;
+    }
+}
+
+// Scan: block b scans tile b (16 consecutive cells per thread) from the sum
+// of the totals of tiles 0..b-1.
+__global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict__ count,
+                                                            uint32_t* __restrict__ cell_start,
+                                                            uint32_t* __restrict__ cell_end,
+                                                            const uint32_t* __restrict__ tile_total,
+                                                            int* __restrict__ info, uint32_t cells) {
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    __shared__ uint32_t s_base[kScanThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tile = blockIdx.x;
+    uint32_t before = 0;
+    for (int t = tid; t < tile; t += kScanThreads) before += __ldg(tile_total + t);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    if (lane == 0) s_base[warp] = before;
+    const uint32_t c0 = (uint32_t)tile * kScanTile + (uint32_t)tid * kScanItems;
+    // a recorded rollout's cell arrays are packed at a stride of nb_cells + 1
+    // words, so their base need not be 16-byte aligned
+    const bool vec = c0 + kScanItems <= cells &&
+                     ((reinterpret_cast<uintptr_t>(count) | reinterpret_cast<uintptr_t>(cell_start)) & 15u) == 0;
+    uint32_t v[kScanItems];
+    load_counts(count, c0, cells, vec, v);
     uint32_t sum = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) sum += v[k];
@@ -176,33 +173,9 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict
     }
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    uint32_t wbefore = 0, total = 0;
+    uint32_t run = x - sum;
 #pragma unroll
-    for (int w = 0; w < kScanThreads / 32; ++w) {
-        const uint32_t t = s_warp[w];
-        wbefore += w < warp ? t : 0u;
-        total += t;
-    }
-    const uint32_t texcl = wbefore + x - sum;
-    if (tid == 0) st_relaxed_u32(tile_total + tile, kPublished | total);
-    // the totals of tiles 0..tile-1, all read at once (bounded waits)
-    uint32_t before = 0;
-    bool late = false;
-    for (int t = tid; t < tile; t += kScanThreads) {
-        uint32_t w = ld_relaxed_u32(tile_total + t);
-        for (int spins = 0; !(w & kPublished) && spins < kSpinLimit; ++spins) w = ld_relaxed_u32(tile_total + t);
-        late |= !(w & kPublished);
-        before += w & ~kPublished;
-    }
-    if (late) atomicOr(info + kError, kErrLookbackTimeout);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
-    if (lane == 0) s_base[warp] = before;
-    __syncthreads();
-    uint32_t tbase = 0;
-#pragma unroll
-    for (int w = 0; w < kScanThreads / 32; ++w) tbase += s_base[w];
-    uint32_t run = tbase + texcl;
+    for (int w = 0; w < kScanThreads / 32; ++w) run += (w < warp ? s_warp[w] : 0u) + s_base[w];
     uint32_t st[kScanItems];
     const uint32_t last = cells - 1;  // the out-of-grid key
 #pragma unroll
@@ -298,10 +271,6 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
 
 // ---------------------------------------------------------------------------
 // Launchers, one per pass (the step profile times each).
-void launch_cell_prologue(uint32_t* tile_total, int nb_cells, int* info, cudaStream_t st) {
-    k_cell_prologue<<<1, 256, 0, st>>>(tile_total, cell_scan_tiles(nb_cells + 1), info);
-}
-
 void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of, uint32_t* count, const int* info,
                        const StepParams& p, int grid_items, cudaStream_t st) {
     const int per = 256 * kItems;
@@ -309,7 +278,12 @@ void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of,
     k_cell_count<<<blocks, 256, 0, st>>>(pos_u, key_of, slot_of, count, info, p);
 }
 
-void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total,
+void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, int nb_cells, cudaStream_t st) {
+    const uint32_t cells = (uint32_t)nb_cells + 1u;
+    k_cell_totals<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, tile_total, info, cells);
+}
+
+void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, const uint32_t* tile_total,
                       int* info, int nb_cells, cudaStream_t st) {
     const uint32_t cells = (uint32_t)nb_cells + 1u;
     k_cell_scan<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, cell_start, cell_end, tile_total, info,

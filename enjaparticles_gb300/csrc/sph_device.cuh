@@ -28,7 +28,6 @@ enum InfoSlot : int {
     kError = 2,      // bit flags, see kErr*
     kDeleted = 3,    // number of particles removed by the last out-of-grid deletion
     kSortTiles = 4,  // 4 slots: tile counters of the radix passes
-    kCellScanTile = 8,  // tile counter of the cell-count scan
     kInfoSlots = 16
 };
 constexpr int kErrLookbackTimeout = 1;
@@ -147,14 +146,14 @@ void launch_radix_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                        const uint32_t* hist, uint32_t* status, int* tile_counter, int* err, int shift, int bits,
                        int grid_items, cudaStream_t st);
 int radix_tiles(int n);
-// Counting sort on the cell key (sph_cellsort.cu): prologue, count, scan,
+// Counting sort on the cell key (sph_cellsort.cu): count, totals, scan,
 // place, then permute (which reads veleval_u/vel_u: after any upload join).
 int cell_scan_tiles(int cells);
-void launch_cell_prologue(uint32_t* tile_total, int nb_cells, int* info, cudaStream_t st);
 void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of, uint32_t* count, const int* info,
                        const StepParams& p, int grid_items, cudaStream_t st);
-void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
-                      int nb_cells, cudaStream_t st);
+void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, int nb_cells, cudaStream_t st);
+void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, const uint32_t* tile_total,
+                      int* info, int nb_cells, cudaStream_t st);
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
                        const int* info, int grid_items, cudaStream_t st);
 void launch_cell_permute(const uint2* entries, const uint32_t* cell_start, const uint32_t* cell_end, uint32_t* keys,
