@@ -148,17 +148,16 @@ class ClockSampler:
 
 
 def algorithmic_bytes(n, c):
-    """Compulsory bytes per launch of each kernel of the step (one read of each
-    input and one write of each output, physics fields only):
-      count 24N (pos in; key, slot out), totals 4C, scan 12C (counts in,
-      cell_start out, counts zeroed; cell_end of the occupied cells not
-      counted), place 16N,
-      permute 8N in + 8N (keys, indices) + 64N (pos, veleval gathered and
-      written), density 20N+8C, force 68N+8C + collision 64N + leapfrog 116N;
-      total 416N + 32C."""
-    return {"k_cell_count": 24.0 * n, "k_cell_totals": 4.0 * c, "k_cell_scan": 12.0 * c,
-            "k_cell_place": 16.0 * n, "k_cell_permute": 80.0 * n,
-            "k_density": 20.0 * n + 8.0 * c, "k_force(fused collision+leapfrog)": 248.0 * n + 8.0 * c}
+    """Compulsory bytes per step: one read of each input and one write of each
+    output per stage of the reference's step, physics fields only (412N +
+    24C), each stage's bytes given to the kernel that does that work:
+      hash 24N -> count; the cell_start reset 4C and cellindices' 4C -> scan;
+      sort 16N -> place; cellindices 4N + permute 100N -> permute;
+      density 20N+8C; force 68N+8C + collision 64N + leapfrog 116N -> force.
+    The tile totals are the counting sort's own and carry none."""
+    return {"k_cell_count": 24.0 * n, "k_cell_totals": 0.0, "k_cell_scan": 8.0 * c, "k_cell_place": 16.0 * n,
+            "k_cell_permute": 104.0 * n, "k_density": 20.0 * n + 8.0 * c,
+            "k_force(fused collision+leapfrog)": 248.0 * n + 8.0 * c}
 
 
 def cpu_baseline_port(n, seconds):

@@ -417,7 +417,10 @@ struct AdjState {
     int nsteps = 0, K = 0, n = 0, exact = 0;
     float dt = 0.f;
     unsigned params_version = 0;
-    size_t N = 0, C1 = 0, state_elems = 0;  // slot capacity, cell entries, state elements checkpointed
+    // slot capacity, cell-array stride (the cell entries rounded up to 4
+    // words so that every slot's cell arrays start 16-byte aligned for the
+    // 128-bit accesses of the sort's scan), state elements checkpointed
+    size_t N = 0, C1 = 0, state_elems = 0;
     int nscenes = 1;
     bool tape_keys = false;
     int cap_K = 0, cap_ckpt = 0;
@@ -781,7 +784,7 @@ int sph_adjoint_record(sph_ctx* c, float dt, int nsteps, int K) {
     if (!c->adj) {
         c->adj = new sph_adjoint();
         c->adj->N = (size_t)c->max_num;
-        c->adj->C1 = (size_t)c->gp.nb_cells + 1;
+        c->adj->C1 = ((size_t)c->gp.nb_cells + 1 + 3) & ~(size_t)3;
     }
     sph_adjoint* a = c->adj;
     a->recorded = 0;
@@ -893,7 +896,7 @@ int sph_loss_mse(sph_ctx* c, const sph_float4* target, sph_float4* dL_dpos, doub
     if (!c->adj) {
         c->adj = new sph_adjoint();
         c->adj->N = (size_t)c->max_num;
-        c->adj->C1 = (size_t)c->gp.nb_cells + 1;
+        c->adj->C1 = ((size_t)c->gp.nb_cells + 1 + 3) & ~(size_t)3;
     }
     const cudaError_t e = ensure_buffers(c->adj, 0, 0);
     if (e != cudaSuccess) return set_err(c, SPH_ENOMEM, "sph_loss_mse: %s", cudaGetErrorString(e));
@@ -920,7 +923,7 @@ int sph_batch_adjoint_record(sph_batch* b, float dt, int nsteps, int K) {
     if (!b->adj) {
         b->adj = new sph_batch_adjoint();
         b->adj->N = (size_t)b->nslots;
-        b->adj->C1 = b->ncells_total;
+        b->adj->C1 = ((size_t)b->ncells_total + 3) & ~(size_t)3;
         b->adj->nscenes = b->nscenes;
         b->adj->tape_keys = true;
         b->adj->state_elems = (size_t)b->nslots;
@@ -1088,7 +1091,7 @@ int sph_batch_loss_mse(sph_batch* b, const sph_float4* target, sph_float4* dL_dp
     if (!b->adj) {
         b->adj = new sph_batch_adjoint();
         b->adj->N = (size_t)b->nslots;
-        b->adj->C1 = b->ncells_total;
+        b->adj->C1 = ((size_t)b->ncells_total + 3) & ~(size_t)3;
         b->adj->nscenes = b->nscenes;
         b->adj->tape_keys = true;
         b->adj->state_elems = (size_t)b->nslots;
