@@ -241,6 +241,10 @@ void free_all(sph_ctx* c) {
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
     if (c->up_done) cudaEventDestroy(c->up_done);
+    if (c->up_veleval) cudaEventDestroy(c->up_veleval);
+    if (c->side_fork) cudaEventDestroy(c->side_fork);
+    if (c->side_join) cudaEventDestroy(c->side_join);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
     if (c->up_start) cudaEventDestroy(c->up_start);
     if (c->up_stream) cudaStreamDestroy(c->up_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -292,7 +296,8 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
     sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, c->gp.nb_cells, st);
     sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, c->gp.nb_cells, st);
     sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
-    int rc = join_upload(c);
+    // the permute gathers veleval (and vel when gather == 2)
+    int rc = gather == 2 ? join_upload(c) : join_upload_veleval(c);
     if (rc) return rc;
     sphk::launch_cell_permute(c->cell_entries, c->cell_start, c->cell_end, c->keys_a, c->idx_a, c->pos_u, c->vel_u,
                               c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, gather, st);
@@ -302,14 +307,10 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
     return SPH_OK;
 }
 
-// Density over the sorted arrays; with_deletion: also the fused step's
-// out-of-grid bookkeeping.
-void density_launch(sph_ctx* c, const uint32_t* idx, bool with_deletion, cudaStream_t st) {
-    // the fused step (with_deletion) skips the neighbour counts
-    sphk::launch_density(c->pos_s, c->veleval_s, c->density, c->rec_pd, c->rec_vi, with_deletion ? nullptr : c->nbr,
-                         c->mask,
-                         (size_t)c->max_num, c->cell_start, c->cell_end, c->info, idx, c->vel_u,
-                         with_deletion ? c->vel_s : nullptr, c->del_pos, c->del_vel, c->P, c->num_hint, st);
+// Density over the sorted arrays; the fused step skips the neighbour counts.
+void density_launch(sph_ctx* c, bool fused, cudaStream_t st) {
+    sphk::launch_density(c->pos_s, c->veleval_s, c->density, c->rec_pd, c->rec_vi, fused ? nullptr : c->nbr, c->mask,
+                         (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, st);
 }
 
 void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {
@@ -328,7 +329,7 @@ static int enqueue_to_force(sph_ctx* c) {
     if (rc) return rc;
     sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
                                c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
-    density_launch(c, c->idx_a, false, c->stream);
+    density_launch(c, false, c->stream);
     force_launch(c, c->idx_a, false, 0.f, c->stream);
     return SPH_OK;
 }
@@ -358,7 +359,16 @@ int enqueue_fused_step(sph_ctx* c, float dt) {
     }
     int rc = enqueue_cell_sort(c, 1);
     if (rc) return rc;
-    density_launch(c, c->idx_a, true, c->stream);
+    // beside the density pass, on the side stream: the deletion bookkeeping,
+    // once the velocities are in (it and the integrator read them)
+    CK(c, cudaEventRecord(c->side_fork, c->stream));
+    CK(c, cudaStreamWaitEvent(c->side_stream, c->side_fork, 0));
+    density_launch(c, true, c->stream);
+    if ((rc = join_upload_on(c, c->side_stream))) return rc;
+    sphk::launch_step_deletion(c->pos_s, c->idx_a, c->vel_u, c->vel_s, c->del_pos, c->del_vel, c->info,
+                               c->side_stream);
+    CK(c, cudaEventRecord(c->side_join, c->side_stream));
+    CK(c, cudaStreamWaitEvent(c->stream, c->side_join, 0));
     force_launch(c, c->idx_a, true, dt, c->stream);
     CK_LAUNCH(c);
     return SPH_OK;
@@ -384,16 +394,31 @@ int check_ctx(sph_ctx* c, bool join) {
     return SPH_OK;
 }
 
-int join_upload(sph_ctx* c) {
+// Stream st waits for the latest upload (st is the context stream, or a
+// stream the context stream later waits for).
+int join_upload_on(sph_ctx* c, cudaStream_t st) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    CK(c, cudaStreamIsCapturing(c->stream, &cs));
+    CK(c, cudaStreamIsCapturing(st, &cs));
     if (cs == cudaStreamCaptureStatusActive) {
         // in the step graph for good: every replay waits for the latest upload
-        CK(c, cudaStreamWaitEvent(c->stream, c->up_done, cudaEventWaitExternal));
+        CK(c, cudaStreamWaitEvent(st, c->up_done, cudaEventWaitExternal));
     } else if (c->up_pending) {
-        CK(c, cudaStreamWaitEvent(c->stream, c->up_done, 0));
+        CK(c, cudaStreamWaitEvent(st, c->up_done, 0));
         c->up_pending = false;
     }
+    return SPH_OK;
+}
+
+int join_upload(sph_ctx* c) { return join_upload_on(c, c->stream); }
+
+// The veleval part of the latest upload only (vel may still be on its way).
+int join_upload_veleval(sph_ctx* c) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(c, cudaStreamIsCapturing(c->stream, &cs));
+    if (cs == cudaStreamCaptureStatusActive)
+        CK(c, cudaStreamWaitEvent(c->stream, c->up_veleval, cudaEventWaitExternal));
+    else if (c->up_pending)
+        CK(c, cudaStreamWaitEvent(c->stream, c->up_veleval, 0));
     return SPH_OK;
 }
 
@@ -485,7 +510,11 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
         rc = set_err(nullptr, SPH_ENOMEM, "cudaMallocHost failed");
     if (rc == SPH_OK && (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
                          cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking) != cudaSuccess ||
+                         cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+                         cudaEventCreateWithFlags(&c->side_fork, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaEventCreateWithFlags(&c->side_join, cudaEventDisableTiming) != cudaSuccess ||
                          cudaEventCreateWithFlags(&c->up_start, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaEventCreateWithFlags(&c->up_veleval, cudaEventDisableTiming) != cudaSuccess ||
                          cudaEventCreateWithFlags(&c->up_done, cudaEventDisableTiming) != cudaSuccess))
         rc = set_err(nullptr, SPH_ECUDA, "cudaStreamCreate / cudaEventCreate failed");
     if (rc != SPH_OK) {
@@ -535,6 +564,7 @@ int sph_destroy(sph_ctx* c) {
     if (!c) return SPH_EINVAL;
     cudaSetDevice(c->device);
     if (c->up_stream) cudaStreamSynchronize(c->up_stream);
+    if (c->side_stream) cudaStreamSynchronize(c->side_stream);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (sph_hose* h : c->hoses) sph_hose_destroy(h);
     free_all(c);
@@ -650,16 +680,18 @@ int sph_upload(sph_ctx* c, const sph_float4* pos, const sph_float4* vel, const s
     const size_t b = (size_t)n * 16;
     if (n > 0) {
         CK(c, cudaMemcpyAsync(c->pos_u, pos, b, cudaMemcpyHostToDevice, c->stream));
-        // vel and veleval follow on the side stream once pos is in (the link
-        // is not shared with it): the next step's hash and sort, which read
-        // only pos, run meanwhile
+        // veleval, then vel, follow on the side stream once pos is in (the
+        // link is not shared with it): the next step's hash and sort, which
+        // read only pos, run meanwhile; its permute needs veleval, and only
+        // its force pass (the integrator) needs vel
         CK(c, cudaEventRecord(c->up_start, c->stream));
         CK(c, cudaStreamWaitEvent(c->up_stream, c->up_start, 0));
-        CK(c, cudaMemcpyAsync(c->vel_u, vel, b, cudaMemcpyHostToDevice, c->up_stream));
         if (veleval)
             CK(c, cudaMemcpyAsync(c->veleval_u, veleval, b, cudaMemcpyHostToDevice, c->up_stream));
         else
             CK(c, cudaMemsetAsync(c->veleval_u, 0, b, c->up_stream));
+        CK(c, cudaEventRecord(c->up_veleval, c->up_stream));
+        CK(c, cudaMemcpyAsync(c->vel_u, vel, b, cudaMemcpyHostToDevice, c->up_stream));
         CK(c, cudaEventRecord(c->up_done, c->up_stream));
         c->up_pending = true;
     }
@@ -790,7 +822,7 @@ int sph_stage_permute(sph_ctx* c) {
 int sph_stage_density(sph_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
-    density_launch(c, c->idx_cur, false, c->stream);
+    density_launch(c, false, c->stream);
     CK_LAUNCH(c);
     return SPH_OK;
 }
@@ -1012,8 +1044,8 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step; with a triangle mesh the step is staged");
     if (!c->hoses.empty()) return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step without hoses");
     // Launches of one fused step: count, totals, scan, place, permute,
-    // density, force+collision+leapfrog.
-    const int nk = 7;
+    // density, deletion bookkeeping, force+collision+leapfrog.
+    const int nk = 8;
     if (nkernels) *nkernels = nk;
     for (int k = 0; k < cap; ++k) kernel_ms[k] = 0.f;
     cudaEvent_t ev[nk + 1];
@@ -1035,7 +1067,9 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
                                   c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, 1,
                                   st);
         CK(c, cudaEventRecord(ev[e++], st));
-        density_launch(c, c->idx_a, true, st);
+        density_launch(c, true, st);
+        CK(c, cudaEventRecord(ev[e++], st));
+        sphk::launch_step_deletion(c->pos_s, c->idx_a, c->vel_u, c->vel_s, c->del_pos, c->del_vel, c->info, st);
         CK(c, cudaEventRecord(ev[e++], st));
         force_launch(c, c->idx_a, true, dt, st);
         CK(c, cudaEventRecord(ev[e++], st));
@@ -1055,8 +1089,9 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
 
 const char* sph_profile_kernel_name(sph_ctx* c, int k) {
     static const char* names[] = {"k_cell_count", "k_cell_totals", "k_cell_scan", "k_cell_place",
-                                  "k_cell_permute", "k_density", "k_force(fused collision+leapfrog)"};
-    if (!c || k < 0 || k >= 7) return "";
+                                  "k_cell_permute", "k_density", "k_step_deletion",
+                                  "k_force(fused collision+leapfrog)"};
+    if (!c || k < 0 || k >= 8) return "";
     return names[k];
 }
 

@@ -15,11 +15,17 @@ struct sph_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
-    // sph_upload copies vel/veleval on up_stream after the position copy, so
-    // that they overlap hash and sort; up_done marks their end, and the step
-    // waits for it before cells+permute (every other call waits on entry).
+    // sph_upload copies veleval, then vel, on up_stream after the position
+    // copy, so that they overlap the step's first passes: up_veleval marks the
+    // veleval copy (the step waits for it before the permute), up_done the
+    // end of both (the step waits for it before the force pass; every other
+    // call waits for it on entry).
     cudaStream_t up_stream = nullptr;
-    cudaEvent_t up_start = nullptr, up_done = nullptr;
+    cudaEvent_t up_start = nullptr, up_veleval = nullptr, up_done = nullptr;
+    // the fused step's deletion bookkeeping runs on side_stream beside the
+    // density pass (after the permute and the velocity upload, before force)
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     bool up_pending = false;
     SPHParams sp;
     GridParams gp, gps;
@@ -100,6 +106,8 @@ int check_ctx(sph_ctx* c, bool join = true);
 // The step's wait for a pending upload, enqueued right before cells+permute
 // (an external event wait node when the stream is being captured).
 int join_upload(sph_ctx* c);
+int join_upload_on(sph_ctx* c, cudaStream_t st);
+int join_upload_veleval(sph_ctx* c);
 // Enqueues one fused step (hash .. leapfrog) on c->stream.
 int enqueue_fused_step(sph_ctx* c, float dt);
 // Reads the device counters into c->host_info (synchronises the stream).

@@ -11,7 +11,9 @@
 // the separately rounded result, even with contraction disabled, which would
 // change |r|^2 and with it the neighbour sets.)
 //
-// nbr (neighbour counts) is optional: the fused step leaves it out.
+// nbr (neighbour counts) is optional: the fused step leaves it out.  The
+// fused step's out-of-grid bookkeeping is its own kernel (sph_integrate.cu),
+// so this pass reads no velocity.
 //
 // While it tests the candidates the pass also records, per particle, which of
 // its first kMaskBits candidates (in walk order) are neighbours (self
@@ -21,33 +23,16 @@
 
 namespace sphk {
 
-// When called from the fused step the kernel also does the out-of-grid
-// deletion bookkeeping (vel_s != nullptr).
 template <bool Exact, bool Unit, bool WantCount, class Scenes>
 __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ veleval_s,
                                                  float* __restrict__ density, float4* __restrict__ rec_pd,
                                                  float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
                                                  uint32_t* __restrict__ mask, const size_t mstride,
                                                  const uint32_t* __restrict__ cs0, const uint32_t* __restrict__ ce0,
-                                                 int* __restrict__ info, const uint32_t* __restrict__ idx,
-                                                 const float4* __restrict__ vel_u, float4* __restrict__ vel_s,
-                                                 float4* __restrict__ del_pos, float4* __restrict__ del_vel,
-                                                 const Scenes R) {
+                                                 const int* __restrict__ info, const Scenes R) {
     int n_old, out;
     const int n = effective_num(info, n_old, out);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vel_s != nullptr && out >= 0 && i < n_old) {
-        // SPH.cpp:220-250: the kept particles' velocities in sorted order
-        // (call_prep copies vel_s to vel_u), the removed ones saved.
-        const float4 v = __ldg(vel_u + __ldg(idx + i));
-        if (i < n) {
-            vel_s[i] = v;
-        } else {
-            del_pos[i - n] = __ldg(pos_s + i);
-            del_vel[i - n] = v;
-            if (i == n) info[kDeleted] = n_old - n;
-        }
-    }
     if (i >= n) return;
     const StepParams& P = R.params(i);
     const uint32_t* cs = cs0 + R.cell_base(i);
@@ -123,16 +108,14 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
 template <class Scenes>
 void launch_density_t(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                       uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
-                      const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
-                      float4* vel_s, float4* del_pos, float4* del_vel, const Scenes& R, bool unit, bool exact,
+                      const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
                       int grid_items, cudaStream_t st) {
     const int threads = 256;
     int blocks = (grid_items + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
-#define SPH_DENSITY_LAUNCH(E, U, W)                                                                                   \
-    k_density<E, U, W, Scenes><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask,     \
-                                                           mask_stride, cell_start, cell_end, (int*)info, idx, vel_u, \
-                                                           vel_s, del_pos, del_vel, R)
+#define SPH_DENSITY_LAUNCH(E, U, W)                                                                               \
+    k_density<E, U, W, Scenes><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, \
+                                                           mask_stride, cell_start, cell_end, info, R)
 #define SPH_DENSITY_LAUNCH_E(E)                                                                \
     if (unit) {                                                                                \
         if (nbr) SPH_DENSITY_LAUNCH(E, true, true); else SPH_DENSITY_LAUNCH(E, true, false);   \
@@ -150,12 +133,9 @@ void launch_density_t(const float4* pos_s, const float4* veleval_s, float* densi
 
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
-                    const uint32_t* cell_end, const int* info, const uint32_t* idx, const float4* vel_u,
-                    float4* vel_s, float4* del_pos, float4* del_vel, const StepParams& p, int grid_items,
-                    cudaStream_t st) {
+                    const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     idx, vel_u, vel_s, del_pos, del_vel, OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items,
-                     st);
+                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, st);
 }
 
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
@@ -163,7 +143,7 @@ void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* d
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                           const ManyScenes& scenes, bool unit, int exact, int grid_items, cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     nullptr, nullptr, nullptr, nullptr, nullptr, scenes, unit, exact != 0, grid_items, st);
+                     scenes, unit, exact != 0, grid_items, st);
 }
 
 }  // namespace sphk

@@ -98,6 +98,36 @@ void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_
     k_euler<<<blocks, 256, 0, st>>>(pos_s, vel_s, force_s, idx, pos_u, vel_u, info, p, dt);
 }
 
+// Fused step's deletion (SPH.cpp:220-250): the kept particles' velocities in
+// sorted order (call_prep copies vel_s to vel_u, done by the force pass, which
+// re-indexes them), the removed ones saved.  A grid-stride loop over a few
+// blocks per SM: the common step, where nothing left the grid, costs one
+// read of info per block.
+__global__ void __launch_bounds__(256) k_step_deletion(const float4* __restrict__ pos_s,
+                                                       const uint32_t* __restrict__ idx,
+                                                       const float4* __restrict__ vel_u, float4* __restrict__ vel_s,
+                                                       float4* __restrict__ del_pos, float4* __restrict__ del_vel,
+                                                       int* __restrict__ info) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    if (out < 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old; i += gridDim.x * blockDim.x) {
+        const float4 v = __ldg(vel_u + __ldg(idx + i));
+        if (i < n) {
+            vel_s[i] = v;
+        } else {
+            del_pos[i - n] = __ldg(pos_s + i);
+            del_vel[i - n] = v;
+            if (i == n) info[kDeleted] = n_old - n;
+        }
+    }
+}
+
+void launch_step_deletion(const float4* pos_s, const uint32_t* idx, const float4* vel_u, float4* vel_s,
+                          float4* del_pos, float4* del_vel, int* info, cudaStream_t st) {
+    k_step_deletion<<<152 * 4, 256, 0, st>>>(pos_s, idx, vel_u, vel_s, del_pos, del_vel, info);
+}
+
 // Staged deletion: after cellindices + permute, when some particles left the
 // grid (cell_start[nb_cells] set), keep the first out_start sorted particles:
 // save the removed ones, and re-index the kept ones in sorted order
