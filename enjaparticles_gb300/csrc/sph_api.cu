@@ -293,8 +293,9 @@ int enqueue_sort(sph_ctx* c) {
 int enqueue_cell_sort(sph_ctx* c, int gather) {
     cudaStream_t st = c->stream;
     sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
-    sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, c->gp.nb_cells, st);
-    sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, c->gp.nb_cells, st);
+    const uint32_t cells = (uint32_t)c->gp.nb_cells + 1u;
+    sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, cells, st);
+    sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, cells, st);
     sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
     // the permute gathers veleval (and vel when gather == 2)
     int rc = gather == 2 ? join_upload(c) : join_upload_veleval(c);
@@ -1056,9 +1057,10 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, c->gp.nb_cells, st);
+        sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, (uint32_t)c->gp.nb_cells + 1u, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, c->gp.nb_cells,
+        sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info,
+                               (uint32_t)c->gp.nb_cells + 1u,
                                st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);

@@ -5,12 +5,17 @@
 // with one launch sequence per step (captured in one CUDA graph):
 //
 //   hash     every particle slot of every scene; key = scene << cell_bits |
-//            cell (the scene's own grid and out-of-grid cell C_s); unused
-//            slots get a key above every scene's keys
-//   sort     the same stable LSD radix sort over the segmented key space:
-//            scenes come out in order, each in its own cell order
-//   cells    cell ranges into per-scene segments of one cell array, and the
-//            gather of pos / veleval into sorted order
+//            cell (the scene's own grid and out-of-grid cell C_s); the
+//            scene's cells are one segment of a cell array shared by all
+//            scenes (global cell = cbase[scene] + cell)
+//   sort     the counting sort of the single system (sph_cellsort.cu) over
+//            the global cells: an atomic count per cell gives each particle a
+//            slot, the scan gives the cell ranges (per-scene segments), each
+//            particle goes to its cell's start + slot, and the permute ranks
+//            it by slot index among its cell's entries.  Scenes come out in
+//            order, each in its own cell order with equal keys by slot, the
+//            order a stable sort of the keys gives; unused slots take no
+//            part
 //   density, force+collision+leapfrog: the neighbour passes with the scene of
 //            each particle looked up from its key (ManyScenes)
 //
@@ -31,82 +36,81 @@ using sphk::StepParams;
 
 namespace {
 
-__global__ void __launch_bounds__(256) k_bhash(const float4* __restrict__ pos_u, uint32_t* __restrict__ keys,
-                                               uint32_t* __restrict__ idx, uint32_t* __restrict__ cell_start,
-                                               size_t ncell_words, uint32_t* __restrict__ hist,
-                                               const uint16_t* __restrict__ scene_of,
-                                               const uint32_t* __restrict__ slot_off,
-                                               const int* __restrict__ num, const StepParams* __restrict__ table,
-                                               int nslots, int cell_bits, uint32_t invalid_key, int passes) {
-    __shared__ uint32_t s_hist[4][256];
-    const int tid = threadIdx.x;
-    for (int k = tid; k < 4 * 256; k += blockDim.x) (&s_hist[0][0])[k] = 0;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t k = (size_t)blockIdx.x * blockDim.x + tid; k < ncell_words; k += stride) cell_start[k] = sphk::kEmpty;
-    __syncthreads();
-    const unsigned lane = tid & 31;
-    for (size_t base = (size_t)blockIdx.x * blockDim.x + (tid & ~31); base < (size_t)nslots; base += stride) {
-        const size_t t = base + lane;
-        const bool inside = t < (size_t)nslots;
-        uint32_t key = invalid_key;
-        if (inside) {
-            const uint32_t s = scene_of[t];
-            if ((int)(t - slot_off[s]) < num[s]) {
-                const StepParams& P = table[s];
-                const float4 q = __ldg(pos_u + t);
-                const int3 c = sphk::grid_cell(q.x, q.y, q.z, P.g_min, P.g_delta);
-                int h = sphk::grid_hash_f(c.x, c.y, c.z, P.g_res);
-                h = h > P.nb_cells ? P.nb_cells : h;
-                h = h < 0 ? P.nb_cells : h;
-                key = (s << cell_bits) | (uint32_t)h;
-            }
-            keys[t] = key;
-            idx[t] = (uint32_t)t;
-        }
-        for (int ps = 0; ps < passes; ++ps) {
-            const uint32_t d = inside ? ((key >> (8 * ps)) & 255u) : 0x100u;
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            if (inside && (int)lane == 31 - __clz(peers)) atomicAdd(&s_hist[ps][d], (uint32_t)__popc(peers));
-        }
+// Count: key and cell slot of every used particle slot; unused slots get
+// invalid_key.
+__global__ void __launch_bounds__(256) k_bcount(const float4* __restrict__ pos_u, uint32_t* __restrict__ key_of,
+                                                uint32_t* __restrict__ slot_of, uint32_t* __restrict__ count,
+                                                const uint16_t* __restrict__ scene_of,
+                                                const uint32_t* __restrict__ slot_off,
+                                                const uint32_t* __restrict__ cbase, const int* __restrict__ num,
+                                                const StepParams* __restrict__ table, int nslots, int cell_bits,
+                                                uint32_t invalid_key) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nslots) return;
+    const uint32_t s = scene_of[t];
+    uint32_t key = invalid_key;
+    if ((int)((uint32_t)t - slot_off[s]) < num[s]) {
+        const StepParams& P = table[s];
+        const float4 q = __ldg(pos_u + t);
+        const int3 c = sphk::grid_cell(q.x, q.y, q.z, P.g_min, P.g_delta);
+        int h = sphk::grid_hash_f(c.x, c.y, c.z, P.g_res);
+        h = h > P.nb_cells ? P.nb_cells : h;
+        h = h < 0 ? P.nb_cells : h;
+        key = (s << cell_bits) | (uint32_t)h;
+        slot_of[t] = atomicAdd(count + cbase[s] + (uint32_t)h, 1u);
     }
-    __syncthreads();
-    for (int k = tid; k < passes * 256; k += blockDim.x) {
-        const uint32_t c = (&s_hist[0][0])[k];
-        if (c) atomicAdd(hist + k, c);
-    }
+    key_of[t] = key;
 }
 
-// Cell ranges (cellindices.cl semantics per scene segment) and the gather.
-__global__ void __launch_bounds__(256) k_bcells(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ idx,
-                                                uint32_t* __restrict__ cell_start, uint32_t* __restrict__ cell_end,
-                                                const uint32_t* __restrict__ cbase,
-                                                const StepParams* __restrict__ table, const float4* __restrict__ pos_u,
-                                                const float4* __restrict__ veleval_u, float4* __restrict__ pos_s,
-                                                float4* __restrict__ veleval_s, int* __restrict__ info, int nvalid,
-                                                int cell_bits) {
+// Place: (slot index, key) at the start of the particle's cell + its slot.
+__global__ void __launch_bounds__(256) k_bplace(const uint32_t* __restrict__ key_of,
+                                                const uint32_t* __restrict__ slot_of,
+                                                const uint32_t* __restrict__ cell_start,
+                                                const uint32_t* __restrict__ cbase, uint2* __restrict__ entries,
+                                                int nslots, int cell_bits, uint32_t invalid_key) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nslots) return;
+    const uint32_t key = __ldg(key_of + t);
+    if (key == invalid_key) return;
+    const uint32_t g = __ldg(cbase + (key >> cell_bits)) + (key & ((1u << cell_bits) - 1u));
+    entries[__ldg(cell_start + g) + __ldg(slot_of + t)] = make_uint2((uint32_t)t, key);
+}
+
+// Permute: rank within the cell, sorted keys (the scene resolver reads them),
+// indices, the gather of pos / veleval; particles in their scene's
+// out-of-grid cell are counted as frozen.
+__global__ void __launch_bounds__(256) k_bpermute(const uint2* __restrict__ entries,
+                                                  const uint32_t* __restrict__ cell_start,
+                                                  const uint32_t* __restrict__ cell_end,
+                                                  const uint32_t* __restrict__ cbase,
+                                                  const StepParams* __restrict__ table, uint32_t* __restrict__ keys,
+                                                  uint32_t* __restrict__ idx, const float4* __restrict__ pos_u,
+                                                  const float4* __restrict__ veleval_u, float4* __restrict__ pos_s,
+                                                  float4* __restrict__ veleval_s, int* __restrict__ info,
+                                                  int cell_bits) {
+    const int nvalid = info[sphk::kNum];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    const uint32_t key = i < nvalid ? keys[i] : 0xffffffffu;
-    uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
-    if (lane == 0 && i > 0 && i < nvalid) prev = keys[i - 1];
     if (i >= nvalid) return;
-    const uint32_t cmask = (1u << cell_bits) - 1u;
-    const uint32_t s = key >> cell_bits, cell = key & cmask;
-    const uint32_t g = cbase[s] + cell;
-    if (i == 0) {
-        cell_start[g] = 0;
-    } else if (prev != key) {
-        cell_start[g] = (uint32_t)i;
-        cell_end[cbase[prev >> cell_bits] + (prev & cmask)] = (uint32_t)i;
-    }
-    if (i == nvalid - 1) cell_end[g] = (uint32_t)nvalid;
+    const uint2 e = __ldg(entries + i);
+    const uint32_t id = e.x, key = e.y;
+    const float4 pq = __ldg(pos_u + id);
+    const float4 vq = __ldg(veleval_u + id);
+    const uint32_t s = key >> cell_bits, cell = key & ((1u << cell_bits) - 1u);
+    const uint32_t g = __ldg(cbase + s) + cell;
+    const uint32_t cs = __ldg(cell_start + g), ce = __ldg(cell_end + g);
+    if (cs >= ce || ce > (uint32_t)nvalid) return;  // never write outside the cell
+    const uint32_t* ids = reinterpret_cast<const uint32_t*>(entries);
+    uint32_t rank = 0;
+    for (uint32_t t = cs; t < ce; ++t) rank += __ldg(ids + 2 * t) < id ? 1u : 0u;
+    const uint32_t p = cs + rank;
+    keys[i] = key;
+    idx[p] = id;
+    pos_s[p] = pq;
+    veleval_s[p] = vq;
     if (cell == (uint32_t)table[s].nb_cells) {
         atomicAdd(info + kBatchFrozen, 1);
         atomicAdd(info + kBatchFrozenTotal, 1);
     }
-    const uint32_t o = __ldg(idx + i);
-    pos_s[i] = __ldg(pos_u + o);
-    veleval_s[i] = __ldg(veleval_u + o);
 }
 
 __global__ void k_bset(int* p, int v) { *p = v; }
@@ -140,7 +144,8 @@ static void batch_free(sph_batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     void* ptrs[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi, b->density,
                     b->mask, b->keys_a, b->idx_a, b->keys_b, b->idx_b, b->cell_start, b->cell_end, b->scene_of,
-                    b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->info_sort, b->info_nb, b->hist, b->status};
+                    b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->info_nb, b->cell_count, b->cell_tile_total,
+                    b->cell_entries};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->host_info) cudaFreeHost(b->host_info);
@@ -153,32 +158,20 @@ sphk::ManyScenes batch_scenes(const sph_batch* b) {
 
 int batch_enqueue_step(sph_batch* b, float dt) {
     cudaStream_t st = b->stream;
-    uint32_t* hkeys = (b->passes & 1) ? b->keys_b : b->keys_a;
-    uint32_t* hidx = (b->passes & 1) ? b->idx_b : b->idx_a;
-    sphk::launch_prologue(b->hist, b->info_sort, st);
-    int blocks = (b->nslots + 255) / 256;
-    blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
-    k_bhash<<<blocks, 256, 0, st>>>(b->pos_u, hkeys, hidx, b->cell_start, b->ncells_total, b->hist, b->scene_of,
-                                     b->d_slot_off, b->d_num, b->d_table, b->nslots, b->cell_bits, b->invalid_key,
-                                     b->passes);
+    const int blocks = (b->nslots + 255) / 256;
+    const uint32_t cells = (uint32_t)b->ncells_total;
     k_bzero_int<<<1, 1, 0, st>>>(b->info_nb + kBatchFrozen);
-    sphk::launch_sort_reset(b->status, (size_t)b->passes * b->tiles_cap * 256, b->info_sort + sphk::kSortTiles, st);
-    uint32_t *kin = hkeys, *vin = hidx;
-    uint32_t *kout = (kin == b->keys_a) ? b->keys_b : b->keys_a, *vout = (vin == b->idx_a) ? b->idx_b : b->idx_a;
-    const int total_bits = b->scene_bits + b->cell_bits;
-    for (int ps = 0; ps < b->passes; ++ps) {
-        int bits = total_bits - 8 * ps;
-        bits = bits > 8 ? 8 : (bits < 1 ? 1 : bits);
-        sphk::launch_radix_pass(kin, vin, kout, vout, b->info_sort, b->hist + ps * 256,
-                                b->status + (size_t)ps * b->tiles_cap * 256, b->info_sort + sphk::kSortTiles + ps,
-                                b->info_sort + sphk::kError, 8 * ps, bits, b->nslots, st);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
+    k_bcount<<<blocks < 1 ? 1 : blocks, 256, 0, st>>>(b->pos_u, b->keys_b, b->idx_b, b->cell_count, b->scene_of,
+                                                       b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->nslots,
+                                                       b->cell_bits, b->invalid_key);
+    sphk::launch_cell_totals(b->cell_count, b->cell_tile_total, nullptr, cells, st);
+    sphk::launch_cell_scan(b->cell_count, b->cell_start, b->cell_end, b->cell_tile_total, nullptr, cells, st);
+    k_bplace<<<blocks < 1 ? 1 : blocks, 256, 0, st>>>(b->keys_b, b->idx_b, b->cell_start, b->d_cbase, b->cell_entries,
+                                                       b->nslots, b->cell_bits, b->invalid_key);
     const int cb = (b->nvalid + 255) / 256;
-    k_bcells<<<cb < 1 ? 1 : cb, 256, 0, st>>>(b->keys_a, b->idx_a, b->cell_start, b->cell_end, b->d_cbase, b->d_table,
-                                              b->pos_u, b->veleval_u, b->pos_s, b->veleval_s, b->info_nb, b->nvalid,
-                                              b->cell_bits);
+    k_bpermute<<<cb < 1 ? 1 : cb, 256, 0, st>>>(b->cell_entries, b->cell_start, b->cell_end, b->d_cbase, b->d_table,
+                                                b->keys_a, b->idx_a, b->pos_u, b->veleval_u, b->pos_s, b->veleval_s,
+                                                b->info_nb, b->cell_bits);
     const sphk::ManyScenes scenes = batch_scenes(b);
     sphk::launch_density_batch(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, nullptr, b->mask,
                                (size_t)b->nslots, b->cell_start, b->cell_end, b->info_nb, scenes, b->unit != 0,
@@ -239,8 +232,6 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
         return berr(nullptr, SPH_EINVAL, "scene and cell bits exceed a 32-bit key");
     }
     b->invalid_key = (uint32_t)(((uint64_t)nscenes << b->cell_bits) - 1u);
-    b->passes = (b->scene_bits + b->cell_bits + 7) / 8;
-    b->tiles_cap = sphk::radix_tiles(b->nslots);
     cudaGetDevice(&b->device);
     const size_t N = slots;
     int rc = SPH_OK;
@@ -271,10 +262,10 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     BALLOC(b->d_cbase, nscenes * 4);
     BALLOC(b->d_num, nscenes * 4);
     BALLOC(b->d_table, nscenes * sizeof(StepParams));
-    BALLOC(b->info_sort, sizeof(int) * sphk::kInfoSlots);
     BALLOC(b->info_nb, sizeof(int) * sphk::kInfoSlots);
-    BALLOC(b->hist, 4 * 256 * 4);
-    BALLOC(b->status, (size_t)b->passes * b->tiles_cap * 256 * 4);
+    BALLOC(b->cell_count, cells * 4);
+    BALLOC(b->cell_tile_total, (size_t)sphk::cell_scan_tiles((int)cells) * 4);
+    BALLOC(b->cell_entries, N * 8);
 #undef BALLOC
     if (rc == SPH_OK && cudaMallocHost((void**)&b->host_info, sizeof(int) * sphk::kInfoSlots) != cudaSuccess)
         rc = berr(nullptr, SPH_ENOMEM, "cudaMallocHost failed");
@@ -295,16 +286,15 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     if (e == cudaSuccess) e = cudaMemcpy(b->d_cbase, b->cbase.data(), nscenes * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_table, b->P.data(), nscenes * sizeof(StepParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_num, 0, nscenes * 4);
-    if (e == cudaSuccess) e = cudaMemset(b->info_sort, 0, sizeof(int) * sphk::kInfoSlots);
     if (e == cudaSuccess) e = cudaMemset(b->info_nb, 0, sizeof(int) * sphk::kInfoSlots);
+    if (e == cudaSuccess) e = cudaMemset(b->cell_count, 0, cells * 4);
+    if (e == cudaSuccess) e = cudaMemset(b->cell_entries, 0, N * 8);
     const void* zero[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi};
     for (const void* p : zero)
         if (e == cudaSuccess) e = cudaMemset((void*)p, 0, N * 16);
     if (e == cudaSuccess) e = cudaMemset(b->cell_start, 0xff, cells * 4);
     if (e == cudaSuccess) e = cudaMemset(b->cell_end, 0, cells * 4);
     if (e == cudaSuccess) {
-        k_bset<<<1, 1, 0, st>>>(b->info_sort + sphk::kNum, b->nslots);
-        k_bset<<<1, 1, 0, st>>>(b->info_sort + sphk::kOutStart, -1);
         k_bset<<<1, 1, 0, st>>>(b->info_nb + sphk::kOutStart, -1);
         e = cudaStreamSynchronize(st);
     }
@@ -442,11 +432,7 @@ int sph_batch_step(sph_batch* b, float dt, int nsteps) {
 
 int sph_batch_sync(sph_batch* b) {
     if (!b) return SPH_EINVAL;
-    BCK(b, cudaMemcpyAsync(b->host_info, b->info_sort, sizeof(int) * sphk::kInfoSlots, cudaMemcpyDeviceToHost,
-                           b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
-    if (b->host_info[sphk::kError] & sphk::kErrLookbackTimeout)
-        return berr(b, SPH_ETIMEOUT, "radix sort look-back wait expired; the step result is invalid");
     return SPH_OK;
 }
 

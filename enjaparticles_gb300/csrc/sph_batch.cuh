@@ -21,7 +21,7 @@ struct sph_batch {
     std::vector<sphk::StepParams> P;
     std::vector<int> max_num, num;
     std::vector<uint32_t> slot_off, cbase;
-    int nslots = 0, nvalid = 0, cell_bits = 0, scene_bits = 0, passes = 1, tiles_cap = 0, unit = 1;
+    int nslots = 0, nvalid = 0, cell_bits = 0, scene_bits = 0, unit = 1;
     size_t ncells_total = 0;
     uint32_t invalid_key = 0;
     unsigned params_version = 1;
@@ -35,8 +35,11 @@ struct sph_batch {
     uint32_t *d_slot_off = nullptr, *d_cbase = nullptr;
     int* d_num = nullptr;
     sphk::StepParams* d_table = nullptr;
-    int *info_sort = nullptr, *info_nb = nullptr;
-    uint32_t *hist = nullptr, *status = nullptr;
+    int* info_nb = nullptr;
+    // counting sort over the global cells: particles per cell (zero between
+    // steps), per tile of 4096 cells, (slot index, key) per cell slot
+    uint32_t *cell_count = nullptr, *cell_tile_total = nullptr;
+    uint2* cell_entries = nullptr;
     int* host_info = nullptr;
     // tape outputs of the fused force pass (see sph_ctx::keep_f)
     float4 *keep_f = nullptr, *keep_v = nullptr;

@@ -108,13 +108,14 @@ __device__ __forceinline__ void load_counts(const uint32_t* __restrict__ count, 
     }
 }
 
-// Totals: block b sums the counts of tile b.
+// Totals: block b sums the counts of tile b.  info may be null (batches: no
+// deletion).
 __global__ void __launch_bounds__(kScanThreads) k_cell_totals(const uint32_t* __restrict__ count,
                                                               uint32_t* __restrict__ tile_total,
                                                               int* __restrict__ info, uint32_t cells) {
     __shared__ uint32_t s_warp[kScanThreads / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (blockIdx.x == 0 && tid == 0) {  // the step's particle count; the scan sets kOutStart anew
+    if (info != nullptr && blockIdx.x == 0 && tid == 0) {  // the step's particle count; the scan sets kOutStart anew
         const int out = info[kOutStart];
         if (out >= 0) info[kNum] = out;
         info[kOutStart] = -1;
@@ -139,7 +140,8 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_totals(const uint32_t* __
 }
 
 // Scan: block b scans tile b (16 consecutive cells per thread) from the sum
-// of the totals of tiles 0..b-1.
+// of the totals of tiles 0..b-1.  With info, the start of the last cell (the
+// out-of-grid key) goes to info[kOutStart].
 __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict__ count,
                                                             uint32_t* __restrict__ cell_start,
                                                             uint32_t* __restrict__ cell_end,
@@ -183,7 +185,7 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict
         st[k] = v[k] ? run : kEmpty;
         if (v[k]) {
             cell_end[c0 + k] = run + v[k];
-            if (c0 + k == last) info[kOutStart] = (int)run;
+            if (info != nullptr && c0 + k == last) info[kOutStart] = (int)run;
         }
         run += v[k];
     }
@@ -278,14 +280,12 @@ void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of,
     k_cell_count<<<blocks, 256, 0, st>>>(pos_u, key_of, slot_of, count, info, p);
 }
 
-void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, int nb_cells, cudaStream_t st) {
-    const uint32_t cells = (uint32_t)nb_cells + 1u;
+void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, uint32_t cells, cudaStream_t st) {
     k_cell_totals<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, tile_total, info, cells);
 }
 
 void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, const uint32_t* tile_total,
-                      int* info, int nb_cells, cudaStream_t st) {
-    const uint32_t cells = (uint32_t)nb_cells + 1u;
+                      int* info, uint32_t cells, cudaStream_t st) {
     k_cell_scan<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, cell_start, cell_end, tile_total, info,
                                                                        cells);
 }
