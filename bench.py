@@ -2,7 +2,7 @@
 """Benchmark: particle-updates/s of the 2,097,152-particle SPH dam break on GB300.
 
 One step = hash+count -> tile totals -> cell scan -> place -> rank+permute -> density ->
-deletion bookkeeping -> force+collision+leapfrog over all particles (the fused path of sph_step,
+velocity pass (beside density) -> force+collision+leapfrog over all particles (the fused path of sph_step,
 replayed from a CUDA graph).  The workload is the 2M-particle configuration:
 unit box, lattice spacing 2^-8, h = 2s, dt = 0.001, 1000-step rollout, seeded
 synthetic dam-break lattice (no dataset exists for it).
@@ -152,12 +152,12 @@ def algorithmic_bytes(n, c):
     output per stage of the reference's step, physics fields only (412N +
     24C), each stage's bytes given to the kernel that does that work:
       hash 24N -> count; the cell_start reset 4C and cellindices' 4C -> scan;
-      sort 16N -> place; cellindices 4N + permute 100N -> permute;
+      sort 16N -> place; cellindices 4N + permute 100N -> permute (72N) and
+      the velocity pass (32N: the veleval gather);
       density 20N+8C; force 68N+8C + collision 64N + leapfrog 116N -> force.
-    The tile totals and the deletion bookkeeping (a no-op unless particles
-    left the grid) carry none."""
+    The tile totals carry none."""
     return {"k_cell_count": 24.0 * n, "k_cell_totals": 0.0, "k_cell_scan": 8.0 * c, "k_cell_place": 16.0 * n,
-            "k_cell_permute": 104.0 * n, "k_density": 20.0 * n + 8.0 * c, "k_step_deletion": 0.0,
+            "k_cell_permute": 72.0 * n, "k_density": 20.0 * n + 8.0 * c, "k_step_velocities": 32.0 * n,
             "k_force(fused collision+leapfrog)": 248.0 * n + 8.0 * c}
 
 

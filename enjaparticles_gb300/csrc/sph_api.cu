@@ -241,7 +241,6 @@ void free_all(sph_ctx* c) {
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
     if (c->up_done) cudaEventDestroy(c->up_done);
-    if (c->up_veleval) cudaEventDestroy(c->up_veleval);
     if (c->side_fork) cudaEventDestroy(c->side_fork);
     if (c->side_join) cudaEventDestroy(c->side_join);
     if (c->side_stream) cudaStreamDestroy(c->side_stream);
@@ -289,7 +288,7 @@ int enqueue_sort(sph_ctx* c) {
 }
 
 // The step's sort: counting sort on the cell key up to the sorted arrays,
-// cell ranges and the gather (gather 1: pos/veleval, 2: + vel).
+// cell ranges and the gather (gather 0: pos, 2: pos/vel/veleval).
 int enqueue_cell_sort(sph_ctx* c, int gather) {
     cudaStream_t st = c->stream;
     sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
@@ -297,9 +296,11 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
     sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, cells, st);
     sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, cells, st);
     sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
-    // the permute gathers veleval (and vel when gather == 2)
-    int rc = gather == 2 ? join_upload(c) : join_upload_veleval(c);
-    if (rc) return rc;
+    // the permute gathers the velocities when gather == 2
+    if (gather == 2) {
+        const int rc = join_upload(c);
+        if (rc) return rc;
+    }
     sphk::launch_cell_permute(c->cell_entries, c->cell_start, c->cell_end, c->keys_a, c->idx_a, c->pos_u, c->vel_u,
                               c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, gather, st);
     c->keys_cur = c->keys_a;
@@ -308,9 +309,11 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
     return SPH_OK;
 }
 
-// Density over the sorted arrays; the fused step skips the neighbour counts.
+// Density over the sorted arrays; the fused step skips the neighbour counts
+// and leaves the veleval lanes of rec_vi to its velocity pass.
 void density_launch(sph_ctx* c, bool fused, cudaStream_t st) {
-    sphk::launch_density(c->pos_s, c->veleval_s, c->density, c->rec_pd, c->rec_vi, fused ? nullptr : c->nbr, c->mask,
+    sphk::launch_density(c->pos_s, fused ? nullptr : c->veleval_s, c->density, c->rec_pd, c->rec_vi,
+                         fused ? nullptr : c->nbr, c->mask,
                          (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, st);
 }
 
@@ -358,16 +361,18 @@ int enqueue_fused_step(sph_ctx* c, float dt) {
         CK_LAUNCH(c);
         return SPH_OK;
     }
-    int rc = enqueue_cell_sort(c, 1);
+    int rc = enqueue_cell_sort(c, 0);
     if (rc) return rc;
-    // beside the density pass, on the side stream: the deletion bookkeeping,
-    // once the velocities are in (it and the integrator read them)
+    // beside the density pass, on the side stream, once the velocities are
+    // in: the veleval lanes of the neighbour records and the deletion
+    // bookkeeping (they and the integrator are the step's only readers of
+    // the uploaded velocities)
     CK(c, cudaEventRecord(c->side_fork, c->stream));
     CK(c, cudaStreamWaitEvent(c->side_stream, c->side_fork, 0));
     density_launch(c, true, c->stream);
     if ((rc = join_upload_on(c, c->side_stream))) return rc;
-    sphk::launch_step_deletion(c->pos_s, c->idx_a, c->vel_u, c->vel_s, c->del_pos, c->del_vel, c->info,
-                               c->side_stream);
+    sphk::launch_step_velocities(c->pos_s, c->idx_a, c->vel_u, c->veleval_u, c->rec_vi, c->vel_s, c->del_pos,
+                                 c->del_vel, c->info, c->num_hint, c->side_stream);
     CK(c, cudaEventRecord(c->side_join, c->side_stream));
     CK(c, cudaStreamWaitEvent(c->stream, c->side_join, 0));
     force_launch(c, c->idx_a, true, dt, c->stream);
@@ -411,17 +416,6 @@ int join_upload_on(sph_ctx* c, cudaStream_t st) {
 }
 
 int join_upload(sph_ctx* c) { return join_upload_on(c, c->stream); }
-
-// The veleval part of the latest upload only (vel may still be on its way).
-int join_upload_veleval(sph_ctx* c) {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    CK(c, cudaStreamIsCapturing(c->stream, &cs));
-    if (cs == cudaStreamCaptureStatusActive)
-        CK(c, cudaStreamWaitEvent(c->stream, c->up_veleval, cudaEventWaitExternal));
-    else if (c->up_pending)
-        CK(c, cudaStreamWaitEvent(c->stream, c->up_veleval, 0));
-    return SPH_OK;
-}
 
 
 extern "C" {
@@ -515,7 +509,6 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
                          cudaEventCreateWithFlags(&c->side_fork, cudaEventDisableTiming) != cudaSuccess ||
                          cudaEventCreateWithFlags(&c->side_join, cudaEventDisableTiming) != cudaSuccess ||
                          cudaEventCreateWithFlags(&c->up_start, cudaEventDisableTiming) != cudaSuccess ||
-                         cudaEventCreateWithFlags(&c->up_veleval, cudaEventDisableTiming) != cudaSuccess ||
                          cudaEventCreateWithFlags(&c->up_done, cudaEventDisableTiming) != cudaSuccess))
         rc = set_err(nullptr, SPH_ECUDA, "cudaStreamCreate / cudaEventCreate failed");
     if (rc != SPH_OK) {
@@ -681,17 +674,15 @@ int sph_upload(sph_ctx* c, const sph_float4* pos, const sph_float4* vel, const s
     const size_t b = (size_t)n * 16;
     if (n > 0) {
         CK(c, cudaMemcpyAsync(c->pos_u, pos, b, cudaMemcpyHostToDevice, c->stream));
-        // veleval, then vel, follow on the side stream once pos is in (the
-        // link is not shared with it): the next step's hash and sort, which
-        // read only pos, run meanwhile; its permute needs veleval, and only
-        // its force pass (the integrator) needs vel
+        // veleval and vel follow on the side stream once pos is in (the link
+        // is not shared with it): the next fused step's hash, sort, permute
+        // and density, which read only pos, run meanwhile
         CK(c, cudaEventRecord(c->up_start, c->stream));
         CK(c, cudaStreamWaitEvent(c->up_stream, c->up_start, 0));
         if (veleval)
             CK(c, cudaMemcpyAsync(c->veleval_u, veleval, b, cudaMemcpyHostToDevice, c->up_stream));
         else
             CK(c, cudaMemsetAsync(c->veleval_u, 0, b, c->up_stream));
-        CK(c, cudaEventRecord(c->up_veleval, c->up_stream));
         CK(c, cudaMemcpyAsync(c->vel_u, vel, b, cudaMemcpyHostToDevice, c->up_stream));
         CK(c, cudaEventRecord(c->up_done, c->up_stream));
         c->up_pending = true;
@@ -1045,7 +1036,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step; with a triangle mesh the step is staged");
     if (!c->hoses.empty()) return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step without hoses");
     // Launches of one fused step: count, totals, scan, place, permute,
-    // density, deletion bookkeeping, force+collision+leapfrog.
+    // density, velocity pass, force+collision+leapfrog.
     const int nk = 8;
     if (nkernels) *nkernels = nk;
     for (int k = 0; k < cap; ++k) kernel_ms[k] = 0.f;
@@ -1066,12 +1057,13 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_permute(c->cell_entries, c->cell_start, c->cell_end, c->keys_a, c->idx_a, c->pos_u,
-                                  c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, 1,
+                                  c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, 0,
                                   st);
         CK(c, cudaEventRecord(ev[e++], st));
         density_launch(c, true, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_step_deletion(c->pos_s, c->idx_a, c->vel_u, c->vel_s, c->del_pos, c->del_vel, c->info, st);
+        sphk::launch_step_velocities(c->pos_s, c->idx_a, c->vel_u, c->veleval_u, c->rec_vi, c->vel_s, c->del_pos,
+                                     c->del_vel, c->info, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
         force_launch(c, c->idx_a, true, dt, st);
         CK(c, cudaEventRecord(ev[e++], st));
@@ -1091,7 +1083,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
 
 const char* sph_profile_kernel_name(sph_ctx* c, int k) {
     static const char* names[] = {"k_cell_count", "k_cell_totals", "k_cell_scan", "k_cell_place",
-                                  "k_cell_permute", "k_density", "k_step_deletion",
+                                  "k_cell_permute", "k_density", "k_step_velocities",
                                   "k_force(fused collision+leapfrog)"};
     if (!c || k < 0 || k >= 8) return "";
     return names[k];

@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(256) k_cell_place(const uint32_t* __restrict__
 
 // ---------------------------------------------------------------------------
 // Permute: rank within the cell, then the sorted arrays.
-// Gather: 1 = pos/veleval, 2 = pos/vel/veleval.
+// Gather: 0 = pos (the fused step gathers veleval later, beside the density
+// pass), 1 = pos/veleval, 2 = pos/vel/veleval.
 template <int Gather>
 __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ entries,
                                                       const uint32_t* __restrict__ cell_start,
@@ -253,8 +254,8 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
     const uint32_t id = e.x, key = e.y;
     // the gathers do not depend on the rank: in flight during the ranking
     const float4 pq = __ldg(pos_u + id);
-    const float4 vq = __ldg(veleval_u + id);
-    float4 wq = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 vq = make_float4(0.f, 0.f, 0.f, 0.f), wq = vq;
+    if (Gather >= 1) vq = __ldg(veleval_u + id);
     if (Gather == 2) wq = __ldg(vel_u + id);
     const uint32_t cs = __ldg(cell_start + key), ce = __ldg(cell_end + key);
     // every entry lies in a cell of [cs, ce) within [0, n) when the counts
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
     keys[s] = key;  // one key over the whole cell
     idx[p] = id;
     pos_s[p] = pq;
-    veleval_s[p] = vq;
+    if (Gather >= 1) veleval_s[p] = vq;
     if (Gather == 2) vel_s[p] = wq;
 }
 
@@ -305,8 +306,11 @@ void launch_cell_permute(const uint2* entries, const uint32_t* cell_start, const
     if (gather == 2)
         k_cell_permute<2><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
                                                   pos_s, vel_s, veleval_s, info);
-    else
+    else if (gather == 1)
         k_cell_permute<1><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
+                                                  pos_s, vel_s, veleval_s, info);
+    else
+        k_cell_permute<0><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
                                                   pos_s, vel_s, veleval_s, info);
 }
 

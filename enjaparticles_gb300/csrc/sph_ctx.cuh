@@ -15,15 +15,14 @@ struct sph_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
-    // sph_upload copies veleval, then vel, on up_stream after the position
-    // copy, so that they overlap the step's first passes: up_veleval marks the
-    // veleval copy (the step waits for it before the permute), up_done the
-    // end of both (the step waits for it before the force pass; every other
-    // call waits for it on entry).
+    // sph_upload copies veleval and vel on up_stream after the position copy,
+    // so that they overlap the fused step's sort and density passes; up_done
+    // marks their end (the fused step's velocity pass waits for it; every
+    // other call waits for it on entry).
     cudaStream_t up_stream = nullptr;
-    cudaEvent_t up_start = nullptr, up_veleval = nullptr, up_done = nullptr;
-    // the fused step's deletion bookkeeping runs on side_stream beside the
-    // density pass (after the permute and the velocity upload, before force)
+    cudaEvent_t up_start = nullptr, up_done = nullptr;
+    // the fused step's velocity pass runs on side_stream beside the density
+    // pass (after the permute and the velocity upload, before force)
     cudaStream_t side_stream = nullptr;
     cudaEvent_t side_fork = nullptr, side_join = nullptr;
     bool up_pending = false;
@@ -107,7 +106,6 @@ int check_ctx(sph_ctx* c, bool join = true);
 // (an external event wait node when the stream is being captured).
 int join_upload(sph_ctx* c);
 int join_upload_on(sph_ctx* c, cudaStream_t st);
-int join_upload_veleval(sph_ctx* c);
 // Enqueues one fused step (hash .. leapfrog) on c->stream.
 int enqueue_fused_step(sph_ctx* c, float dt);
 // Reads the device counters into c->host_info (synchronises the stream).

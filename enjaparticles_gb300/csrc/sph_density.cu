@@ -13,7 +13,9 @@
 //
 // nbr (neighbour counts) is optional: the fused step leaves it out.  The
 // fused step's out-of-grid bookkeeping is its own kernel (sph_integrate.cu),
-// so this pass reads no velocity.
+// so this pass reads no velocity.  veleval_s is optional too: without it the
+// pass writes only the 1/rho lane of rec_vi, and the fused step's velocity
+// kernel fills the veleval lanes beside it.
 //
 // While it tests the candidates the pass also records, per particle, which of
 // its first kMaskBits candidates (in walk order) are neighbours (self
@@ -42,7 +44,10 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
     if (R.frozen(i)) {
         density[i] = 0.f;
         rec_pd[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
-        rec_vi[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (veleval_s != nullptr)
+            rec_vi[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else
+            reinterpret_cast<float*>(rec_vi + i)[3] = 0.f;
         if (WantCount) nbr[i] = 0;
         return;
     }
@@ -99,9 +104,13 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
     }
     const float rho = __fmul_rn(P.dens_coef, acc);
     density[i] = rho;
-    const float4 ve = __ldg(veleval_s + i);
     rec_pd[i] = make_float4(pi.x, pi.y, pi.z, rho);
-    rec_vi[i] = make_float4(ve.x, ve.y, ve.z, __frcp_rn(rho));
+    if (veleval_s != nullptr) {
+        const float4 ve = __ldg(veleval_s + i);
+        rec_vi[i] = make_float4(ve.x, ve.y, ve.z, __frcp_rn(rho));
+    } else {
+        reinterpret_cast<float*>(rec_vi + i)[3] = __frcp_rn(rho);
+    }
     if (WantCount) nbr[i] = cnt;
 }
 

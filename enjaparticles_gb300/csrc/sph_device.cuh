@@ -168,12 +168,13 @@ void launch_cells_permute(const uint32_t* keys, const uint32_t* idx, uint32_t* c
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, cudaStream_t st);
-// The fused step's out-of-grid bookkeeping, after density and before force
-// (the first pass that needs vel_u): kept velocities into vel_s in sorted
-// order, removed particles into del_pos/del_vel.  Exits at once when nothing
-// left the grid.
-void launch_step_deletion(const float4* pos_s, const uint32_t* idx, const float4* vel_u, float4* vel_s,
-                          float4* del_pos, float4* del_vel, int* info, cudaStream_t st);
+// The fused step's velocity pass, beside density and before force (the first
+// passes that need the uploaded velocities): the veleval lanes of rec_vi in
+// sorted order, and the out-of-grid bookkeeping (kept velocities into vel_s
+// in sorted order, removed particles into del_pos/del_vel).
+void launch_step_velocities(const float4* pos_s, const uint32_t* idx, const float4* vel_u, const float4* veleval_u,
+                            float4* rec_vi, float4* vel_s, float4* del_pos, float4* del_vel, int* info, int grid_items,
+                            cudaStream_t st);
 // keep_f / keep_v (fused only, nullable): per sorted particle, the SPH force
 // before the walls and the velocity the step integrates.
 void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,

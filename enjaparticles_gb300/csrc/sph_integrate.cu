@@ -98,34 +98,47 @@ void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_
     k_euler<<<blocks, 256, 0, st>>>(pos_s, vel_s, force_s, idx, pos_u, vel_u, info, p, dt);
 }
 
-// Fused step's deletion (SPH.cpp:220-250): the kept particles' velocities in
-// sorted order (call_prep copies vel_s to vel_u, done by the force pass, which
-// re-indexes them), the removed ones saved.  A grid-stride loop over a few
-// blocks per SM: the common step, where nothing left the grid, costs one
-// read of info per block.
-__global__ void __launch_bounds__(256) k_step_deletion(const float4* __restrict__ pos_s,
-                                                       const uint32_t* __restrict__ idx,
-                                                       const float4* __restrict__ vel_u, float4* __restrict__ vel_s,
-                                                       float4* __restrict__ del_pos, float4* __restrict__ del_vel,
-                                                       int* __restrict__ info) {
+// The fused step's velocity pass, once vel and veleval are uploaded, beside
+// the density pass (which writes the 1/rho lane of rec_vi):
+//   - the veleval lanes of the force pass's neighbour records, in sorted
+//     order (the gather permute.cl:10-46 does into veleval_s);
+//   - the out-of-grid deletion (SPH.cpp:220-250): the kept particles'
+//     velocities in sorted order (call_prep copies vel_s to vel_u, done by the
+//     force pass, which re-indexes them), the removed ones saved.
+__global__ void __launch_bounds__(256) k_step_velocities(const float4* __restrict__ pos_s,
+                                                         const uint32_t* __restrict__ idx,
+                                                         const float4* __restrict__ vel_u,
+                                                         const float4* __restrict__ veleval_u,
+                                                         float4* __restrict__ rec_vi, float4* __restrict__ vel_s,
+                                                         float4* __restrict__ del_pos, float4* __restrict__ del_vel,
+                                                         int* __restrict__ info) {
     int n_old, out;
     const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_old) return;
+    const uint32_t o = __ldg(idx + i);
+    if (i < n) {
+        const float4 ve = __ldg(veleval_u + o);
+        float* r = reinterpret_cast<float*>(rec_vi + i);
+        *reinterpret_cast<float2*>(r) = make_float2(ve.x, ve.y);
+        r[2] = ve.z;
+    }
     if (out < 0) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old; i += gridDim.x * blockDim.x) {
-        const float4 v = __ldg(vel_u + __ldg(idx + i));
-        if (i < n) {
-            vel_s[i] = v;
-        } else {
-            del_pos[i - n] = __ldg(pos_s + i);
-            del_vel[i - n] = v;
-            if (i == n) info[kDeleted] = n_old - n;
-        }
+    const float4 v = __ldg(vel_u + o);
+    if (i < n) {
+        vel_s[i] = v;
+    } else {
+        del_pos[i - n] = __ldg(pos_s + i);
+        del_vel[i - n] = v;
+        if (i == n) info[kDeleted] = n_old - n;
     }
 }
 
-void launch_step_deletion(const float4* pos_s, const uint32_t* idx, const float4* vel_u, float4* vel_s,
-                          float4* del_pos, float4* del_vel, int* info, cudaStream_t st) {
-    k_step_deletion<<<152 * 4, 256, 0, st>>>(pos_s, idx, vel_u, vel_s, del_pos, del_vel, info);
+void launch_step_velocities(const float4* pos_s, const uint32_t* idx, const float4* vel_u, const float4* veleval_u,
+                            float4* rec_vi, float4* vel_s, float4* del_pos, float4* del_vel, int* info, int grid_items,
+                            cudaStream_t st) {
+    const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
+    k_step_velocities<<<blocks, 256, 0, st>>>(pos_s, idx, vel_u, veleval_u, rec_vi, vel_s, del_pos, del_vel, info);
 }
 
 // Staged deletion: after cellindices + permute, when some particles left the
