@@ -199,10 +199,10 @@ int sph_set_stream(sph_ctx* ctx, void* stream);
 /* Replace the state with n particles.  veleval may be NULL: it is then zero,
  * as in the reference, where pushParticles never writes veleval.  Host
  * pointers; pinned memory makes the copy asynchronous.  pos is copied on the
- * context stream, veleval and then vel after it on a side stream: the next
- * fused step waits for veleval only before its permute and for vel only
- * before its force pass, so they overlap its hash, sort and density; every
- * other call waits for both on entry.  Host arrays must stay
+ * context stream, veleval and vel after it on a side stream: the next fused
+ * step waits for them only in its velocity pass, which runs beside its
+ * density pass, so they overlap its hash, sort, permute and density; every
+ * other call waits for them on entry.  Host arrays must stay
  * valid until the next call that waits (sph_sync, a download, ...). */
 int sph_upload(sph_ctx* ctx, const sph_float4* pos, const sph_float4* vel,
                const sph_float4* veleval, int n);
