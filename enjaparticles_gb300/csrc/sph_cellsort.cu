@@ -22,8 +22,12 @@
 //   place    each particle's (index, key) at cell_start[key] + slot.
 //   permute  slots within a cell come in atomic order, so each sorted
 //            position ranks its particle index among the entries of its cell
-//            and writes index, key and the gathered pos/veleval(/vel) at
-//            cell_start + rank.
+//            and writes index, key and the gathered pos at cell_start + rank
+//            (vel and veleval too for the staged update; the fused step
+//            gathers veleval in its velocity pass, sph_integrate.cu).
+//
+// The batched step (sph_batch.cu) runs the totals and scan passes over the
+// cells of all its scenes, with its own count, place and permute.
 //
 // The ranking reads every entry of a cell once per entry: quadratic in the
 // occupancy of one cell, as the neighbour passes are (they walk every entry of
