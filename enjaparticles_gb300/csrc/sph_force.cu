@@ -136,6 +136,8 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     const uint32_t* mrow = mask + i;
     const uint32_t mbits = M < (uint32_t)kMaskBits ? M : (uint32_t)kMaskBits;
     uint32_t w = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
+    // the next mask word, in flight while this one's neighbours are processed
+    uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     uint32_t q = (uint32_t)kMaskBits;  // next candidate past the bitmask to test
     int r = 0;
     for (;;) {
@@ -144,7 +146,8 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
         uint32_t p = 0;
         while (m == 0 && (w + 1) * 32u < mbits) {
             ++w;
-            m = __ldg(mrow + (size_t)w * mstride);
+            m = m_next;
+            m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
         }
         if (m != 0) {
             p = w * 32u + (uint32_t)(__ffs(m) - 1);
