@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     uint32_t M = 0;
     const int3 c = grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
     if (cell_fast(P, c)) {
-        walk_rows_fast(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {  // at most 9 runs
+        walk_rows_fast_batched(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {  // at most 9 runs
             s_rs[nrows][t] = rs;
             s_off[nrows][t] = M;
             M += re - rs;

@@ -56,6 +56,45 @@ __device__ __forceinline__ void walk_rows_fast(const StepParams& P, const uint32
     }
 }
 
+// The same 9 row runs as walk_rows_fast, in the same order, with every
+// cell_start load of the 27 cells issued before any is used and the 9
+// cell_end loads issued together after them: two memory round trips instead
+// of two per row, for callers that do little per run (the force pass only
+// records the runs).
+template <class F>
+__device__ __forceinline__ void walk_rows_fast_batched(const StepParams& P, const uint32_t* __restrict__ cs,
+                                                       const uint32_t* __restrict__ ce, const int3& c, F&& f) {
+    const uint32_t C = (uint32_t)P.nb_cells;
+    uint32_t s[27];
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const int base = ((c.z + r / 3 - 1) * P.res_y + (c.y + r % 3 - 1)) * P.res_x + c.x;
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+            const uint32_t h = (uint32_t)(base + dx - 1);
+            s[3 * r + dx] = h < C ? __ldg(cs + h) : kEmpty;
+        }
+    }
+    uint32_t rs[9], re[9];
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const int base = ((c.z + r / 3 - 1) * P.res_y + (c.y + r % 3 - 1)) * P.res_x + c.x;
+        rs[r] = kEmpty;
+        uint32_t last = 0;
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+            if (s[3 * r + dx] != kEmpty) {
+                if (rs[r] == kEmpty) rs[r] = s[3 * r + dx];
+                last = (uint32_t)(base + dx - 1);
+            }
+        }
+        re[r] = rs[r] != kEmpty ? __ldg(ce + last) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+        if (rs[r] != kEmpty) f(rs[r], re[r]);
+}
+
 // The 27 cells one by one with the reference's float hash (up to 27 calls).
 template <class F>
 __device__ __forceinline__ void walk_rows_slow(const StepParams& P, const uint32_t* __restrict__ cs,
