@@ -172,7 +172,7 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
     uint32_t M = 0;
     const int3 c = sphk::grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
     if (sphk::cell_fast(P, c)) {
-        sphk::walk_rows_fast(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {
+        sphk::walk_rows_fast_batched(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {
             s_rs[nrows][t] = rs;
             s_off[nrows][t] = M;
             M += re - rs;
@@ -191,6 +191,8 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
     const uint32_t* mrow = T.mask + i;
     const uint32_t mbits = M < (uint32_t)sphk::kMaskBits ? M : (uint32_t)sphk::kMaskBits;
     uint32_t w = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
+    // the next mask word, in flight while this one's neighbours are processed
+    uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     uint32_t q = (uint32_t)sphk::kMaskBits;
     int r = 0;
     for (;;) {
@@ -198,7 +200,8 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
         uint32_t p = 0;
         while (m == 0 && (w + 1) * 32u < mbits) {
             ++w;
-            m = __ldg(mrow + (size_t)w * mstride);
+            m = m_next;
+            m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
         }
         if (m != 0) {
             p = w * 32u + (uint32_t)(__ffs(m) - 1);
