@@ -69,7 +69,9 @@ __device__ __forceinline__ void force_pair(ForceSums& a, const float4& pi, const
         a.vx = fmaf(dvx, vh, a.vx);
         a.vy = fmaf(dvy, vh, a.vy);
         a.vz = fmaf(dvz, vh, a.vz);
-        const float wx = w6 * __frcp_rn(dsum);
+        // the fast division (a few ulp): the XSPH weight is a smoothing term,
+        // far inside the default mode's 1e-5 tolerance
+        const float wx = __fdividef(w6, dsum);
         a.xx = fmaf(wx, dvx, a.xx);
         a.xy = fmaf(wx, dvy, a.xy);
         a.xz = fmaf(wx, dvz, a.xz);
