@@ -101,6 +101,7 @@ int sph_make_step_params(const SPHParams& s, const GridParams& gp, const GridPar
     P.rho0 = s.rest_density;
     P.K = s.K;
     P.eps = s.EPSILON;
+    P.inv_eps = 1.0f / s.EPSILON;
     P.visc = s.viscosity;
     P.wpoly6 = s.wpoly6_coef;
     P.wspiky_d = s.wspiky_d_coef;

@@ -48,6 +48,7 @@ struct StepParams {
     float coef_b;      // (float)(-0.5 * (double)wspiky_d)
     float coef_s;      // viscosity * wvisc_dd (float)
     float coef_d;      // (float)(2.0 * (double)mass * (double)wpoly6)
+    float inv_eps;     // 1 / eps, correctly rounded (the force pass's clamp)
     // unscaled grid (hash) and scaled grid (neighbour walk, walls)
     float4 g_min, g_delta, g_res;
     float4 gs_min, gs_delta, gs_res, gs_bnd_min, gs_bnd_max;

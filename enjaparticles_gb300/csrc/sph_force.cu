@@ -61,7 +61,7 @@ __device__ __forceinline__ void force_pair(ForceSums& a, const float4& pi, const
         float irl = inv_r;
         if (!(rlen >= P.eps)) {
             rlen = P.eps;
-            irl = __frcp_rn(P.eps);
+            irl = P.inv_eps;
         }
         const float hr = P.h - rlen;
         const float kern = hr * hr * irl * ((Pi + Pj) * idj);
