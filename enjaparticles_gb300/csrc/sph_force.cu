@@ -89,9 +89,10 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     float4* __restrict__ xsph_s, uint32_t* __restrict__ idx, const float4* __restrict__ vel_s,
     float4* __restrict__ pos_u, float4* __restrict__ vel_u, float4* __restrict__ veleval_u,
     float4* __restrict__ keep_f, float4* __restrict__ keep_v, const Scenes R, const float dt) {
-    // Row table of each thread: sorted index of the run's first candidate and
-    // walk-order offset of it; rows without candidates are left out.
-    __shared__ uint32_t s_rs[9][kForceThreads];
+    // Row table of each thread: walk-order offset of the run's first
+    // candidate, and sorted index minus walk-order position over the run
+    // (j = p + delta, modulo 2^32); rows without candidates are left out.
+    __shared__ uint32_t s_delta[9][kForceThreads];
     __shared__ uint32_t s_off[10][kForceThreads];
     int n_old, out;
     const int n = effective_num(info, n_old, out);
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     const int3 c = grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
     if (cell_fast(P, c)) {
         walk_rows_fast_batched(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {  // at most 9 runs
-            s_rs[nrows][t] = rs;
+            s_delta[nrows][t] = rs - M;
             s_off[nrows][t] = M;
             M += re - rs;
             ++nrows;
@@ -142,6 +143,7 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     uint32_t q = (uint32_t)kMaskBits;  // next candidate past the bitmask to test
     int r = 0;
+    uint32_t next_off = s_off[1][t], delta = s_delta[0][t];  // row r's end and index offset
     for (;;) {
         // next neighbour of this lane, as its walk-order position p
         bool have = false;
@@ -158,8 +160,12 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
         } else {
             while (q < M) {
                 const uint32_t pp = q++;
-                while (pp >= s_off[r + 1][t]) ++r;
-                const uint32_t j = s_rs[r][t] + (pp - s_off[r][t]);
+                while (pp >= next_off) {
+                    ++r;
+                    next_off = s_off[r + 1][t];
+                    delta = s_delta[r][t];
+                }
+                const uint32_t j = pp + delta;
                 const float4 pj = __ldg(rec_pd + j);
                 const float r2 = dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
                 // The self term is multiplied by iej = 0 in the reference
@@ -173,8 +179,12 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
         }
         if (!__any_sync(wmask, have)) break;
         if (have) {
-            while (p >= s_off[r + 1][t]) ++r;
-            const uint32_t j = s_rs[r][t] + (p - s_off[r][t]);
+            while (p >= next_off) {
+                ++r;
+                next_off = s_off[r + 1][t];
+                delta = s_delta[r][t];
+            }
+            const uint32_t j = p + delta;
             force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
         }
     }
