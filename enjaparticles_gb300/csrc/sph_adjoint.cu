@@ -173,7 +173,7 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
     const int3 c = sphk::grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
     if (sphk::cell_fast(P, c)) {
         sphk::walk_rows_fast_batched(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {
-            s_rs[nrows][t] = rs;
+            s_rs[nrows][t] = rs - M;  // sorted index minus walk position over the run
             s_off[nrows][t] = M;
             M += re - rs;
             ++nrows;
@@ -195,6 +195,7 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
     uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     uint32_t q = (uint32_t)sphk::kMaskBits;
     int r = 0;
+    uint32_t next_off = s_off[1][t], delta = s_rs[0][t];  // row r's end and index offset
     for (;;) {
         bool have = false;
         uint32_t p = 0;
@@ -210,8 +211,12 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
         } else {
             while (q < M) {
                 const uint32_t pp = q++;
-                while (pp >= s_off[r + 1][t]) ++r;
-                const uint32_t j = s_rs[r][t] + (pp - s_off[r][t]);
+                while (pp >= next_off) {
+                    ++r;
+                    next_off = s_off[r + 1][t];
+                    delta = s_rs[r][t];
+                }
+                const uint32_t j = pp + delta;
                 const float4 pj = __ldg(T.rec_pd + j);
                 const float r2 = sphk::dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
                 if (r2 <= rc2 && j != (uint32_t)i) {
@@ -223,8 +228,12 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
         }
         if (!__any_sync(wmask, have)) break;
         if (have) {
-            while (p >= s_off[r + 1][t]) ++r;
-            fn(s_rs[r][t] + (p - s_off[r][t]));
+            while (p >= next_off) {
+                ++r;
+                next_off = s_off[r + 1][t];
+                delta = s_rs[r][t];
+            }
+            fn(p + delta);
         }
     }
 }
