@@ -3,6 +3,8 @@
 // XSPH), with the wall collision and leapfrog integration of the step fused in.
 // Compiled with FMA contraction allowed: the default (fast) arithmetic uses
 // it; the exact variant spells every operation with a rounding intrinsic.
+#include <type_traits>
+
 #include "sph_walk.cuh"
 
 namespace sphk {
@@ -143,7 +145,29 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     uint32_t q = (uint32_t)kMaskBits;  // next candidate past the bitmask to test
     int r = 0;
-    uint32_t next_off = s_off[1][t], delta = s_delta[0][t];  // row r's end and index offset
+    // One scene: row r's end and index offset in registers, reloaded when the
+    // cursor changes row.  Batches read them from shared memory: with the
+    // scene lookups the registers would spill (measured slower).
+    constexpr bool kRegCursor = std::is_same<Scenes, OneScene>::value;
+    uint32_t next_off = 0, delta = 0;
+    if constexpr (kRegCursor) {
+        next_off = s_off[1][t];
+        delta = s_delta[0][t];
+    }
+    // sorted index of the candidate at walk position p, advancing row r
+    auto index_of = [&](uint32_t p) -> uint32_t {
+        if constexpr (kRegCursor) {
+            while (p >= next_off) {
+                ++r;
+                next_off = s_off[r + 1][t];
+                delta = s_delta[r][t];
+            }
+            return p + delta;
+        } else {
+            while (p >= s_off[r + 1][t]) ++r;
+            return p + s_delta[r][t];
+        }
+    };
     for (;;) {
         // next neighbour of this lane, as its walk-order position p
         bool have = false;
@@ -160,12 +184,7 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
         } else {
             while (q < M) {
                 const uint32_t pp = q++;
-                while (pp >= next_off) {
-                    ++r;
-                    next_off = s_off[r + 1][t];
-                    delta = s_delta[r][t];
-                }
-                const uint32_t j = pp + delta;
+                const uint32_t j = index_of(pp);
                 const float4 pj = __ldg(rec_pd + j);
                 const float r2 = dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
                 // The self term is multiplied by iej = 0 in the reference
@@ -179,12 +198,7 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
         }
         if (!__any_sync(wmask, have)) break;
         if (have) {
-            while (p >= next_off) {
-                ++r;
-                next_off = s_off[r + 1][t];
-                delta = s_delta[r][t];
-            }
-            const uint32_t j = p + delta;
+            const uint32_t j = index_of(p);
             force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
         }
     }
