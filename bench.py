@@ -49,8 +49,8 @@ FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) of one launch, from an ncu capture of the 2M step
 # (profiles/sph_density_force_2M.md); reported as roofline.traffic for the
 # dominant kernel when it is one of these.
-MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 203.5776e6 + 70.55232e6,
-                    "k_density": 55.80928e6 + 75.27552e6}
+MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 203.607552e6 + 72.219392e6,
+                    "k_density": 55.70176e6 + 74.822144e6}
 
 
 def parse():
