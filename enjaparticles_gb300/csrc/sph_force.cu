@@ -13,14 +13,16 @@ namespace sphk {
 // Force (+ collision + leapfrog when Fused).
 //
 // One thread per sorted particle.  The thread first lays out its 9 row runs
-// (sorted-index start and walk-order offset of each) in shared memory, then
-// walks its neighbours with a cursor over the density pass's bitmask
-// (candidates past kMaskBits are tested).  The warp advances all cursors in
-// lock step, one neighbour per lane per iteration, and runs the pair
-// arithmetic for every lane in the same iteration, until no lane has a
-// neighbour left: lanes never serialise on each other's neighbour lists.
-// Neighbour data is the 32-byte record (x, y, z, rho), (veleval.xyz, 1/rho)
-// written by the density pass, read through L1.
+// in shared memory (walk-order offset of each, and sorted index minus walk
+// position over it), from cell range loads issued together, then walks its
+// neighbours with a cursor over the density pass's bitmask (candidates past
+// kMaskBits are tested), the next mask word already in flight.  The warp
+// advances all cursors in lock step, one neighbour per lane per iteration,
+// and runs the pair arithmetic for every lane in the same iteration, until no
+// lane has a neighbour left: lanes never serialise on each other's neighbour
+// lists.  Neighbour data is the 32-byte record (x, y, z, rho),
+// (veleval.xyz, 1/rho) written by the density pass and the velocity pass,
+// read through L1.
 constexpr int kForceThreads = 128;
 
 struct ForceSums {
