@@ -351,32 +351,32 @@ static int enqueue_update(sph_ctx* c) {
 }
 
 int enqueue_fused_step(sph_ctx* c, float dt) {
-    if (c->n_tri > 0) {
-        // the triangle stage sits between the walls and the integrator: the
-        // staged passes up to force, then one kernel for gravity, walls,
-        // triangles and the integrator
-        int rc = enqueue_to_force(c);
-        if (rc) return rc;
-        sphk::launch_triangles_step(c->pos_s, c->vel_s, c->force_s, c->xsph_s, c->idx_a, c->pos_u, c->vel_u,
-                                    c->veleval_u, c->info, c->P, dt, c->num_hint, c->stream);
-        CK_LAUNCH(c);
-        return SPH_OK;
-    }
+    const bool mesh = c->n_tri > 0;
     int rc = enqueue_cell_sort(c, 0);
     if (rc) return rc;
     // beside the density pass, on the side stream, once the velocities are
     // in: the veleval lanes of the neighbour records and the deletion
     // bookkeeping (they and the integrator are the step's only readers of
-    // the uploaded velocities)
+    // the uploaded velocities; with a mesh, also the sorted velocities the
+    // triangle kernel reads)
     CK(c, cudaEventRecord(c->side_fork, c->stream));
     CK(c, cudaStreamWaitEvent(c->side_stream, c->side_fork, 0));
     density_launch(c, true, c->stream);
     if ((rc = join_upload_on(c, c->side_stream))) return rc;
     sphk::launch_step_velocities(c->pos_s, c->idx_a, c->vel_u, c->veleval_u, c->rec_vi, c->vel_s, c->del_pos,
-                                 c->del_vel, c->info, c->num_hint, c->side_stream);
+                                 c->del_vel, c->info, mesh ? 1 : 0, c->num_hint, c->side_stream);
     CK(c, cudaEventRecord(c->side_join, c->side_stream));
     CK(c, cudaStreamWaitEvent(c->stream, c->side_join, 0));
-    force_launch(c, c->idx_a, true, dt, c->stream);
+    if (mesh) {
+        // the triangle stage sits between the walls and the integrator: the
+        // force pass without them, then one kernel for gravity, walls,
+        // triangles and the integrator
+        force_launch(c, c->idx_a, false, 0.f, c->stream);
+        sphk::launch_triangles_step(c->pos_s, c->vel_s, c->force_s, c->xsph_s, c->idx_a, c->pos_u, c->vel_u,
+                                    c->veleval_u, c->info, c->P, dt, c->num_hint, c->stream);
+    } else {
+        force_launch(c, c->idx_a, true, dt, c->stream);
+    }
     CK_LAUNCH(c);
     return SPH_OK;
 }
@@ -1034,7 +1034,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
     if (nsteps < 0 || !std::isfinite(dt) || !kernel_ms || cap <= 0)
         return set_err(c, SPH_EINVAL, "sph_step_profile: bad arguments");
     if (c->n_tri > 0)
-        return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step; with a triangle mesh the step is staged");
+        return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step without a triangle mesh");
     if (!c->hoses.empty()) return set_err(c, SPH_ESTATE, "sph_step_profile times the fused step without hoses");
     // Launches of one fused step: count, totals, scan, place, permute,
     // density, velocity pass, force+collision+leapfrog.
@@ -1064,7 +1064,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         density_launch(c, true, st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_step_velocities(c->pos_s, c->idx_a, c->vel_u, c->veleval_u, c->rec_vi, c->vel_s, c->del_pos,
-                                     c->del_vel, c->info, c->num_hint, st);
+                                     c->del_vel, c->info, 0, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
         force_launch(c, c->idx_a, true, dt, st);
         CK(c, cudaEventRecord(ev[e++], st));

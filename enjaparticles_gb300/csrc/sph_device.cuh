@@ -172,10 +172,11 @@ void launch_density(const float4* pos_s, const float4* veleval_s, float* density
 // The fused step's velocity pass, beside density and before force (the first
 // passes that need the uploaded velocities): the veleval lanes of rec_vi in
 // sorted order, and the out-of-grid bookkeeping (kept velocities into vel_s
-// in sorted order, removed particles into del_pos/del_vel).
+// in sorted order, removed particles into del_pos/del_vel); all_vel: vel_s of
+// every kept particle in every step.
 void launch_step_velocities(const float4* pos_s, const uint32_t* idx, const float4* vel_u, const float4* veleval_u,
-                            float4* rec_vi, float4* vel_s, float4* del_pos, float4* del_vel, int* info, int grid_items,
-                            cudaStream_t st);
+                            float4* rec_vi, float4* vel_s, float4* del_pos, float4* del_vel, int* info, int all_vel,
+                            int grid_items, cudaStream_t st);
 // keep_f / keep_v (fused only, nullable): per sorted particle, the SPH force
 // before the walls and the velocity the step integrates.
 void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
@@ -206,7 +207,7 @@ void launch_triangles(const float4* pos_s, const float4* vel_s, float4* force_s,
 // The end of the step with a mesh: gravity, walls, triangles and the
 // integrator in one kernel after the (unfused) force pass.
 void launch_triangles_step(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
-                           const uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
+                           uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
                            const StepParams& p, float dt, int grid_items, cudaStream_t st);
 void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_s, uint32_t* idx, float4* pos_u,
                   float4* vel_u, const int* info, const StepParams& p, float dt, int grid_items, cudaStream_t st);

@@ -104,14 +104,16 @@ void launch_euler(const float4* pos_s, const float4* vel_s, const float4* force_
 //     order (the gather permute.cl:10-46 does into veleval_s);
 //   - the out-of-grid deletion (SPH.cpp:220-250): the kept particles'
 //     velocities in sorted order (call_prep copies vel_s to vel_u, done by the
-//     force pass, which re-indexes them), the removed ones saved.
+//     force pass, which re-indexes them), the removed ones saved;
+//   - with all_vel (the step with a triangle mesh, whose last kernel reads
+//     vel_s), the sorted velocities of every kept particle, deletion or not.
 __global__ void __launch_bounds__(256) k_step_velocities(const float4* __restrict__ pos_s,
                                                          const uint32_t* __restrict__ idx,
                                                          const float4* __restrict__ vel_u,
                                                          const float4* __restrict__ veleval_u,
                                                          float4* __restrict__ rec_vi, float4* __restrict__ vel_s,
                                                          float4* __restrict__ del_pos, float4* __restrict__ del_vel,
-                                                         int* __restrict__ info) {
+                                                         int* __restrict__ info, int all_vel) {
     int n_old, out;
     const int n = effective_num(info, n_old, out);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(256) k_step_velocities(const float4* __restric
         *reinterpret_cast<float2*>(r) = make_float2(ve.x, ve.y);
         r[2] = ve.z;
     }
-    if (out < 0) return;
+    if (out < 0 && !all_vel) return;
     const float4 v = __ldg(vel_u + o);
     if (i < n) {
         vel_s[i] = v;
@@ -135,10 +137,11 @@ __global__ void __launch_bounds__(256) k_step_velocities(const float4* __restric
 }
 
 void launch_step_velocities(const float4* pos_s, const uint32_t* idx, const float4* vel_u, const float4* veleval_u,
-                            float4* rec_vi, float4* vel_s, float4* del_pos, float4* del_vel, int* info, int grid_items,
-                            cudaStream_t st) {
+                            float4* rec_vi, float4* vel_s, float4* del_pos, float4* del_vel, int* info, int all_vel,
+                            int grid_items, cudaStream_t st) {
     const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
-    k_step_velocities<<<blocks, 256, 0, st>>>(pos_s, idx, vel_u, veleval_u, rec_vi, vel_s, del_pos, del_vel, info);
+    k_step_velocities<<<blocks, 256, 0, st>>>(pos_s, idx, vel_u, veleval_u, rec_vi, vel_s, del_pos, del_vel, info,
+                                              all_vel);
 }
 
 // Staged deletion: after cellindices + permute, when some particles left the

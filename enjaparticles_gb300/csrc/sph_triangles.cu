@@ -186,10 +186,12 @@ __device__ __forceinline__ bool box_holds(float4 lo, float4 hi, float4 p) {
 }
 
 // The rest of the step after the force pass, when the kernel ends it (Step):
-// sorted xsph and sort_indices in, the integrated state out.
+// sorted xsph and sort_indices in, the integrated state out.  After an
+// out-of-grid deletion the kept particles are re-indexed in sorted order
+// (sort_indices becomes the identity), as in the fused force pass.
 struct TriStepTail {
     const float4* xsph_s;
-    const uint32_t* idx;
+    uint32_t* idx;
     float4* pos_u;
     float4* vel_u;
     float4* veleval_u;
@@ -313,7 +315,13 @@ __global__ void __launch_bounds__(kTriThreads) k_triangles(const float4* __restr
         force_s[i] = ff;
         return;
     }
-    const uint32_t o = __ldg(S.idx + i);
+    uint32_t o;
+    if (out >= 0) {
+        o = (uint32_t)i;
+        S.idx[i] = o;
+    } else {
+        o = S.idx[i];
+    }
     float4 po, vo, eo;
     if (P.integrator == kIntegratorEuler) {
         euler_core(pos, vel, ff, S.dt, P, po, vo);
@@ -341,7 +349,7 @@ void launch_triangles(const float4* pos_s, const float4* vel_s, float4* force_s,
 }
 
 void launch_triangles_step(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
-                           const uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
+                           uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, const int* info,
                            const StepParams& p, float dt, int grid_items, cudaStream_t st) {
     if (p.n_tri <= 0) return;
     k_tri_prep<<<(p.n_tri + 255) / 256, 256, 0, st>>>(p.tri_raw, p.n_tri, p.tri_geo, p.tri_box, p);

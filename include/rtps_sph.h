@@ -385,9 +385,10 @@ int sph_integrate(sph_ctx* ctx, float dt);
 /* nsteps x (update + integrate) on the fused path: hash and sort (a counting
  * sort on the cell key, with the same canonical order as sph_stage_sort) ->
  * cellindices+permute -> density -> force+gravity+collision+integrator,
- * replayed from a captured CUDA graph.  With a triangle mesh loaded the graph holds the
- * staged launches of update + integrate instead.  Results equal nsteps staged
- * update()+integrate() calls.  Asynchronous. */
+ * replayed from a captured CUDA graph.  With a triangle mesh loaded the force
+ * pass leaves out the walls and the integrator, and one triangle kernel
+ * applies gravity, walls, triangles and the integrator.  Results equal
+ * nsteps staged update()+integrate() calls.  Asynchronous. */
 int sph_step(sph_ctx* ctx, float dt, int nsteps);
 
 /* The same fused step launched kernel by kernel, without a graph (for

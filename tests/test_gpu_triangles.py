@@ -114,6 +114,35 @@ def test_fused_exact_matches_reference_golden():
             np.testing.assert_array_equal(s.get(f), d["s%d_%s" % (k, f)], err_msg="step %d %s" % (k, f))
 
 
+def test_fused_with_mesh_and_deletion_equals_staged():
+    """With a mesh loaded, particles leaving the grid: the graph step (the
+    velocity pass's deletion bookkeeping, the triangle kernel's re-indexing)
+    equals staged update()+integrate() bit for bit, deleted particles
+    included."""
+    d, sp, g, gs = golden_io.load("triangles_n2048.npz")
+    pos = np.array(d["in_pos"], np.float32)
+    vel = np.array(d["in_vel"], np.float32)
+    sel = np.arange(0, pos.shape[0], 37)
+    pos[sel, 2] = np.float32(5.0)  # far above the grid: deleted by the step
+    dt = float(d["dt"])
+    out = {}
+    for mode in ("staged", "graph"):
+        s = SPH(sp, g, pos.shape[0], gs, exact=True)
+        s.loadTriangles(d["triangles"])
+        s.upload(pos, vel)
+        for _ in range(3):
+            if mode == "staged":
+                s.update()
+                s.integrate(dt)
+            else:
+                s.step(dt, 1)
+        out[mode] = [s.getNum()] + [s.get(f) for f in STATE] + list(s.getDeleted())
+        s.close()
+    assert out["graph"][0] == out["staged"][0] == pos.shape[0] - len(sel)
+    for a, b, name in zip(out["graph"][1:], out["staged"][1:], STATE + ("deleted pos", "deleted vel")):
+        np.testing.assert_array_equal(a, b, err_msg=name)
+
+
 def test_fast_within_tolerance_of_reference_golden():
     d, sp, g, gs = golden_io.load("triangles_n2048.npz")
     s = _system(d, sp, g, gs, exact=False)
