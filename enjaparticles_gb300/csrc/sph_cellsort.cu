@@ -14,6 +14,9 @@
 //   totals   the number of particles in each tile of 4096 cells; the first
 //            thread also applies the previous step's out-of-grid deletion to
 //            the particle count (count derives the same number on its own).
+//            Grids of more than kDirectTiles tiles then scan the totals in
+//            one block; smaller ones let every scan block sum the totals
+//            before its tile itself (one launch fewer).
 //   scan     an exclusive scan of the counts, one block per tile, its base the
 //            sum of the totals of the tiles before it (no block waits on
 //            another), writes cell_start (kEmpty for an empty cell) and
@@ -47,6 +50,7 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 cells per tile
 constexpr int kItems = 4;                               // particles per thread in count and place
+constexpr int kTileScanThreads = 1024;
 
 }  // namespace
 
@@ -143,20 +147,56 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_totals(const uint32_t* __
     }
 }
 
+// Tile scan (grids of more than kDirectTiles tiles): tile_total becomes the
+// exclusive prefix of the totals, in one block.
+__global__ void __launch_bounds__(kTileScanThreads) k_cell_tile_scan(uint32_t* __restrict__ tile_total, int tiles) {
+    __shared__ uint32_t s_warp[kTileScanThreads / 32];
+    __shared__ uint32_t s_carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_carry = 0;
+    for (int k0 = 0; k0 < tiles; k0 += kTileScanThreads) {
+        const int k = k0 + tid;
+        const uint32_t v = k < tiles ? tile_total[k] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        uint32_t before = s_carry, all = 0;
+#pragma unroll
+        for (int w = 0; w < kTileScanThreads / 32; ++w) {
+            const uint32_t t = s_warp[w];
+            before += w < warp ? t : 0u;
+            all += t;
+        }
+        if (k < tiles) tile_total[k] = before + x - v;
+        __syncthreads();
+        if (tid == 0) s_carry += all;
+        __syncthreads();
+    }
+}
+
 // Scan: block b scans tile b (16 consecutive cells per thread) from the sum
-// of the totals of tiles 0..b-1.  With info, the start of the last cell (the
+// of the totals of tiles 0..b-1, or from tile_total[b] when the totals were
+// scanned already (prescanned).  With info, the start of the last cell (the
 // out-of-grid key) goes to info[kOutStart].
 __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict__ count,
                                                             uint32_t* __restrict__ cell_start,
                                                             uint32_t* __restrict__ cell_end,
                                                             const uint32_t* __restrict__ tile_total,
-                                                            int* __restrict__ info, uint32_t cells) {
+                                                            int* __restrict__ info, uint32_t cells, int prescanned) {
     __shared__ uint32_t s_warp[kScanThreads / 32];
     __shared__ uint32_t s_base[kScanThreads / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tile = blockIdx.x;
     uint32_t before = 0;
-    for (int t = tid; t < tile; t += kScanThreads) before += __ldg(tile_total + t);
+    if (prescanned)
+        before = tid == 0 ? __ldg(tile_total + tile) : 0u;
+    else
+        for (int t = tid; t < tile; t += kScanThreads) before += __ldg(tile_total + t);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
     if (lane == 0) s_base[warp] = before;
@@ -289,10 +329,12 @@ void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, 
     k_cell_totals<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, tile_total, info, cells);
 }
 
-void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, const uint32_t* tile_total,
-                      int* info, uint32_t cells, cudaStream_t st) {
-    k_cell_scan<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, cell_start, cell_end, tile_total, info,
-                                                                       cells);
+void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
+                      uint32_t cells, cudaStream_t st) {
+    const int tiles = cell_scan_tiles((int)cells);
+    const int prescanned = tiles > kDirectTiles;
+    if (prescanned) k_cell_tile_scan<<<1, kTileScanThreads, 0, st>>>(tile_total, tiles);
+    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
 }
 
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,

@@ -152,10 +152,13 @@ int radix_tiles(int n);
 int cell_scan_tiles(int cells);
 void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of, uint32_t* count, const int* info,
                        const StepParams& p, int grid_items, cudaStream_t st);
-// totals and scan over cells [0, cells); info null for a batch
+// totals and scan over cells [0, cells); info null for a batch.  Above
+// kDirectTiles tiles of 4096 cells the scan first scans the tile totals in
+// one block (one more launch) instead of summing them in every block.
+constexpr int kDirectTiles = 2048;
 void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, uint32_t cells, cudaStream_t st);
-void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, const uint32_t* tile_total,
-                      int* info, uint32_t cells, cudaStream_t st);
+void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
+                      uint32_t cells, cudaStream_t st);
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
                        const int* info, int grid_items, cudaStream_t st);
 void launch_cell_permute(const uint2* entries, const uint32_t* cell_start, const uint32_t* cell_end, uint32_t* keys,

@@ -149,3 +149,30 @@ def test_fused_step_crowded_and_outside_equals_oracle():
     for f in ("pos_u", "vel_u", "veleval_u"):
         np.testing.assert_array_equal(s.get(f), sim.get(f), err_msg=f)
     s.close()
+
+
+def test_large_grid_scans_tile_totals_first():
+    """A grid of more than 2048 tiles of 4096 cells, where the scan first
+    scans the tile totals in one block: two exact fused steps equal the
+    oracle, and the cell ranges equal the stable order's."""
+    n = 20000
+    spacing = 1.0 / 450  # about 12 M cells: more than 2048 tiles, below the 2^24 - 2 cell limit
+    sp, g, gs = abi.dambreak_params(n, 0.01, spacing=spacing)
+    assert (g.nb_cells + 1 + 4095) // 4096 > 2048 and g.nb_cells <= (1 << 24) - 2
+    pos = scenes.dambreak_positions(n, spacing=spacing)
+    vel = np.zeros_like(pos)
+    s = SPH(sp, g, n, gs, exact=True)
+    s.upload(pos, vel)
+    s.step(DT, 2)
+    sim = ob.OracleSim(sp, g, gs, n)
+    sim.upload(pos, vel)
+    sim.step(DT, 2)
+    for f in ("pos_u", "vel_u", "veleval_u"):
+        np.testing.assert_array_equal(s.get(f), sim.get(f), err_msg=f)
+    # the last sort: keys of the positions the second step started from
+    start_pos = s.get("pos_s", n)
+    keys, _, start, end, occ = canonical(start_pos, g)
+    np.testing.assert_array_equal(s.get("sort_hashes", n), keys)
+    np.testing.assert_array_equal(s.get("cell_start"), start)
+    np.testing.assert_array_equal(s.get("cell_end")[occ], end[occ])
+    s.close()
