@@ -145,3 +145,31 @@ def test_argument_errors_are_reported():
     big.nb_cells = 1 << 25
     with pytest.raises(abi.SPHError):
         SPH(sp, big, n, gs)
+
+
+def test_step_profile_is_the_same_step():
+    """sph_step_profile (the fused step launched kernel by kernel, with events
+    between the launches) computes the graph step bit for bit, and names its
+    eight launches."""
+    import ctypes as C
+    n = 16384
+    sp, g, gs = abi.dambreak_params(n)
+    pos, vel = scenes.dambreak(n, velocity_sigma=0.05)
+    a = SPH(sp, g, n, gs, exact=True)
+    a.upload(pos, vel)
+    a.step(DT, 3)
+    b = SPH(sp, g, n, gs, exact=True)
+    b.upload(pos, vel)
+    ms = (C.c_float * 32)()
+    nk = C.c_int()
+    b._ck(b.lib.sph_step_profile(b.ctx, DT, 3, ms, 32, C.byref(nk)))
+    assert nk.value == 8
+    names = [b.lib.sph_profile_kernel_name(b.ctx, k).decode() for k in range(nk.value)]
+    assert names == ["k_cell_count", "k_cell_totals", "k_cell_scan", "k_cell_place", "k_cell_permute", "k_density",
+                     "k_step_velocities", "k_force(fused collision+leapfrog)"]
+    assert all(ms[k] > 0.0 for k in range(nk.value))
+    sa, sb = state(a), state(b)
+    for f in sa:
+        np.testing.assert_array_equal(sb[f], sa[f], err_msg=f)
+    a.close()
+    b.close()
