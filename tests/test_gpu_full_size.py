@@ -47,3 +47,24 @@ def test_full_size_default_steps_within_tolerance(scene):
     err = np.abs(s.get("pos_u") - sim.get("pos_u")).max()
     assert err <= 1e-4 * sp.smoothing_distance, err / sp.smoothing_distance
     s.close()
+
+
+def test_full_size_mesh_step_equals_oracle(scene):
+    """The same scene with the 524-triangle ramp-and-box mesh of the mesh
+    benchmark: one exact graph step (the triangle kernel after the fused
+    passes) bit for bit against the oracle."""
+    from enjaparticles_gb300.scenes import ramp_and_box_mesh
+    sp, g, gs, pos, vel = scene
+    tris = ramp_and_box_mesh()
+    s = SPH(sp, g, N, gs, exact=True)
+    s.loadTriangles(tris)
+    s.upload(pos, vel)
+    s.step(DT, 1)
+    sim = ob.OracleSim(sp, g, gs, N)
+    sim.set_triangles(tris)
+    sim.upload(pos, vel)
+    sim.step(DT, 1)
+    assert s.getNum() == sim.num
+    for f in ("pos_u", "vel_u", "veleval_u"):
+        np.testing.assert_array_equal(s.get(f), sim.get(f), err_msg=f)
+    s.close()
