@@ -31,3 +31,26 @@ def test_batch_scenes_equal_their_own_contexts(exact):
             np.testing.assert_array_equal(b.get(k, f), s.get(f), err_msg="scene %d %s" % (k, f))
         s.close()
     b.close()
+
+
+def test_full_batched_configuration_equals_lone_contexts():
+    """The batched benchmark's 256 scenes (4.47 M particles, the default
+    arithmetic the benchmark times): after three steps every scene equals the
+    same scene stepped in its own context, bit for bit."""
+    from enjaparticles_gb300.batch import dambreak_batch_scenes
+    ns, mus = dambreak_batch_scenes(256)
+    params = [abi.dambreak_params(n, mu) for n, mu in zip(ns, mus)]
+    data = [scenes.dambreak(n, scene=k) for k, n in enumerate(ns)]
+    b = Batch(params, ns)
+    for k, (pos, vel) in enumerate(data):
+        b.upload(k, pos, vel)
+    b.step(DT, 3)
+    b.sync()
+    for k, ((sp, g, gs), (pos, vel)) in enumerate(zip(params, data)):
+        s = SPH(sp, g, ns[k], gs)
+        s.upload(pos, vel)
+        s.step(DT, 3)
+        for f in ("pos_u", "vel_u", "veleval_u"):
+            np.testing.assert_array_equal(b.get(k, f), s.get(f), err_msg="scene %d %s" % (k, f))
+        s.close()
+    b.close()
