@@ -82,6 +82,9 @@ def parse():
     ap.add_argument("--no-triangles", action="store_true")
     ap.add_argument("--no-surface", action="store_true")
     ap.add_argument("--tri-steps", type=int, default=0, help="0: same as --steps")
+    ap.add_argument("--steady-at", type=int, default=1000,
+                    help="also time --steady-steps steps from this step of the rollout (0: skip)")
+    ap.add_argument("--steady-steps", type=int, default=100)
     return ap.parse_args()
 
 
@@ -197,9 +200,10 @@ def run_reference(args):
         return 0
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_bind
-    from enjaparticles_gb300 import abi, scenes
+    from enjaparticles_gb300 import scenes
     n = args.n
-    sp, g, gs = abi.dambreak_params(n)
+    # parameters derived by the oracle: this arm loads no library of the product
+    sp, g, gs = oracle_bind.dambreak_params(n)
     pos, vel = scenes.dambreak(n)
     sim = oracle_bind.OracleSim(sp, g, gs, n)
     sim.upload(pos, vel)
@@ -219,7 +223,7 @@ def run_reference(args):
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * el / max(steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded dam-break lattice, zero initial velocity)",
-        "config": config_block(n, g.nb_cells),
+        "config": config_block(n, g.nb_cells, warm, steps),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "particle-updates/s", "cores": threads, "kind": "port",
                          "sample": "%d full SPH steps of the %d-particle dam break after %d warm-up steps (%.1f s; "
@@ -484,9 +488,9 @@ def bench_surface(args, torch, peak):
     return out
 
 
-def config_block(n, c):
-    return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001, "
-                        "1000-step rollout config" % n,
+def config_block(n, c, warmup, steps):
+    return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001; "
+                        "timed: steps %d..%d of the rollout from the lattice at rest" % (n, warmup, warmup + steps),
             "particles": n, "nb_cells": c, "dt": DT,
             "l2": "no flush: each step streams > 0.3 GB (> 129 MB L2)", "parallelism": "replicas (one scene per GPU)"}
 
@@ -543,6 +547,9 @@ def main():
     ms = (C.c_float * cap)()
     nk = C.c_int()
     phase = max(1, min(100, psteps))
+    kname = [lib.sph_profile_kernel_name(s.ctx, k).decode() for k in range(cap)]
+    i_force = next(k for k, nm in enumerate(kname) if nm.startswith("k_force"))
+    i_density = kname.index("k_density")
     tot = None
     by_phase = []
     done = 0
@@ -552,7 +559,7 @@ def main():
         row = [ms[q] for q in range(nk.value)]
         tot = row if tot is None else [a + b for a, b in zip(tot, row)]
         by_phase.append({"steps": [args.warmup + done, args.warmup + done + k], "ms_per_step": sum(row) / k,
-                         "force_ms": row[-1] / k, "density_ms": row[-2] / k})
+                         "force_ms": row[i_force] / k, "density_ms": row[i_density] / k})
         done += k
     names = [lib.sph_profile_kernel_name(s.ctx, k).decode() for k in range(nk.value)]
     kern_ms = {names[k]: tot[k] / psteps for k in range(nk.value)}
@@ -576,6 +583,26 @@ def main():
         abi.check(lib, s.ctx, lib.sph_sync(s.ctx))
     t_e2e = max_over_ranks(time.perf_counter() - t0)
     barrier()
+    # --- the same step later in the rollout (the fluid has collapsed: more
+    # neighbours per particle than near the lattice at rest) ------------------
+    steady = None
+    if args.steady_at > 0 and args.steady_steps > 0:
+        s.upload(pos0, vel0)
+        s.step(DT, args.steady_at)
+        s.sync()
+        barrier()
+        e0.record(stream)
+        s.step(DT, args.steady_steps)
+        e1.record(stream)
+        e1.synchronize()
+        barrier()
+        t_st = max_over_ranks(e0.elapsed_time(e1))
+        s.sync()
+        n_st = s.getNum()
+        steady = {"steps": [args.steady_at, args.steady_at + args.steady_steps],
+                  "ms_per_step": t_st / args.steady_steps,
+                  "value": n_st * args.steady_steps * world / (t_st / 1e3), "unit": "particle-updates/s",
+                  "particles": n_st}
     clocks = sampler.stop()
 
     steps = args.steps
@@ -591,7 +618,7 @@ def main():
         "metric": "particle-updates/s at 2M SPH", "value": value, "unit": "particle-updates/s", "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break lattice, zero initial velocity)",
-        "config": config_block(n, c),
+        "config": config_block(n, c, args.warmup, steps),
         "e2e": {"value": n * args.e2e_steps * world / t_e2e, "unit": "particle-updates/s",
                 "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n,
                 "note": "state (pos, vel, veleval) uploaded from and downloaded to pinned host memory every step; "
@@ -603,6 +630,7 @@ def main():
                      "algorithmic_bytes": ab[dom], "mean_launch_ms": kern_ms[dom]},
         "step_roofline": {"algorithmic_bytes": b_step, "achieved": b_step / (step_ms / 1e3) / 1e9, "peak": peak,
                           "frac": b_step / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s"},
+        "steady_state": steady,
         "kernels_ms": kern_ms,
         "kernels_by_phase": by_phase,
         "particles_after": num_after,

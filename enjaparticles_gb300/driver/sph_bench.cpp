@@ -17,6 +17,13 @@
 //             the run (every frame with --frames); prints the mesh's triangles.
 //   sph_bench --n N --dump-scene FILE: write the scene's positions (N x 4
 //             float32) to FILE and exit (no GPU needed).
+//   sph_bench --add-rect NUM SPACING SCALE LX LY LZ HX HY HZ FILE: write
+//             rtps::addRect(NUM, lo, hi, SPACING, SCALE) (k x 4 float32) to
+//             FILE and exit (no GPU needed).
+//   sph_bench --n N --add-box NUM SCALE LX LY LZ HX HY HZ FILE: a system with
+//             the dam-break parameters of N particles and simulation_scale
+//             SCALE, filled by SPH::addBox(NUM, lo, hi, false); writes its
+//             positions (getPositions) to FILE and prints getSpacing().
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -101,7 +108,10 @@ std::vector<rtps::Triangle> ramp_and_box_mesh() {
 int main(int argc, char** argv) {
     int n = 262144, steps = 200, warmup = 10, frames = 0, exact = 0, mesh = 0, post_res = 0;
     float dt = 0.001f, mu = 0.01f;
-    std::string dump;
+    std::string dump, box_file;
+    int box_num = -1, rect_only = 0;
+    float box_spacing = 0.f, box_scale = 1.f;
+    rtps::float4 box_lo = rtps::make_float4(0, 0, 0, 0), box_hi = box_lo;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
         auto next = [&]() -> const char* {
@@ -121,6 +131,17 @@ int main(int argc, char** argv) {
         else if (a == "--dump-scene") dump = next();
         else if (a == "--mesh") mesh = 1;
         else if (a == "--post-process") post_res = std::atoi(next());
+        else if (a == "--add-rect" || a == "--add-box") {
+            rect_only = a == "--add-rect";
+            box_num = std::atoi(next());
+            if (rect_only) box_spacing = (float)std::atof(next());
+            box_scale = (float)std::atof(next());
+            float v[6];
+            for (float& x : v) x = (float)std::atof(next());
+            box_lo = rtps::make_float4(v[0], v[1], v[2], 0.f);
+            box_hi = rtps::make_float4(v[3], v[4], v[5], 0.f);
+            box_file = next();
+        }
         else {
             std::fprintf(stderr, "unknown argument %s\n", a.c_str());
             return 2;
@@ -133,11 +154,32 @@ int main(int argc, char** argv) {
         if (!f || std::fwrite(pos.data(), sizeof(rtps::float4), pos.size(), f) != pos.size()) return 1;
         return std::fclose(f) == 0 ? 0 : 1;
     }
+    auto write_f4 = [](const std::string& path, const std::vector<rtps::float4>& v) {
+        FILE* f = std::fopen(path.c_str(), "wb");
+        if (!f) return false;
+        const bool ok = v.empty() || std::fwrite(v.data(), sizeof(rtps::float4), v.size(), f) == v.size();
+        return std::fclose(f) == 0 && ok;
+    };
+    if (rect_only) return write_f4(box_file, rtps::addRect(box_num, box_lo, box_hi, box_spacing, box_scale)) ? 0 : 1;
     SPHParams sp;
     GridParams g, gs;
     if (sph_dambreak_params(n, lattice_spacing(n), mu, &sp, &g, &gs) != SPH_OK) {
         std::fprintf(stderr, "sph_dambreak_params failed\n");
         return 1;
+    }
+    if (!box_file.empty()) {
+        try {
+            sp.simulation_scale = box_scale;
+            rtps::SPH sph(sp, g, n, nullptr, dt);
+            const int added = sph.addBox(box_num, box_lo, box_hi, false);
+            if (!write_f4(box_file, sph.getPositions())) return 1;
+            std::printf("{\"added\": %d, \"num\": %d, \"spacing\": %.9g}\n", added, sph.getNum(),
+                        (double)sph.getSpacing());
+        } catch (const rtps::SPHError& e) {
+            std::fprintf(stderr, "error %d: %s\n", e.code(), e.what());
+            return 1;
+        }
+        return 0;
     }
     try {
         rtps::SPH sph(sp, g, n, &gs, dt);

@@ -125,9 +125,12 @@ public:
     }
     void setNum(int nn) { check(sph_set_num(ctx_, nn)); }
     int getMaxNum() const { return max_num_; }
+    // SPH::getSpacing (SPH.cpp:66): the "spacing" setting, written by
+    // SPH::calculate as rest_distance / simulation_scale (SPHSettings.cpp:
+    // 94-96) and read back through the settings map (6 significant digits).
     float getSpacing() {
         SPHParams p = params();
-        return p.rest_distance / p.simulation_scale;  // SPHSettings.cpp:94
+        return sph_settings_round(p.rest_distance / p.simulation_scale);
     }
     // System::addBox (System.cpp:331-338): addRect at the SPH spacing, zero
     // velocity.  color and mass are accepted for interface parity and unused.

@@ -2,7 +2,9 @@
 // (rtpslib/domain/Domain.cpp:38-81, compiled from the reference tree) driven
 // as System::setupDomain does (rtpslib/system/System.cpp:294-329).
 #include <cstring>
+#include <vector>
 #include "domain/Domain.h"
+#include "domain/IV.h"
 #include "ref_api.h"
 
 extern "C" void ref_setup_domain(const float* bmin, const float* bmax, float cell_size, float sim_scale, void* grid,
@@ -31,4 +33,19 @@ extern "C" void ref_setup_domain(const float* bmin, const float* bmax, float cel
     static_assert(sizeof(rtps::GridParams) == 128, "GridParams layout");
     std::memcpy(grid, &g, 128);
     std::memcpy(grid_scaled, &s, 128);
+}
+
+// The reference's addRect (rtpslib/domain/IV.cpp:165-202, compiled from the
+// reference tree): at most num lattice points, written as float4 rows to out;
+// returns how many were made.
+extern "C" int ref_add_rect(int num, const float* lo, const float* hi, float spacing, float scale, float* out) {
+    std::vector<rtps::float4> v = rtps::addRect(num, rtps::float4(lo[0], lo[1], lo[2], lo[3]),
+                                                rtps::float4(hi[0], hi[1], hi[2], hi[3]), spacing, scale);
+    for (size_t i = 0; i < v.size(); ++i) {
+        out[4 * i] = v[i].x;
+        out[4 * i + 1] = v[i].y;
+        out[4 * i + 2] = v[i].z;
+        out[4 * i + 3] = v[i].w;
+    }
+    return (int)v.size();
 }

@@ -30,6 +30,9 @@ Fixtures
   hose_sprays.npz    the reference's Hose (common/Hose.cpp, addDiscRandom)
                      through the scripts of tests/hose_cases.py, rand()
                      seeded per script: counts, positions, push velocities
+  addrect.npz        the reference's addRect (domain/IV.cpp) for the boxes of
+                     tests/addrect_cases.py at the getSpacing() of each
+                     system (System::addBox): the spacing and the points
 Usage: python tests/golden/make_golden.py [--only NAME ...]
 """
 import ctypes as C
@@ -217,6 +220,18 @@ def hose_fixture():
     return out
 
 
+def addrect_fixture():
+    import addrect_cases
+    import oracle_bind
+    out = {}
+    for name, n, scale, num, lo, hi in addrect_cases.CASES:
+        sp, _ = addrect_cases.scene_params(n, scale)
+        sx = addrect_cases.spacing(sp)
+        out[name + "_spacing"] = np.float32(sx)
+        out[name + "_points"] = oracle_bind.ref_add_rect(num, lo, hi, sx, 1.0)
+    return out
+
+
 FIXTURES = {
     "stages_n4096.npz": lambda: stages_fixture(4096, 0.1),
     "ragged_n1000.npz": lambda: stages_fixture(1000, 0.1, steps_after=(3,)),
@@ -226,6 +241,7 @@ FIXTURES = {
     "triangles_n2048.npz": triangles_fixture,
     "hose_sprays.npz": hose_fixture,
     "surface_n4096.npz": surface_fixture,
+    "addrect.npz": addrect_fixture,
 }
 
 

@@ -70,6 +70,8 @@ def oracle():
             "oracle_rollout64": (_I, [_P, _P, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_rollout64_jvp": (_I, [_P, _P, C.c_double, C.c_double, C.c_double, _I, _I, _P, _P, _P, _P, _P,
                                           _P, _P, _P]),
+            "oracle_dambreak_params": (_I, [_I, _F, _F, _P, _P, _P]),
+            "oracle_settings_round": (_F, [_F]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -77,6 +79,36 @@ def oracle():
             f.argtypes = a
         _oracle = lib
     return _oracle
+
+
+def dambreak_params(n, viscosity=0.01, spacing=None):
+    """(SPHParams, GridParams, GridParams scaled) of the dam-break scenes,
+    derived by the oracle (oracle/sph_params_oracle.cpp) without loading the
+    product library: the structs are the ctypes views of include/rtps_sph.h."""
+    from enjaparticles_gb300 import abi, scenes
+    sp, g, gs = abi.SPHParams(), abi.GridParams(), abi.GridParams()
+    s = scenes.lattice_spacing(n) if spacing is None else spacing
+    rc = oracle().oracle_dambreak_params(int(n), float(s), float(viscosity), C.addressof(sp), C.addressof(g),
+                                         C.addressof(gs))
+    if rc != 0:
+        raise ValueError("oracle_dambreak_params: invalid arguments")
+    return sp, g, gs
+
+
+def settings_round(value):
+    """A float through the reference's settings map (6 significant digits)."""
+    import numpy as np
+    return float(oracle().oracle_settings_round(float(np.float32(value))))
+
+
+def ref_add_rect(num, lo, hi, spacing, scale=1.0):
+    """The reference's addRect (rtpslib/domain/IV.cpp:165-202) from oracle/_ref:
+    (k, 4) float32 lattice points."""
+    lo4 = np.asarray(list(lo) + [0.0] * (4 - len(lo)), np.float32)
+    hi4 = np.asarray(list(hi) + [0.0] * (4 - len(hi)), np.float32)
+    out = np.zeros((num, 4), np.float32)
+    k = ref().ref_add_rect(int(num), ptr(lo4), ptr(hi4), float(spacing), float(scale), ptr(out))
+    return out[:k]
 
 
 def ref_available():
@@ -110,6 +142,7 @@ def ref():
             "ref_colorfield_slices": (_I, [_I]),
             "ref_colorfield": (_I, [_I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
             "ref_marching_cubes": (_I, [_I, _P, _F, _P, _P, _I, _P]),
+            "ref_add_rect": (_I, [_I, _P, _P, _F, _F, _P]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)

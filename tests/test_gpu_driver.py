@@ -1,11 +1,13 @@
 """The headless C++ driver (rtps::SPH class over the C ABI) steps the same
 scene to the same bits as the Python harness, in fused and frame-loop modes."""
 import json
+import os
 import subprocess
 
 import numpy as np
 import pytest
 
+import addrect_cases
 from enjaparticles_gb300 import abi, build_ext
 from enjaparticles_gb300.sph import dambreak_system
 
@@ -55,3 +57,19 @@ def test_driver_mesh_and_post_process_match_python():
     v, _ = s.postProcess(res)
     assert d["mesh"] == 1 and d["checksum"] == want
     assert d["triangles"] == len(v) > 0
+
+
+@pytest.mark.parametrize("case", addrect_cases.CASES, ids=[c[0] for c in addrect_cases.CASES])
+def test_driver_add_box_equals_reference_add_rect(case, tmp_path):
+    """rtps::SPH::addBox through the C++ class: the system's positions are the
+    reference's addRect points (golden, from oracle/_ref) at the reference's
+    getSpacing, bit for bit, and the class's getSpacing is that spacing."""
+    name, n, scale, num, lo, hi = case
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "addrect.npz"))
+    out = tmp_path / "box.bin"
+    d = _run("--n", n, "--add-box", num, scale, *lo[:3], *hi[:3], out)
+    want = gold[name + "_points"]
+    got = np.fromfile(out, np.float32).reshape(-1, 4)
+    assert d["added"] == d["num"] == len(want)
+    assert np.float32(d["spacing"]) == gold[name + "_spacing"]
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
