@@ -10,6 +10,7 @@
 // buffer, counters) in one file-scope __device__ array.  That array is part
 // of the library image: every GPU that loads the library holds it (about
 // 9 MiB) until the process exits.
+#include <atomic>
 #include <cstdio>
 
 #include "sph_device.cuh"
@@ -33,9 +34,15 @@ constexpr size_t kScratchWords = kOffInfo + (size_t)kInfoSlots;
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kScratchWords];
 
 // Device address of g_noalloc_scratch per device, looked up on the first call
-// made with that device current.
+// made with that device current.  Two host threads making their first calls
+// at once may both look it up: the runtime gives both the same address, and
+// the atomic store makes the publication of either one safe to read.  A
+// cudaDeviceReset unloads the library's module and with it this address (the
+// header tells callers not to use the function after one); a call whose
+// launches fail forgets the cached address, so that the next call looks it
+// up again.
 constexpr int kMaxDevices = 64;
-uint32_t* g_scratch_ptr[kMaxDevices] = {nullptr};
+std::atomic<uint32_t*> g_scratch_ptr[kMaxDevices];
 
 __global__ void k_noalloc_reset(uint32_t* __restrict__ hist_status, size_t words, int* __restrict__ info, int n) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -43,9 +50,11 @@ __global__ void k_noalloc_reset(uint32_t* __restrict__ hist_status, size_t words
     if (blockIdx.x == 0 && threadIdx.x < kInfoSlots) info[threadIdx.x] = threadIdx.x == kNum ? n : 0;
 }
 
-// Digit histograms of every pass, aggregated per warp with match_any.
+// Digit histograms of every pass, aggregated per warp with match_any.  Pass
+// ps counts the digit (key >> 8 ps) masked to the pass's width, the digit the
+// radix pass ranks by: the low key_bits bits of a key are its sort key.
 __global__ void __launch_bounds__(256) k_noalloc_hist(const uint32_t* __restrict__ keys, int n, int passes,
-                                                      uint32_t* __restrict__ hist) {
+                                                      int key_bits, uint32_t* __restrict__ hist) {
     __shared__ uint32_t s_hist[kNoAllocPasses][256];
     const int tid = threadIdx.x;
     for (int k = tid; k < kNoAllocPasses * 256; k += blockDim.x) (&s_hist[0][0])[k] = 0;
@@ -57,7 +66,8 @@ __global__ void __launch_bounds__(256) k_noalloc_hist(const uint32_t* __restrict
         const bool valid = i < (size_t)n;
         const uint32_t key = valid ? __ldg(keys + i) : 0u;
         for (int ps = 0; ps < passes; ++ps) {
-            const uint32_t d = valid ? ((key >> (8 * ps)) & 255u) : 0x100u;
+            const int bits = key_bits - 8 * ps < 8 ? key_bits - 8 * ps : 8;
+            const uint32_t d = valid ? ((key >> (8 * ps)) & ((1u << bits) - 1u)) : 0x100u;
             const unsigned peers = __match_any_sync(0xffffffffu, d);
             if (valid && (int)lane == 31 - __clz(peers)) atomicAdd(&s_hist[ps][d], (uint32_t)__popc(peers));
         }
@@ -69,9 +79,10 @@ __global__ void __launch_bounds__(256) k_noalloc_hist(const uint32_t* __restrict
     }
 }
 
-int set_error(char* msg, int len, const char* text) {
-    if (msg && len > 0) std::snprintf(msg, (size_t)len, "%s", text);
-    return SPH_EINVAL;
+// [a, a+n) and [b, b+n) share an element.
+bool overlaps(const uint32_t* a, const uint32_t* b, int n) {
+    const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b, len = (uintptr_t)n * sizeof(uint32_t);
+    return x < y + len && y < x + len;
 }
 
 }  // namespace
@@ -84,21 +95,24 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
     if (n < 0 || n > kNoAllocMaxKeys) return SPH_EINVAL;  // more than 1,048,576 pairs
     if (key_bits < 1 || key_bits > 32) return SPH_EINVAL;
     if (n > 0 && (!keys_in || !vals_in || !keys_out || !vals_out)) return SPH_EINVAL;
-    if (keys_out == keys_in || vals_out == vals_in) return SPH_EINVAL;  // not in place
     if (n == 0) return SPH_OK;
+    // not in place: no output may share an element with an input or with the
+    // other output (the inputs are only read and may overlap each other)
+    if (overlaps(keys_out, keys_in, n) || overlaps(keys_out, vals_in, n) || overlaps(keys_out, vals_out, n) ||
+        overlaps(vals_out, keys_in, n) || overlaps(vals_out, vals_in, n))
+        return SPH_EINVAL;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SPH_ECUDA;
-    if (!g_scratch_ptr[dev]) {
+    uint32_t* s = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (!s) {
         // First call on this device: the host-side name of the array is not a
         // device address, so ask the runtime for the address on this device.
-        uint32_t* p = nullptr;
-        if (cudaGetSymbolAddress((void**)&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        if (cudaGetSymbolAddress((void**)&s, g_noalloc_scratch) != cudaSuccess || !s) {
             cudaGetLastError();
             return SPH_ECUDA;
         }
-        g_scratch_ptr[dev] = p;
+        g_scratch_ptr[dev].store(s, std::memory_order_release);
     }
-    uint32_t* s = g_scratch_ptr[dev];
     cudaStream_t st = (cudaStream_t)stream;
     const int passes = (key_bits + 7) / 8;
     int* info = reinterpret_cast<int*>(s + kOffInfo);
@@ -106,7 +120,7 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
     k_noalloc_reset<<<256, 256, 0, st>>>(s + kOffHist, zero_words, info, n);
     int hblocks = (n + 255) / 256;
     hblocks = hblocks > 152 * 8 ? 152 * 8 : hblocks;
-    k_noalloc_hist<<<hblocks, 256, 0, st>>>(keys_in, n, passes, s + kOffHist);
+    k_noalloc_hist<<<hblocks, 256, 0, st>>>(keys_in, n, passes, key_bits, s + kOffHist);
     // Passes alternate between the caller's output and the scratch buffer so
     // that the last one lands in the output and the input is never written.
     const uint32_t *kin = keys_in, *vin = vals_in;
@@ -122,9 +136,14 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
         kin = kout;
         vin = vout;
     }
-    if (cudaGetLastError() != cudaSuccess) return SPH_ECUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return SPH_ECUDA;
+    // The error word is read on the caller's stream, so only that stream is
+    // waited for (no device-wide synchronisation).
     int err = 0;
-    if (cudaMemcpy(&err, info + kError, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return SPH_ECUDA;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(&err, info + kError, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        g_scratch_ptr[dev].store(nullptr, std::memory_order_release);
+        return SPH_ECUDA;
+    }
     return err ? SPH_ETIMEOUT : SPH_OK;
 }

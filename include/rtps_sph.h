@@ -554,16 +554,21 @@ int sph_batch_adjoint_backward_traj(sph_batch* batch, const sph_float4* dL_dpos_
  * the allocator.  Same stable LSD radix sort as sph_stage_sort: ascending keys
  * (the low key_bits bits of each key are the sort key; keys must fit in them),
  * equal keys keep their input order.  keys_in/vals_in are read only;
- * keys_out/vals_out must be distinct from them.  stream is a cudaStream_t
- * (NULL: the legacy default stream).
+ * keys_out/vals_out must not overlap them or each other (SPH_EINVAL).
+ * Bits of a key above key_bits are ignored by the ordering and kept in the
+ * output.  stream is a cudaStream_t (NULL: the legacy default stream).
  *
  * Limit: n <= 1,048,576 (SPH_EINVAL above).  All scratch memory lives in one
  * statically sized device array of the library (about 9 MiB, held by every
  * GPU that loads the library until the process exits).  The first call on a
  * device looks up that array's device address; make it before any stream
  * capture.  Calls share the array: calls that overlap on the GPU (other
- * streams, other threads) race and corrupt each other.  Blocking: returns
- * when the sort has finished. */
+ * streams, other threads) race and corrupt each other; each call clears the
+ * parts of it that must start at zero.  Blocking: every call copies its status
+ * word back on the given stream and waits for that stream (and no other)
+ * before it returns.  The address is cached per device for the life of the
+ * process: a cudaDeviceReset invalidates it, so do not call this function
+ * after resetting a device it was used on. */
 int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                            uint32_t* vals_out, int n, int key_bits, void* stream);
 
