@@ -36,10 +36,10 @@
 //     the lattice replaced by the point itself (map3Dto2DClamp), mixed along
 //     the edge and normalised as v * (1 / sqrt(v.v));
 //   - positions scaled to the reference's render box: p / (res - 1) * 10.
-// The triangulation of each case comes from sph_mc_case_table below, built
-// here from the cube's topology; the reference uses a published case table.
-// The vertex set of every cube is the same either way (every crossed edge);
-// the triangles that join them can differ.
+//   - the triangles of each case, in order: the reference's case table
+//     (traversehp.cl:74), carried in sph_mc_table.inc; it decides which
+//     diagonal splits a quad or pentagon, so the triangle list equals the
+//     reference's triangle for triangle.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -59,8 +59,6 @@ constexpr int kMcCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1}, {0,
 // and interpolation direction (traversehp.cl:35-72).
 constexpr int kMcEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
                                 {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-// Faces as corner cycles.
-constexpr int kMcFace[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}, {0, 1, 5, 4}, {3, 2, 6, 7}};
 
 struct McTable {
     signed char tri[256][kMcMaxTriEdges];
@@ -68,108 +66,23 @@ struct McTable {
     int max_count;
 };
 
-int mc_edge_of(int a, int b) {
-    for (int e = 0; e < 12; ++e)
-        if ((kMcEdge[e][0] == a && kMcEdge[e][1] == b) || (kMcEdge[e][0] == b && kMcEdge[e][1] == a)) return e;
-    return -1;
-}
+#include "sph_mc_table.inc"
 
-// The surface polygons of one case: on each face, the crossed edges are
-// joined by segments (a face with four crossings separates its two inside
-// corners); the segments chain into closed loops around the cube; each loop
-// is oriented so that its normal points from the inside corners (above the
-// isolevel) to the outside ones, then fanned into triangles from its first
-// vertex.
-void mc_build_case(int cs, McTable& T) {
-    bool in[8];
-    for (int k = 0; k < 8; ++k) in[k] = (cs >> k) & 1;
-    std::vector<int> nbr[12];
-    for (const auto& f : kMcFace) {
-        int e[4];
-        bool cross[4];
-        int n = 0;
-        for (int i = 0; i < 4; ++i) {
-            e[i] = mc_edge_of(f[i], f[(i + 1) % 4]);
-            cross[i] = in[f[i]] != in[f[(i + 1) % 4]];
-            n += cross[i];
-        }
-        auto join = [&](int a, int b) {
-            nbr[a].push_back(b);
-            nbr[b].push_back(a);
-        };
-        if (n == 2) {
-            int a = -1, b = -1;
-            for (int i = 0; i < 4; ++i)
-                if (cross[i]) (a < 0 ? a : b) = e[i];
-            join(a, b);
-        } else if (n == 4) {
-            for (int i = 0; i < 4; ++i)
-                if (in[f[i]]) join(e[(i + 3) % 4], e[i]);
-        }
-    }
-    auto mid = [](int e, double* p) {
-        for (int a = 0; a < 3; ++a) p[a] = 0.5 * (kMcCorner[kMcEdge[e][0]][a] + kMcCorner[kMcEdge[e][1]][a]);
-    };
-    bool seen[12] = {false};
-    int nt = 0;
-    for (int e0 = 0; e0 < 12; ++e0) {
-        if (seen[e0] || nbr[e0].empty()) continue;
-        std::vector<int> loop;
-        int prev = -1, cur = e0;
-        do {
-            loop.push_back(cur);
-            seen[cur] = true;
-            const int next = (nbr[cur][0] == prev) ? nbr[cur][1] : nbr[cur][0];
-            prev = cur;
-            cur = next;
-        } while (cur != e0);
-        // Newell normal and centroid of the loop
-        double N[3] = {0, 0, 0}, Cc[3] = {0, 0, 0};
-        for (size_t i = 0; i < loop.size(); ++i) {
-            double p[3], q[3];
-            mid(loop[i], p);
-            mid(loop[(i + 1) % loop.size()], q);
-            N[0] += (p[1] - q[1]) * (p[2] + q[2]);
-            N[1] += (p[2] - q[2]) * (p[0] + q[0]);
-            N[2] += (p[0] - q[0]) * (p[1] + q[1]);
-            for (int a = 0; a < 3; ++a) Cc[a] += p[a] / loop.size();
-        }
-        // gradient at the centroid of the trilinear blend of the corner states
-        double G[3] = {0, 0, 0};
-        for (int k = 0; k < 8; ++k) {
-            if (!in[k]) continue;
-            double w[3], d[3];
-            for (int a = 0; a < 3; ++a) {
-                w[a] = kMcCorner[k][a] ? Cc[a] : 1.0 - Cc[a];
-                d[a] = kMcCorner[k][a] ? 1.0 : -1.0;
-            }
-            G[0] += d[0] * w[1] * w[2];
-            G[1] += w[0] * d[1] * w[2];
-            G[2] += w[0] * w[1] * d[2];
-        }
-        if (N[0] * G[0] + N[1] * G[1] + N[2] * G[2] > 0) std::reverse(loop.begin() + 1, loop.end());
-        for (size_t i = 1; i + 1 < loop.size(); ++i) {
-            if (3 * (nt + 1) > kMcMaxTriEdges) {  // cannot happen for a cube; kept as a hard stop
-                T.max_count = kMcMaxTriEdges;
-                break;
-            }
-            T.tri[cs][3 * nt] = (signed char)loop[0];
-            T.tri[cs][3 * nt + 1] = (signed char)loop[i];
-            T.tri[cs][3 * nt + 2] = (signed char)loop[i + 1];
-            ++nt;
-        }
-    }
-    T.count[cs] = (unsigned char)nt;
-    T.max_count = std::max(T.max_count, nt);
-}
-
+// The case table unpacked: the triangles of case cs as edge numbers, the
+// triangle count, the largest count.
 const McTable& mc_table() {
     static McTable T = [] {
         McTable t;
         std::memset(t.tri, -1, sizeof(t.tri));
         std::memset(t.count, 0, sizeof(t.count));
         t.max_count = 0;
-        for (int cs = 0; cs < 256; ++cs) mc_build_case(cs, t);
+        for (int cs = 0; cs < 256; ++cs) {
+            const unsigned long long w = kMcCasePacked[cs];
+            const int nt = (int)((w >> 60) & 7u);
+            for (int e = 0; e < 3 * nt; ++e) t.tri[cs][e] = (signed char)((w >> (4 * e)) & 15u);
+            t.count[cs] = (unsigned char)nt;
+            t.max_count = std::max(t.max_count, nt);
+        }
         return t;
     }();
     return T;

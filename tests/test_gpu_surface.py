@@ -1,8 +1,7 @@
 """Colour field and marching cubes on the GPU (SPH::postProcess) against the
 reference's own kernels (tests/golden/surface_n4096.npz: colorfield.cl and
 the histopyramid marching cubes after 20 steps of the reference): the field
-bit for bit; the mesh cube by cube (same cubes in the same order, same
-vertices and normals; the split of a quad may differ)."""
+and the mesh (triangles, vertices, normals, in order) bit for bit."""
 import ctypes as C
 
 import numpy as np
@@ -40,25 +39,16 @@ def test_colorfield_default_arithmetic_close_to_reference_golden():
 
 
 @pytest.mark.parametrize("res", [16, 32])
-def test_surface_matches_reference_golden_cube_by_cube(res):
+def test_surface_matches_reference_golden(res):
+    """The mesh of SPH::postProcess equals the reference's triangle list bit
+    for bit: the same triangles in the same order, each with its vertices and
+    normals in the same order."""
     s, d = _system()
     v, nr = s.postProcess(res)
     rv, rn = d["mesh%d_vertices" % res], d["mesh%d_normals" % res]
     assert v.shape == rv.shape and len(v) > 100
-    cubes, rcubes = sc.triangle_cubes(v, res), sc.triangle_cubes(rv, res)
-    np.testing.assert_array_equal(cubes, rcubes)  # the same cube for every triangle
-    np.testing.assert_array_equal(sc.vertex_rows(v, nr), sc.vertex_rows(rv, rn))
-    # cube by cube: the same vertices (with normals)
-    starts = np.flatnonzero(np.r_[True, (cubes[1:] != cubes[:-1]).any(1)])
-    ends = np.r_[starts[1:], len(v)]
-    same_tris = 0
-    for a, b in zip(starts, ends):
-        mine, ref = sc.vertex_rows(v[a:b], nr[a:b]), sc.vertex_rows(rv[a:b], rn[a:b])
-        np.testing.assert_array_equal(mine, ref)
-        t1 = sorted(tuple(sorted(map(tuple, t))) for t in v[a:b].view(np.uint32))
-        t2 = sorted(tuple(sorted(map(tuple, t))) for t in rv[a:b].view(np.uint32))
-        same_tris += t1 == t2
-    assert same_tris >= len(starts) // 4
+    np.testing.assert_array_equal(v.view(np.uint32), rv.view(np.uint32))
+    np.testing.assert_array_equal(nr.view(np.uint32), rn.view(np.uint32))
 
 
 def _blob_field(res, seed=3):
