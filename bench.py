@@ -265,7 +265,7 @@ def bench_batched(args, torch):
     e1.synchronize()
     t_batch = e0.elapsed_time(e1) / 1e3
     b.sync()
-    frozen = b.out_of_grid()
+    deleted_last = b.out_of_grid()
     b.close()
     ctxs = []
     for (sp, g, gs), (pos, vel), n in zip(params, data, ns):
@@ -291,7 +291,7 @@ def bench_batched(args, torch):
     return {"metric": "scenes/s", "scenes": S, "particles": int(sum(ns)), "value": batched,
             "serial_value": serial, "speedup_vs_serial": batched / serial, "batch_steps": args.batch_steps,
             "serial_steps": args.serial_steps, "ms_per_batch_step": 1e3 * t_batch / args.batch_steps,
-            "frozen_out_of_grid": frozen,
+            "deleted_in_last_step": deleted_last,
             "note": "each scene of a batch steps bit-identically to the same scene in its own context"}
 
 

@@ -130,6 +130,8 @@ SIGNATURES = {
     "sph_batch_step": (_I, [_P, _F, _I]),
     "sph_batch_download": (_I, [_P, _I, _I, _P, _I]),
     "sph_batch_out_of_grid": (_I, [_P, C.POINTER(_I)]),
+    "sph_batch_get_num": (_I, [_P, _I, C.POINTER(_I)]),
+    "sph_batch_get_deleted": (_I, [_P, _I, _P, _P, _I, C.POINTER(_I)]),
     "sph_batch_sync": (_I, [_P]),
     "sph_batch_last_error": (_I, [_P, C.c_char_p, _I]),
     "sph_batch_set_params": (_I, [_P, _I, _P]),

@@ -64,12 +64,32 @@ class Batch:
     def sync(self):
         self._ck(self.lib.sph_batch_sync(self.h))
 
+    def getNum(self, scene):
+        """The scene's current particle count (it drops after a deletion)."""
+        c = C.c_int()
+        self._ck(self.lib.sph_batch_get_num(self.h, int(scene), C.byref(c)))
+        self.num[scene] = c.value
+        return c.value
+
     def get(self, scene, field):
-        out = np.empty((self.num[scene], 4), np.float32)
-        self._ck(self.lib.sph_batch_download(self.h, scene, abi.FIELDS[field], out.ctypes.data, self.num[scene]))
+        n = self.getNum(scene)
+        out = np.empty((n, 4), np.float32)
+        self._ck(self.lib.sph_batch_download(self.h, scene, abi.FIELDS[field], out.ctypes.data, n))
         return out
 
+    def getDeleted(self, scene):
+        """(pos, vel) of the particles the scene's last deletion removed, sorted order."""
+        cnt = C.c_int()
+        self._ck(self.lib.sph_batch_get_deleted(self.h, int(scene), None, None, 0, C.byref(cnt)))
+        pos = np.empty((cnt.value, 4), np.float32)
+        vel = np.empty((cnt.value, 4), np.float32)
+        if cnt.value:
+            self._ck(self.lib.sph_batch_get_deleted(self.h, int(scene), pos.ctypes.data, vel.ctypes.data, cnt.value,
+                                                    C.byref(cnt)))
+        return pos, vel
+
     def out_of_grid(self):
+        """Particles removed by the last step (all scenes)."""
         c = C.c_int()
         self._ck(self.lib.sph_batch_out_of_grid(self.h, C.byref(c)))
         return c.value

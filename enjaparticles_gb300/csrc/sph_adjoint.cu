@@ -932,6 +932,10 @@ int sph_batch_adjoint_record(sph_batch* b, float dt, int nsteps, int K) {
     if (!b || nsteps <= 0 || K <= 0 || !std::isfinite(dt))
         return berr(b, SPH_EINVAL, "sph_batch_adjoint_record: bad arguments (nsteps=%d, K=%d)", nsteps, K);
     cudaSetDevice(b->device);
+    {
+        const int rc = batch_refresh_num(b);  // counts after earlier deletions
+        if (rc) return rc;
+    }
     if (!b->adj) {
         b->adj = new sph_batch_adjoint();
         b->adj->N = (size_t)b->nslots;

@@ -237,7 +237,8 @@ void free_all(sph_ctx* c) {
     void* ptrs[] = {c->pos_u, c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->force_s, c->xsph_s,
                     c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
                     c->cell_start, c->cell_end, c->info, c->scratch, c->grav, c->tri, c->cf, c->cf_inv,
-                    c->mc_scan, c->mc_table, c->mesh, c->cell_count, c->cell_tile_total, c->cell_entries};
+                    c->mc_scan, c->mc_table, c->mesh, c->cell_count, c->cell_tile_total, c->cell_entries,
+                    c->pos_xy, c->pos_z};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
@@ -303,7 +304,8 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
         if (rc) return rc;
     }
     sphk::launch_cell_permute(c->cell_entries, c->cell_start, c->cell_end, c->keys_a, c->idx_a, c->pos_u, c->vel_u,
-                              c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, gather, st);
+                              c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, gather, c->pos_xy,
+                              c->pos_z, st);
     c->keys_cur = c->keys_a;
     c->idx_cur = c->idx_a;
     CK_LAUNCH(c);
@@ -311,11 +313,14 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
 }
 
 // Density over the sorted arrays; the fused step skips the neighbour counts
-// and leaves the veleval lanes of rec_vi to its velocity pass.
-void density_launch(sph_ctx* c, bool fused, cudaStream_t st) {
+// and leaves the veleval lanes of rec_vi to its velocity pass.  pack: the
+// position pairs of the default arithmetic are written from pos_s first
+// (the stage API's permutes do not write them; the counting sort's does).
+void density_launch(sph_ctx* c, bool fused, cudaStream_t st, bool pack = false) {
     sphk::launch_density(c->pos_s, fused ? nullptr : c->veleval_s, c->density, c->rec_pd, c->rec_vi,
                          fused ? nullptr : c->nbr, c->mask,
-                         (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, st);
+                         (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, c->pos_xy,
+                         c->pos_z, pack, st);
 }
 
 void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {
@@ -486,6 +491,8 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->nbr, N * 4);
     ALLOC(c->rec_pd, N * 16);
     ALLOC(c->rec_vi, N * 16);
+    ALLOC(c->pos_xy, (N / 2 + 1) * 16);
+    ALLOC(c->pos_z, (N / 2 + 1) * 8);
     ALLOC(c->mask, N * 4 * sphk::kMaskWords);
     ALLOC(c->keys_a, N * 4);
     ALLOC(c->idx_a, N * 4);
@@ -533,6 +540,8 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     cudaMemsetAsync(c->nbr, 0, N * 4, st);
     cudaMemsetAsync(c->rec_pd, 0, N * 16, st);
     cudaMemsetAsync(c->rec_vi, 0, N * 16, st);
+    cudaMemsetAsync(c->pos_xy, 0, (N / 2 + 1) * 16, st);
+    cudaMemsetAsync(c->pos_z, 0, (N / 2 + 1) * 8, st);
     cudaMemsetAsync(c->mask, 0, N * 4 * sphk::kMaskWords, st);
     fill_u32(c->keys_a, N, 0x7fffffffu, st);
     fill_u32(c->idx_a, N, 0x7fffffffu, st);
@@ -815,7 +824,7 @@ int sph_stage_permute(sph_ctx* c) {
 int sph_stage_density(sph_ctx* c) {
     int rc = check_ctx(c);
     if (rc) return rc;
-    density_launch(c, false, c->stream);
+    density_launch(c, false, c->stream, true);
     CK_LAUNCH(c);
     return SPH_OK;
 }
@@ -1059,7 +1068,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_permute(c->cell_entries, c->cell_start, c->cell_end, c->keys_a, c->idx_a, c->pos_u,
                                   c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, 0,
-                                  st);
+                                  c->pos_xy, c->pos_z, st);
         CK(c, cudaEventRecord(ev[e++], st));
         density_launch(c, true, st);
         CK(c, cudaEventRecord(ev[e++], st));

@@ -21,8 +21,10 @@
 //
 // Per particle the arithmetic is the single-system one, so every scene of a
 // batch steps exactly as it would alone.  Particles that leave their scene's
-// grid are frozen (counted by sph_batch_out_of_grid); a lone system would
-// delete them.
+// grid are deleted as a lone system deletes them (SPH.cpp:220-250): the
+// scene keeps its first sorted particles, re-indexed in sorted order, its
+// count drops, and the removed particles are kept after them in the scene's
+// slots (sph_batch_get_deleted).
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -76,8 +78,47 @@ __global__ void __launch_bounds__(256) k_bplace(const uint32_t* __restrict__ key
     entries[__ldg(cell_start + g) + __ldg(slot_of + t)] = make_uint2((uint32_t)t, key);
 }
 
+// Scenes' first sorted indices: the exclusive scan of the particle counts
+// (scene after scene in sorted order), and the batch's particle total.
+__global__ void __launch_bounds__(1024) k_bscene_scan(const int* __restrict__ num, uint32_t* __restrict__ seg,
+                                                      int* __restrict__ info, int nscenes) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    if (t == 0) s_carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nscenes; base += 1024) {
+        const int k = base + t;
+        const uint32_t v = k < nscenes ? (uint32_t)num[k] : 0u;
+        uint32_t x = v;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (lane == 31) s_warp[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t w = s_warp[lane];
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, d);
+                if (lane >= d) w += y;
+            }
+            s_warp[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t before = s_carry + (wid > 0 ? s_warp[wid - 1] : 0u) + x - v;
+        if (k < nscenes) seg[k] = before;
+        __syncthreads();
+        if (t == 1023) s_carry = before + v;
+        __syncthreads();
+    }
+    if (t == 0) info[sphk::kNum] = (int)s_carry;
+}
+
 // Permute: rank within the cell, sorted keys (the scene resolver reads them),
-// indices, the gather of pos / veleval; particles in their scene's
+// indices, the gather of pos / veleval (and vel, for a scene that deletes
+// particles this step: its kept particles are re-indexed by the force pass,
+// which then reads no velocity by slot); particles in their scene's
 // out-of-grid cell are counted as frozen.
 __global__ void __launch_bounds__(256) k_bpermute(const uint2* __restrict__ entries,
                                                   const uint32_t* __restrict__ cell_start,
@@ -87,7 +128,8 @@ __global__ void __launch_bounds__(256) k_bpermute(const uint2* __restrict__ entr
                                                   uint32_t* __restrict__ idx, const float4* __restrict__ pos_u,
                                                   const float4* __restrict__ veleval_u, float4* __restrict__ pos_s,
                                                   float4* __restrict__ veleval_s, int* __restrict__ info,
-                                                  int cell_bits) {
+                                                  int cell_bits, float* __restrict__ pxy, float* __restrict__ pz,
+                                                  const float4* __restrict__ vel_u, float4* __restrict__ vel_s) {
     const int nvalid = info[sphk::kNum];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nvalid) return;
@@ -106,7 +148,20 @@ __global__ void __launch_bounds__(256) k_bpermute(const uint2* __restrict__ entr
     keys[i] = key;
     idx[p] = id;
     pos_s[p] = pq;
+    {
+        // the pair layout of the default arithmetic's density pass
+        const uint32_t k = p >> 1, l = p & 1u;
+        pxy[4 * k + l] = pq.x;
+        pxy[4 * k + 2 + l] = pq.y;
+        pz[2 * k + l] = pq.z;
+        if (i == nvalid - 1 && (nvalid & 1)) {  // the last pair's unused lane
+            pxy[4 * (nvalid >> 1) + 1] = sphk::kFarAway;
+            pxy[4 * (nvalid >> 1) + 3] = sphk::kFarAway;
+            pz[2 * (nvalid >> 1) + 1] = sphk::kFarAway;
+        }
+    }
     veleval_s[p] = vq;
+    if (__ldg(cell_start + __ldg(cbase + s) + (uint32_t)table[s].nb_cells) != sphk::kEmpty) vel_s[p] = __ldg(vel_u + id);
     if (cell == (uint32_t)table[s].nb_cells) {
         atomicAdd(info + kBatchFrozen, 1);
         atomicAdd(info + kBatchFrozenTotal, 1);
@@ -145,7 +200,7 @@ static void batch_free(sph_batch* b) {
     void* ptrs[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi, b->density,
                     b->mask, b->keys_a, b->idx_a, b->keys_b, b->idx_b, b->cell_start, b->cell_end, b->scene_of,
                     b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->info_nb, b->cell_count, b->cell_tile_total,
-                    b->cell_entries};
+                    b->cell_entries, b->pos_xy, b->pos_z, b->vel_s, b->d_seg, b->d_del};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->host_info) cudaFreeHost(b->host_info);
@@ -153,7 +208,21 @@ static void batch_free(sph_batch* b) {
 }
 
 sphk::ManyScenes batch_scenes(const sph_batch* b) {
-    return sphk::ManyScenes{b->d_table, b->d_cbase, b->keys_a, b->cell_bits};
+    return sphk::ManyScenes{b->d_table, b->d_cbase, b->keys_a, b->cell_bits, b->d_seg, b->d_slot_off,
+                            b->cell_start, b->d_num, b->d_del, b->vel_s};
+}
+
+int batch_refresh_num(sph_batch* b) {
+    std::vector<int> n(b->nscenes);
+    BCK(b, cudaMemcpyAsync(n.data(), b->d_num, sizeof(int) * b->nscenes, cudaMemcpyDeviceToHost, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    int total = 0;
+    for (int s = 0; s < b->nscenes; ++s) {
+        b->num[s] = n[s];
+        total += n[s];
+    }
+    b->nvalid = total;
+    return SPH_OK;
 }
 
 int batch_enqueue_step(sph_batch* b, float dt) {
@@ -164,6 +233,7 @@ int batch_enqueue_step(sph_batch* b, float dt) {
     k_bcount<<<blocks < 1 ? 1 : blocks, 256, 0, st>>>(b->pos_u, b->keys_b, b->idx_b, b->cell_count, b->scene_of,
                                                        b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->nslots,
                                                        b->cell_bits, b->invalid_key);
+    k_bscene_scan<<<1, 1024, 0, st>>>(b->d_num, b->d_seg, b->info_nb, b->nscenes);
     sphk::launch_cell_totals(b->cell_count, b->cell_tile_total, nullptr, cells, st);
     sphk::launch_cell_scan(b->cell_count, b->cell_start, b->cell_end, b->cell_tile_total, nullptr, cells, st);
     k_bplace<<<blocks < 1 ? 1 : blocks, 256, 0, st>>>(b->keys_b, b->idx_b, b->cell_start, b->d_cbase, b->cell_entries,
@@ -171,11 +241,12 @@ int batch_enqueue_step(sph_batch* b, float dt) {
     const int cb = (b->nvalid + 255) / 256;
     k_bpermute<<<cb < 1 ? 1 : cb, 256, 0, st>>>(b->cell_entries, b->cell_start, b->cell_end, b->d_cbase, b->d_table,
                                                 b->keys_a, b->idx_a, b->pos_u, b->veleval_u, b->pos_s, b->veleval_s,
-                                                b->info_nb, b->cell_bits);
+                                                b->info_nb, b->cell_bits, reinterpret_cast<float*>(b->pos_xy),
+                                                reinterpret_cast<float*>(b->pos_z), b->vel_u, b->vel_s);
     const sphk::ManyScenes scenes = batch_scenes(b);
     sphk::launch_density_batch(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, nullptr, b->mask,
                                (size_t)b->nslots, b->cell_start, b->cell_end, b->info_nb, scenes, b->unit != 0,
-                               b->exact, b->nvalid, st);
+                               b->exact, b->nvalid, b->pos_xy, b->pos_z, false, st);
     sphk::launch_force_batch(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->cell_start, b->cell_end,
                              b->info_nb, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, b->keep_f, b->keep_v, scenes,
                              b->unit != 0, dt, b->exact, b->nvalid, st);
@@ -249,6 +320,11 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     BALLOC(b->veleval_s, N * 16);
     BALLOC(b->rec_pd, N * 16);
     BALLOC(b->rec_vi, N * 16);
+    BALLOC(b->pos_xy, (N / 2 + 1) * 16);
+    BALLOC(b->vel_s, N * 16);
+    BALLOC(b->d_seg, nscenes * 4);
+    BALLOC(b->d_del, nscenes * 4);
+    BALLOC(b->pos_z, (N / 2 + 1) * 8);
     BALLOC(b->density, N * 4);
     BALLOC(b->mask, N * 4 * sphk::kMaskWords);
     BALLOC(b->keys_a, N * 4);
@@ -286,10 +362,12 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     if (e == cudaSuccess) e = cudaMemcpy(b->d_cbase, b->cbase.data(), nscenes * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_table, b->P.data(), nscenes * sizeof(StepParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_num, 0, nscenes * 4);
+    if (e == cudaSuccess) e = cudaMemset(b->d_del, 0, nscenes * 4);
+    if (e == cudaSuccess) e = cudaMemset(b->d_seg, 0, nscenes * 4);
     if (e == cudaSuccess) e = cudaMemset(b->info_nb, 0, sizeof(int) * sphk::kInfoSlots);
     if (e == cudaSuccess) e = cudaMemset(b->cell_count, 0, cells * 4);
     if (e == cudaSuccess) e = cudaMemset(b->cell_entries, 0, N * 8);
-    const void* zero[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi};
+    const void* zero[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi, b->vel_s};
     for (const void* p : zero)
         if (e == cudaSuccess) e = cudaMemset((void*)p, 0, N * 16);
     if (e == cudaSuccess) e = cudaMemset(b->cell_start, 0xff, cells * 4);
@@ -380,6 +458,8 @@ int sph_batch_upload(sph_batch* b, int scene, const sph_float4* pos, const sph_f
     if (!b || scene < 0 || scene >= b->nscenes || !pos || !vel || n < 0 || n > b->max_num[scene])
         return berr(b, SPH_EINVAL, "sph_batch_upload: bad arguments");
     cudaStream_t st = b->stream;
+    int rc = batch_refresh_num(b);  // earlier steps may have deleted particles
+    if (rc) return rc;
     const size_t off = b->slot_off[scene], bytes = (size_t)n * 16;
     if (n > 0) {
         BCK(b, cudaMemcpyAsync(b->pos_u + off, pos, bytes, cudaMemcpyHostToDevice, st));
@@ -390,6 +470,7 @@ int sph_batch_upload(sph_batch* b, int scene, const sph_float4* pos, const sph_f
             BCK(b, cudaMemsetAsync(b->veleval_u + off, 0, bytes, st));
     }
     k_bset<<<1, 1, 0, st>>>(b->d_num + scene, n);
+    k_bset<<<1, 1, 0, st>>>(b->d_del + scene, 0);
     b->nvalid += n - b->num[scene];
     b->num[scene] = n;
     k_bset<<<1, 1, 0, st>>>(b->info_nb + sphk::kNum, b->nvalid);
@@ -443,6 +524,34 @@ int sph_batch_out_of_grid(sph_batch* b, int* count) {
     BCK(b, cudaStreamSynchronize(b->stream));
     *count = v;
     return SPH_OK;
+}
+
+int sph_batch_get_num(sph_batch* b, int scene, int* n) {
+    if (!b || !n || scene < 0 || scene >= b->nscenes) return berr(b, SPH_EINVAL, "sph_batch_get_num: bad arguments");
+    cudaSetDevice(b->device);
+    const int rc = batch_refresh_num(b);
+    if (rc) return rc;
+    *n = b->num[scene];
+    return SPH_OK;
+}
+
+int sph_batch_get_deleted(sph_batch* b, int scene, sph_float4* pos, sph_float4* vel, int cap, int* count) {
+    if (!b || !count || scene < 0 || scene >= b->nscenes || cap < 0 || (cap > 0 && (!pos || !vel)))
+        return berr(b, SPH_EINVAL, "sph_batch_get_deleted: bad arguments");
+    cudaSetDevice(b->device);
+    int rc = batch_refresh_num(b);
+    if (rc) return rc;
+    int del = 0;
+    BCK(b, cudaMemcpyAsync(&del, b->d_del + scene, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    *count = del;
+    const int k = del < cap ? del : cap;
+    if (k > 0) {
+        const size_t off = (size_t)b->slot_off[scene] + (size_t)b->num[scene];
+        BCK(b, cudaMemcpyAsync(pos, b->pos_u + off, (size_t)k * 16, cudaMemcpyDeviceToHost, b->stream));
+        BCK(b, cudaMemcpyAsync(vel, b->vel_u + off, (size_t)k * 16, cudaMemcpyDeviceToHost, b->stream));
+    }
+    return sph_batch_sync(b);
 }
 
 int sph_batch_download(sph_batch* b, int scene, int field, void* host, int n) {

@@ -28,6 +28,11 @@ struct sph_batch {
     // device
     float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr, *pos_s = nullptr, *veleval_s = nullptr;
     float4 *rec_pd = nullptr, *rec_vi = nullptr;
+    float4* vel_s = nullptr;   // sorted velocities of the scenes that delete particles this step
+    uint32_t* d_seg = nullptr;  // first sorted index of every scene (this step)
+    int* d_del = nullptr;       // particles removed by every scene's last deletion
+    float4* pos_xy = nullptr;  // sorted positions as pairs (default arithmetic's density pass)
+    float2* pos_z = nullptr;
     float* density = nullptr;
     uint32_t *mask = nullptr, *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
     uint32_t *cell_start = nullptr, *cell_end = nullptr;
@@ -51,6 +56,9 @@ struct sph_batch {
 };
 
 int berr(sph_batch* b, int code, const char* fmt, ...);
+// Reads the per-scene particle counts back (they drop when a scene deletes
+// particles that left its grid) into b->num and b->nvalid.  Blocking.
+int batch_refresh_num(sph_batch* b);
 sphk::ManyScenes batch_scenes(const sph_batch* b);
 int batch_enqueue_step(sph_batch* b, float dt);
 void sph_batch_adjoint_release(sph_batch* b);

@@ -290,7 +290,8 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
                                                       const float4* __restrict__ vel_u,
                                                       const float4* __restrict__ veleval_u,
                                                       float4* __restrict__ pos_s, float4* __restrict__ vel_s,
-                                                      float4* __restrict__ veleval_s, const int* __restrict__ info) {
+                                                      float4* __restrict__ veleval_s, const int* __restrict__ info,
+                                                      float* __restrict__ pxy, float* __restrict__ pz) {
     const int n = info[kNum];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
@@ -312,6 +313,18 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
     keys[s] = key;  // one key over the whole cell
     idx[p] = id;
     pos_s[p] = pq;
+    if (pxy != nullptr) {
+        // the pair layout of k_density_pairs: (x, x', y, y') and (z, z')
+        const uint32_t k = p >> 1, l = p & 1u;
+        pxy[4 * k + l] = pq.x;
+        pxy[4 * k + 2 + l] = pq.y;
+        pz[2 * k + l] = pq.z;
+        if (s == n - 1 && (n & 1)) {  // the last pair's unused lane
+            pxy[4 * (n >> 1) + 1] = kFarAway;
+            pxy[4 * (n >> 1) + 3] = kFarAway;
+            pz[2 * (n >> 1) + 1] = kFarAway;
+        }
+    }
     if (Gather >= 1) veleval_s[p] = vq;
     if (Gather == 2) vel_s[p] = wq;
 }
@@ -347,17 +360,19 @@ void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const ui
 void launch_cell_permute(const uint2* entries, const uint32_t* cell_start, const uint32_t* cell_end, uint32_t* keys,
                          uint32_t* idx, const float4* pos_u, const float4* vel_u, const float4* veleval_u,
                          float4* pos_s, float4* vel_s, float4* veleval_s, const int* info, int grid_items, int gather,
-                         cudaStream_t st) {
+                         float4* pxy, float2* pz, cudaStream_t st) {
     const int blocks = grid_items > 0 ? (grid_items + 255) / 256 : 1;
+    float* fxy = reinterpret_cast<float*>(pxy);
+    float* fz = reinterpret_cast<float*>(pz);
     if (gather == 2)
         k_cell_permute<2><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
-                                                  pos_s, vel_s, veleval_s, info);
+                                                  pos_s, vel_s, veleval_s, info, fxy, fz);
     else if (gather == 1)
         k_cell_permute<1><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
-                                                  pos_s, vel_s, veleval_s, info);
+                                                  pos_s, vel_s, veleval_s, info, fxy, fz);
     else
         k_cell_permute<0><<<blocks, 256, 0, st>>>(entries, cell_start, cell_end, keys, idx, pos_u, vel_u, veleval_u,
-                                                  pos_s, vel_s, veleval_s, info);
+                                                  pos_s, vel_s, veleval_s, info, fxy, fz);
 }
 
 }  // namespace sphk

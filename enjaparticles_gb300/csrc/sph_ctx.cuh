@@ -40,6 +40,10 @@ struct sph_ctx {
     float* density = nullptr;
     float4* rec_pd = nullptr;    // (scaled pos, rho) per sorted particle
     float4* rec_vi = nullptr;    // (veleval, 1/rho) per sorted particle
+    // sorted positions as pairs for the default arithmetic's density pass:
+    // (x, x', y, y') and (z, z') of sorted particles 2k, 2k+1
+    float4* pos_xy = nullptr;
+    float2* pos_z = nullptr;
     uint32_t* nbr = nullptr;
     uint32_t* mask = nullptr;    // neighbour bitmask [kMaskWords][max_num]
     uint32_t *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;

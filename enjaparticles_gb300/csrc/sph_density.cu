@@ -114,14 +114,164 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
     if (WantCount) nbr[i] = cnt;
 }
 
+// ---------------------------------------------------------------------------
+// Default arithmetic, unit simulation scale: the same walk, candidates taken
+// two at a time with Blackwell's two-lane FP32 instructions.  The sorted
+// positions are also kept as pairs, pxy[k] = (x, x', y, y') and
+// pz[k] = (z, z') of sorted particles 2k and 2k+1, so that the x, y and z of
+// two candidates are one register pair each; one packed instruction forms
+// both candidates' dx (dy, dz), r^2 takes three, the clamped weight
+// (h^2 - r^2)^3 and its sum two more.  A run [rs, re) of sorted indices is
+// walked as the pairs that hold it; the first and the last pair may hold one
+// element outside the run, which takes no part (neither in the sum nor in
+// the mask).  The density is the sum of the two lanes' partial sums: the
+// summation order differs from the reference's, within the default mode's
+// tolerance.  The neighbour bitmask is the one the scalar pass writes (bit b:
+// the b-th candidate in walk order), built per segment of up to 16 pairs and
+// appended to the word stream.
+constexpr int kPairSegment = 16;  // pairs per mask segment (32 bits)
+
+template <bool WantCount, class Scenes>
+__global__ void __launch_bounds__(256) k_density_pairs(const float4* __restrict__ pos_s,
+                                                       const float4* __restrict__ pxy, const float2* __restrict__ pz,
+                                                       const float4* __restrict__ veleval_s,
+                                                       float* __restrict__ density, float4* __restrict__ rec_pd,
+                                                       float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
+                                                       uint32_t* __restrict__ mask, const size_t mstride,
+                                                       const uint32_t* __restrict__ cs0,
+                                                       const uint32_t* __restrict__ ce0, const int* __restrict__ info,
+                                                       const Scenes R) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const StepParams& P = R.params(i);
+    const uint32_t* cs = cs0 + R.cell_base(i);
+    const uint32_t* ce = ce0 + R.cell_base(i);
+    const float4 pi = __ldg(pos_s + i);
+    if (R.frozen(i)) {
+        density[i] = 0.f;
+        rec_pd[i] = make_float4(pi.x, pi.y, pi.z, 0.f);
+        if (veleval_s != nullptr)
+            rec_vi[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else
+            reinterpret_cast<float*>(rec_vi + i)[3] = 0.f;
+        if (WantCount) nbr[i] = 0;
+        return;
+    }
+    const float rc2 = P.rcut2;
+    const float2 px = make_float2(pi.x, pi.x), py = make_float2(pi.y, pi.y), pzz = make_float2(pi.z, pi.z);
+    const float2 h2 = make_float2(P.h2, P.h2), neg1 = make_float2(-1.f, -1.f);
+    float2 acc = make_float2(0.f, 0.f);
+    uint32_t cnt = 0;
+    // word stream of the bitmask: `cur` holds `fill` bits of word `wo`
+    uint32_t cur = 0, fill = 0, wo = 0;
+    uint32_t* mrow = mask + i;
+    auto append = [&](uint32_t v, uint32_t len) {  // len in [0, 32], v has no bits at or above len
+        cur |= v << fill;
+        if (fill + len >= 32u) {
+            if (wo < (uint32_t)kMaskWords) mrow[(size_t)wo * mstride] = cur;
+            ++wo;
+            cur = fill ? (v >> (32u - fill)) : 0u;
+            fill = fill + len - 32u;
+        } else {
+            fill += len;
+        }
+    };
+    auto pair_of = [&](uint32_t k, bool v0, bool v1, uint32_t& seg, uint32_t bit) {
+        const float4 xy = __ldg(pxy + k);
+        const float2 zz = __ldg(pz + k);
+        const float2 dx = __ffma2_rn(make_float2(xy.x, xy.y), neg1, px);
+        const float2 dy = __ffma2_rn(make_float2(xy.z, xy.w), neg1, py);
+        const float2 dz = __ffma2_rn(zz, neg1, pzz);
+        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+        float2 hr = __ffma2_rn(r2, neg1, h2);
+        const bool n0 = v0 && r2.x <= rc2, n1 = v1 && r2.y <= rc2;
+        hr.x = n0 ? hr.x : 0.f;
+        hr.y = n1 ? hr.y : 0.f;
+        acc = __ffma2_rn(__fmul2_rn(hr, hr), hr, acc);
+        if (n0) seg |= bit;
+        if (n1) seg |= bit << 1;
+    };
+    auto run = [&](uint32_t rs, uint32_t re) {
+        const uint32_t kend = (re + 1u) >> 1;
+        for (uint32_t ks = rs >> 1; ks < kend; ks += kPairSegment) {
+            const uint32_t ke = ks + kPairSegment < kend ? ks + kPairSegment : kend;
+            uint32_t seg = 0;
+            uint32_t k = ks;
+            // the run's first pair (its element 2k may precede rs)
+            if (2u * k < rs) {
+                pair_of(k, false, 2u * k + 1u < re, seg, 1u);
+                ++k;
+            }
+            // inner pairs: both elements in the run
+            const uint32_t kin = (2u * ke <= re) ? ke : ke - 1u;
+#pragma unroll 2
+            for (; k < kin; ++k) pair_of(k, true, true, seg, 1u << (2u * (k - ks)));
+            // the run's last pair (its element 2k+1 may be re)
+            if (k < ke) pair_of(k, true, 2u * k + 1u < re, seg, 1u << (2u * (k - ks)));
+            if (WantCount) cnt += (uint32_t)__popc(seg);
+            const uint32_t e0 = 2u * ks;
+            if ((uint32_t)i - e0 < 32u) seg &= ~(1u << ((uint32_t)i - e0));  // not itself
+            const uint32_t lo = rs > e0 ? rs - e0 : 0u;
+            const uint32_t hi = (re < 2u * ke ? re : 2u * ke) - e0;
+            append(seg >> lo, hi - lo);
+        }
+    };
+    const int3 c = grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
+    if (cell_fast(P, c))
+        walk_rows_fast(P, cs, ce, c, run);
+    else
+        walk_rows_slow(P, cs, ce, c, run);
+    if (fill != 0 && wo < (uint32_t)kMaskWords) mrow[(size_t)wo * mstride] = cur;
+    const float rho = P.dens_coef * (acc.x + acc.y);
+    density[i] = rho;
+    rec_pd[i] = make_float4(pi.x, pi.y, pi.z, rho);
+    if (veleval_s != nullptr) {
+        const float4 ve = __ldg(veleval_s + i);
+        rec_vi[i] = make_float4(ve.x, ve.y, ve.z, __frcp_rn(rho));
+    } else {
+        reinterpret_cast<float*>(rec_vi + i)[3] = __frcp_rn(rho);
+    }
+    if (WantCount) nbr[i] = cnt;
+}
+
+// Sorted positions as pairs (see k_density_pairs), for the passes whose
+// permute does not write them.
+__global__ void k_pack_pairs(const float4* __restrict__ pos_s, float4* __restrict__ pxy, float2* __restrict__ pz,
+                             const int* __restrict__ info) {
+    const int n = info[kNum];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (2 * k >= n) return;
+    const float4 a = __ldg(pos_s + 2 * k);
+    const float4 b = 2 * k + 1 < n ? __ldg(pos_s + 2 * k + 1) : make_float4(kFarAway, kFarAway, kFarAway, 1.f);
+    pxy[k] = make_float4(a.x, b.x, a.y, b.y);
+    pz[k] = make_float2(a.z, b.z);
+}
+
 template <class Scenes>
 void launch_density_t(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                       uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                       const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
-                      int grid_items, cudaStream_t st) {
+                      int grid_items, float4* pxy, float2* pz, bool pack, cudaStream_t st) {
     const int threads = 256;
     int blocks = (grid_items + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
+    if (pxy != nullptr && pz != nullptr && unit && !exact) {
+        if (pack) {
+            const int pb = ((grid_items + 1) / 2 + 255) / 256;
+            k_pack_pairs<<<pb < 1 ? 1 : pb, 256, 0, st>>>(pos_s, pxy, pz, info);
+        }
+        if (nbr)
+            k_density_pairs<true, Scenes><<<blocks, threads, 0, st>>>(pos_s, pxy, pz, veleval_s, density, rec_pd,
+                                                                      rec_vi, nbr, mask, mask_stride, cell_start,
+                                                                      cell_end, info, R);
+        else
+            k_density_pairs<false, Scenes><<<blocks, threads, 0, st>>>(pos_s, pxy, pz, veleval_s, density, rec_pd,
+                                                                       rec_vi, nbr, mask, mask_stride, cell_start,
+                                                                       cell_end, info, R);
+        return;
+    }
 #define SPH_DENSITY_LAUNCH(E, U, W)                                                                               \
     k_density<E, U, W, Scenes><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, \
                                                            mask_stride, cell_start, cell_end, info, R)
@@ -142,17 +292,19 @@ void launch_density_t(const float4* pos_s, const float4* veleval_s, float* densi
 
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
-                    const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, cudaStream_t st) {
+                    const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
+                    float2* pz, bool pack, cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, st);
+                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, pxy, pz, pack, st);
 }
 
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                          const ManyScenes& scenes, bool unit, int exact, int grid_items, cudaStream_t st) {
+                          const ManyScenes& scenes, bool unit, int exact, int grid_items, float4* pxy, float2* pz,
+                          bool pack, cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     scenes, unit, exact != 0, grid_items, st);
+                     scenes, unit, exact != 0, grid_items, pxy, pz, pack, st);
 }
 
 }  // namespace sphk

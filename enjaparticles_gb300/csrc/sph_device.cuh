@@ -20,6 +20,8 @@
 namespace sphk {
 
 constexpr uint32_t kEmpty = 0xffffffffu;
+// Coordinate of the unused lane of the last position pair (never a neighbour).
+constexpr float kFarAway = 1.0e18f;
 
 // Device counters block (ctx->info).
 enum InfoSlot : int {
@@ -82,8 +84,11 @@ constexpr int kMaxTriangles = 1 << 20;
 //   ManyScenes: a batch of independent systems sorted together; the scene of
 //   sorted particle i is the high part of its key (key = scene << cell_bits |
 //   cell), each scene has its own parameter block and its own segment of the
-//   cell arrays.  A particle in its scene's out-of-grid cell is frozen: not
-//   walked, not integrated (a lone system would delete it).
+//   cell arrays.  A particle in its scene's out-of-grid cell is left out of
+//   the neighbour passes (`frozen`) and deleted by the force pass, as a lone
+//   system deletes it (SPH.cpp:220-250): the scene keeps its first sorted
+//   particles, re-indexed in sorted order, and the removed ones go to the
+//   slots after them.
 struct OneScene {
     StepParams P;
     __device__ __forceinline__ const StepParams& params(int) const { return P; }
@@ -96,12 +101,23 @@ struct ManyScenes {
     const uint32_t* cbase;
     const uint32_t* keys;
     int cell_bits;
+    // deletion (the force pass of the batched step; null elsewhere)
+    const uint32_t* seg;       // first sorted index of every scene this step
+    const uint32_t* slot_off;  // first particle slot of every scene
+    const uint32_t* cstart;    // cell_start of all scenes' cells
+    int* num;                  // particles per scene
+    int* del;                  // particles removed by the scene's last deletion
+    const float4* vel_s;       // sorted velocities of the scenes that delete
     __device__ __forceinline__ uint32_t scene(int i) const { return __ldg(keys + i) >> cell_bits; }
     __device__ __forceinline__ const StepParams& params(int i) const { return table[scene(i)]; }
     __device__ __forceinline__ uint32_t cell_base(int i) const { return __ldg(cbase + scene(i)); }
     __device__ __forceinline__ bool frozen(int i) const {
         const uint32_t k = __ldg(keys + i);
         return (k & ((1u << cell_bits) - 1u)) == (uint32_t)table[k >> cell_bits].nb_cells;
+    }
+    // First out-of-grid sorted index of scene s, kEmpty when it has none.
+    __device__ __forceinline__ uint32_t out_start(uint32_t s) const {
+        return __ldg(cstart + __ldg(cbase + s) + (uint32_t)table[s].nb_cells);
     }
 };
 
@@ -161,17 +177,23 @@ void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end,
                       uint32_t cells, cudaStream_t st);
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
                        const int* info, int grid_items, cudaStream_t st);
+// pxy / pz (nullable): the sorted positions also as pairs (launch_density).
 void launch_cell_permute(const uint2* entries, const uint32_t* cell_start, const uint32_t* cell_end, uint32_t* keys,
                          uint32_t* idx, const float4* pos_u, const float4* vel_u, const float4* veleval_u,
                          float4* pos_s, float4* vel_s, float4* veleval_s, const int* info, int grid_items, int gather,
-                         cudaStream_t st);
+                         float4* pxy, float2* pz, cudaStream_t st);
 void launch_cells_permute(const uint32_t* keys, const uint32_t* idx, uint32_t* cell_start, uint32_t* cell_end,
                           const float4* pos_u, const float4* vel_u, const float4* veleval_u, float4* pos_s,
                           float4* vel_s, float4* veleval_s, int* info, int nb_cells, int grid_items, int gather,
                           cudaStream_t st);
+// pxy / pz: the sorted positions as pairs (k_density_pairs, sph_density.cu),
+// used by the default arithmetic at unit simulation scale (nullable: the
+// scalar pass then runs); pack: write them from pos_s first (for sorts
+// whose permute does not).
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
-                    const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, cudaStream_t st);
+                    const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
+                    float2* pz, bool pack, cudaStream_t st);
 // The fused step's velocity pass, beside density and before force (the first
 // passes that need the uploaded velocities): the veleval lanes of rec_vi in
 // sorted order, and the out-of-grid bookkeeping (kept velocities into vel_s
@@ -191,7 +213,8 @@ void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_v
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                          const ManyScenes& scenes, bool unit, int exact, int grid_items, cudaStream_t st);
+                          const ManyScenes& scenes, bool unit, int exact, int grid_items, float4* pxy, float2* pz,
+                          bool pack, cudaStream_t st);
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                         size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                         uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,

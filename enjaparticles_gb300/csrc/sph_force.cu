@@ -103,6 +103,24 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     const int t = threadIdx.x;
     const int i = blockIdx.x * kForceThreads + t;
     const bool live = i < n && !R.frozen(i);
+    if constexpr (std::is_same<Scenes, ManyScenes>::value) {
+        // A batch particle outside its scene's grid: removed from the scene
+        // (SPH.cpp:220-250), stored after the scene's kept particles (in
+        // sorted order, as a lone system's deleted list); the first one sets
+        // the scene's new count.  The scene's kept particles read their
+        // velocities from vel_s and are re-indexed below, so no slot written
+        // here is read by this pass.
+        if (Fused && i < n && !live) {
+            const uint32_t sc = R.scene(i), os = R.out_start(sc), kept = os - __ldg(R.seg + sc);
+            const uint32_t j = (uint32_t)i - os, dst = __ldg(R.slot_off + sc) + kept + j;
+            pos_u[dst] = __ldg(pos_s + i);
+            vel_u[dst] = __ldg(R.vel_s + i);
+            if (j == 0) {
+                R.del[sc] = R.num[sc] - (int)kept;
+                R.num[sc] = (int)kept;
+            }
+        }
+    }
     const unsigned wmask = __ballot_sync(0xffffffffu, live);
     if (!live) return;
     const StepParams& P = R.params(i);
@@ -228,13 +246,24 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     // (sort_indices becomes the identity; their velocities are in vel_s).
     uint32_t orig;
     float4 v;
-    if (out >= 0) {
+    bool reindex = out >= 0;
+    if constexpr (std::is_same<Scenes, ManyScenes>::value) {
+        // a scene that deletes keeps its particles in sorted order
+        const uint32_t sc = R.scene(i);
+        if (R.out_start(sc) != kEmpty) {
+            orig = __ldg(R.slot_off + sc) + ((uint32_t)i - __ldg(R.seg + sc));
+            v = __ldg(R.vel_s + i);
+            idx[i] = orig;
+            reindex = true;
+        }
+    }
+    if (!reindex) {
+        orig = __ldg(idx + i);
+        v = vel_u[orig];
+    } else if (out >= 0) {
         orig = (uint32_t)i;
         v = vel_s[i];
         idx[i] = (uint32_t)i;
-    } else {
-        orig = __ldg(idx + i);
-        v = vel_u[orig];
     }
     if (keep_f != nullptr) {
         keep_f[i] = f;

@@ -472,9 +472,10 @@ int sph_loss_mse(sph_ctx* ctx, const sph_float4* target, sph_float4* dL_dpos, do
  * grid and particle count) stepped together.  No counterpart in the
  * reference, which steps one system per SPH object.  All scenes share one
  * launch sequence per step (captured in one CUDA graph); every scene steps
- * exactly as it would in its own context.  Particles that leave their
- * scene's grid are frozen and counted (sph_batch_out_of_grid) instead of
- * deleted.
+ * exactly as it would in its own context, deletions included: particles that
+ * leave their scene's grid are removed from it as SPH::updateGPU removes
+ * them (SPH.cpp:220-250), the scene's count drops (sph_batch_get_num) and
+ * the removed particles can be read back (sph_batch_get_deleted).
  * ------------------------------------------------------------------------- */
 typedef struct sph_batch sph_batch;
 
@@ -492,8 +493,17 @@ int sph_batch_upload(sph_batch* batch, int scene, const sph_float4* pos, const s
 int sph_batch_step(sph_batch* batch, float dt, int nsteps);
 /* Copy n elements of pos_u, vel_u or veleval_u of one scene.  Blocking. */
 int sph_batch_download(sph_batch* batch, int scene, int field, void* host, int n);
-/* Number of frozen (out-of-grid) particles in the last step.  Blocking. */
+/* Number of particles, over all scenes, that the last step removed because
+ * they had left their scene's grid.  Blocking. */
 int sph_batch_out_of_grid(sph_batch* batch, int* count);
+/* Current particle count of one scene (SPH::getNum; it drops after a
+ * deletion).  Blocking. */
+int sph_batch_get_num(sph_batch* batch, int scene, int* n);
+/* The particles removed by the scene's last deletion, in sorted order, as
+ * SPH::getDeletedPos / getDeletedVel (SPH.h:83-84): *count = how many; the
+ * first min(count, cap) positions and velocities are copied to the host
+ * arrays.  Valid until the scene's next upload or deletion.  Blocking. */
+int sph_batch_get_deleted(sph_batch* batch, int scene, sph_float4* pos, sph_float4* vel, int cap, int* count);
 int sph_batch_sync(sph_batch* batch);
 int sph_batch_last_error(sph_batch* batch, char* buf, int len);
 /* Replace scene `scene`'s SPHParams (same simulation_scale; the grid stays).
