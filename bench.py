@@ -46,9 +46,11 @@ sys.path.insert(0, ROOT)
 N_DEFAULT = 2097152
 DT = 0.001
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) of one launch, from an ncu capture of the 2M step
-# (profiles/sph_density_force_2M.md); reported as roofline.traffic for the
-# dominant kernel when it is one of these.
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the current kernels, from one ncu capture of the 2,097,152-particle dam break
+# at the state named here; reported as roofline.traffic (with that state) for
+# the dominant kernel at that workload.
+TRAFFIC_STATE = "one launch at step 6 of the 2,097,152-particle dam break from the lattice at rest (ncu)"
 MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 203.607552e6 + 72.219392e6,
                     "k_density": 55.70176e6 + 74.822144e6}
 
@@ -68,7 +70,7 @@ def parse():
     ap.add_argument("--ref-seconds", type=float, default=120.0, help="time bound of the reference (CPU) arm")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256)
-    ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--serial-steps", type=int, default=10)
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-calibration", action="store_true")
@@ -85,6 +87,7 @@ def parse():
     ap.add_argument("--steady-at", type=int, default=1000,
                     help="also time --steady-steps steps from this step of the rollout (0: skip)")
     ap.add_argument("--steady-steps", type=int, default=100)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     return ap.parse_args()
 
 
@@ -257,6 +260,7 @@ def bench_batched(args, torch):
         b.upload(k, pos, vel)
     b.step(DT, 5)
     b.sync()
+    shape = list(b.launch_config()) if args.no_autotune else list(b.autotune(DT, steps=3))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(stream)
@@ -265,6 +269,21 @@ def bench_batched(args, torch):
     e1.synchronize()
     t_batch = e0.elapsed_time(e1) / 1e3
     b.sync()
+    # the same steps under the queue scheduler (persistent blocks over
+    # (scene, tile) items), from the same starting state
+    for k, (pos, vel) in enumerate(data):
+        b.upload(k, pos, vel)
+    b.set_scheduler(True)
+    b.step(DT, 5)
+    b.sync()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.step(DT, args.batch_steps)
+    e1.record(stream)
+    e1.synchronize()
+    t_queue = e0.elapsed_time(e1) / 1e3
+    b.sync()
+    b.set_scheduler(False)
     deleted_last = b.out_of_grid()
     b.close()
     ctxs = []
@@ -276,6 +295,9 @@ def bench_batched(args, torch):
     for _ in range(2):
         for s in ctxs:
             s.step(DT, 1)
+    if not args.no_autotune:  # the same tuner for the lone contexts (shapes change no result)
+        for s in ctxs:
+            s.autotune(DT, steps=2)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(args.serial_steps):
@@ -292,6 +314,9 @@ def bench_batched(args, torch):
             "serial_value": serial, "speedup_vs_serial": batched / serial, "batch_steps": args.batch_steps,
             "serial_steps": args.serial_steps, "ms_per_batch_step": 1e3 * t_batch / args.batch_steps,
             "deleted_in_last_step": deleted_last,
+            "launch_config": shape,
+            "schedulers_ms_per_batch_step": {"grid": 1e3 * t_batch / args.batch_steps,
+                                             "queue": 1e3 * t_queue / args.batch_steps},
             "note": "each scene of a batch steps bit-identically to the same scene in its own context"}
 
 
@@ -527,6 +552,14 @@ def main():
     s.upload(pos0, vel0)
     s.step(DT, args.warmup)
     s.sync()
+    # launch shapes: the autotuner times its candidates on this state (which
+    # it restores) and keeps the fastest of each kernel
+    launch = {"tuned": False, "shape": list(s.launch_config())}
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        launch = {"tuned": True, "shape": list(s.autotune(DT, steps=3)),
+                  "tuning_s": time.perf_counter() - t0}
+    launch["keys"] = ["density_threads", "force_threads", "scan_tile_cells"]
     sampler.start()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -626,11 +659,13 @@ def main():
         "gpu_launches": nk.value * steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "traffic": MEASURED_TRAFFIC.get(dom) if n == N_DEFAULT else None, "peak_source": peak_kind,
+                     "traffic": MEASURED_TRAFFIC.get(dom) if n == N_DEFAULT else None,
+                     "traffic_state": TRAFFIC_STATE if n == N_DEFAULT else None, "peak_source": peak_kind,
                      "algorithmic_bytes": ab[dom], "mean_launch_ms": kern_ms[dom]},
         "step_roofline": {"algorithmic_bytes": b_step, "achieved": b_step / (step_ms / 1e3) / 1e9, "peak": peak,
                           "frac": b_step / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s"},
         "steady_state": steady,
+        "launch_config": launch,
         "kernels_ms": kern_ms,
         "kernels_by_phase": by_phase,
         "particles_after": num_after,

@@ -35,6 +35,19 @@ class GridParams(C.Structure):
                 ("grid_delta", sph_float4), ("nb_cells", C.c_int), ("_pad", C.c_int * 3)]
 
 
+class sph_launch_config(C.Structure):
+    """Launch shapes of the step's kernels (include/rtps_sph.h)."""
+    _fields_ = [("density_threads", C.c_int), ("force_threads", C.c_int), ("scan_tile_cells", C.c_int),
+                ("reserved", C.c_int)]
+
+    def as_tuple(self):
+        return (self.density_threads, self.force_threads, self.scan_tile_cells)
+
+
+LAUNCH_CANDIDATES = [(128, 64, 2048), (256, 128, 4096), (512, 256, 8192)]
+SPH_TUNE_RETIME = 1
+SPH_SCHED_GRID, SPH_SCHED_QUEUE = 0, 1
+
 assert C.sizeof(SPHParams) == 144 and SPHParams.gravity.offset == 128
 assert C.sizeof(GridParams) == 128 and GridParams.nb_cells.offset == 112
 
@@ -148,6 +161,15 @@ SIGNATURES = {
     "sph_adjoint_rewind": (_I, [_P]),
     "sph_loss_mse": (_I, [_P, _P, _P, C.POINTER(C.c_double)]),
     "sph_sort_pairs_noalloc": (_I, [_P, _P, _P, _P, _I, _I, _P]),
+    "sph_get_launch_config": (_I, [_P, C.POINTER(sph_launch_config)]),
+    "sph_set_launch_config": (_I, [_P, C.POINTER(sph_launch_config)]),
+    "sph_autotune": (_I, [_P, _F, _I, _I, C.POINTER(sph_launch_config)]),
+    "sph_batch_get_launch_config": (_I, [_P, C.POINTER(sph_launch_config)]),
+    "sph_batch_set_launch_config": (_I, [_P, C.POINTER(sph_launch_config)]),
+    "sph_batch_autotune": (_I, [_P, _F, _I, _I, C.POINTER(sph_launch_config)]),
+    "sph_batch_set_scheduler": (_I, [_P, _I]),
+    "sph_batch_get_scheduler": (_I, [_P, C.POINTER(_I)]),
+    "sph_batch_queue_test_hold": (_I, [_P, _I, C.c_uint]),
     "sph_build_info": (C.c_char_p, []),
 }
 

@@ -88,6 +88,28 @@ class Batch:
                                                     C.byref(cnt)))
         return pos, vel
 
+    def launch_config(self):
+        cfg = abi.sph_launch_config()
+        self._ck(self.lib.sph_batch_get_launch_config(self.h, C.byref(cfg)))
+        return cfg.as_tuple()
+
+    def set_launch_config(self, density_threads, force_threads, scan_tile_cells):
+        cfg = abi.sph_launch_config(int(density_threads), int(force_threads), int(scan_tile_cells), 0)
+        self._ck(self.lib.sph_batch_set_launch_config(self.h, C.byref(cfg)))
+
+    def autotune(self, dt=0.001, steps=3, retime=False):
+        cfg = abi.sph_launch_config()
+        self._ck(self.lib.sph_batch_autotune(self.h, float(dt), int(steps), abi.SPH_TUNE_RETIME if retime else 0,
+                                             C.byref(cfg)))
+        return cfg.as_tuple()
+
+    def set_scheduler(self, queue):
+        """False: one grid per pass (default); True: persistent blocks over (scene, tile) items."""
+        self._ck(self.lib.sph_batch_set_scheduler(self.h, abi.SPH_SCHED_QUEUE if queue else abi.SPH_SCHED_GRID))
+
+    def queue_test_hold(self, hold, spin_limit=1 << 22):
+        self._ck(self.lib.sph_batch_queue_test_hold(self.h, 1 if hold else 0, int(spin_limit)))
+
     def out_of_grid(self):
         """Particles removed by the last step (all scenes)."""
         c = C.c_int()

@@ -3,11 +3,15 @@
 // (rtpslib/opencl/{CLL,Kernel,Buffer}) and the buffer setup of
 // System::prepareSorted / SPH::prepareSorted (System.cpp:198-291,
 // SPH.cpp:482-520).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 
 #include "sph_ctx.cuh"
 
@@ -295,8 +299,9 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
     cudaStream_t st = c->stream;
     sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
     const uint32_t cells = (uint32_t)c->gp.nb_cells + 1u;
-    sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, cells, st);
-    sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, cells, st);
+    sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, cells, c->lc.scan_tile_cells, st);
+    sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, cells,
+                           c->lc.scan_tile_cells, st);
     sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
     // the permute gathers the velocities when gather == 2
     if (gather == 2) {
@@ -312,22 +317,23 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
     return SPH_OK;
 }
 
-// Density over the sorted arrays; the fused step skips the neighbour counts
-// and leaves the veleval lanes of rec_vi to its velocity pass.  pack: the
+// Density over the sorted arrays (with the neighbour counts the force pass
+// reads); the fused step leaves the veleval lanes of rec_vi to its velocity
+// pass.  pack: the
 // position pairs of the default arithmetic are written from pos_s first
 // (the stage API's permutes do not write them; the counting sort's does).
 void density_launch(sph_ctx* c, bool fused, cudaStream_t st, bool pack = false) {
     sphk::launch_density(c->pos_s, fused ? nullptr : c->veleval_s, c->density, c->rec_pd, c->rec_vi,
-                         fused ? nullptr : c->nbr, c->mask,
+                         c->nbr, c->mask,
                          (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, c->pos_xy,
-                         c->pos_z, pack, st);
+                         c->pos_z, pack, c->lc.density_threads, st);
 }
 
 void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {
-    sphk::launch_force(c->pos_s, c->rec_pd, c->rec_vi, c->mask, (size_t)c->max_num, c->cell_start, c->cell_end,
+    sphk::launch_force(c->pos_s, c->rec_pd, c->rec_vi, c->mask, (size_t)c->max_num, c->nbr, c->cell_start, c->cell_end,
                        c->info, c->force_s, c->xsph_s, idx, c->vel_s, c->pos_u, c->vel_u, c->veleval_u,
                        fused ? c->keep_f : nullptr, fused ? c->keep_v : nullptr, c->P, dt, fused ? 1 : 0, c->exact,
-                       c->num_hint, st);
+                       c->num_hint, c->lc.force_threads, st);
 }
 
 }  // namespace
@@ -424,6 +430,51 @@ int join_upload_on(sph_ctx* c, cudaStream_t st) {
 int join_upload(sph_ctx* c) { return join_upload_on(c, c->stream); }
 
 
+// --- launch shapes and the autotuner (helpers shared with the batch) -------
+
+bool sph_launch_config_valid(const sph_launch_config& g) {
+    return (g.density_threads == 128 || g.density_threads == 256 || g.density_threads == 512) &&
+           (g.force_threads == 64 || g.force_threads == 128 || g.force_threads == 256) &&
+           (g.scan_tile_cells == 2048 || g.scan_tile_cells == 4096 || g.scan_tile_cells == 8192) && g.reserved == 0;
+}
+
+// The tuner's candidates: every knob has three values; candidate k takes the
+// k-th of each (the knobs are separate kernels, timed separately).
+const sph_launch_config sph_tune_candidates[3] = {{128, 64, 2048, 0}, {256, 128, 4096, 0}, {512, 256, 8192, 0}};
+
+namespace {
+std::mutex g_tune_mutex;
+std::map<SphTuneKey, sph_launch_config> g_tune_cache;  // results of the tuner in this process
+}  // namespace
+
+bool sph_tune_cache_get(const SphTuneKey& k, sph_launch_config& out) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    const auto it = g_tune_cache.find(k);
+    if (it == g_tune_cache.end()) return false;
+    out = it->second;
+    return true;
+}
+
+void sph_tune_cache_put(const SphTuneKey& k, const sph_launch_config& v) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[k] = v;
+}
+
+sph_launch_config sph_tune_pick(const double t[3][3]) {
+    sph_launch_config best = sph_tune_candidates[1];
+    int bd = 1, bf = 1, bs = 1;
+    for (int k = 0; k < 3; ++k) {
+        if (t[k][0] < t[bd][0]) bd = k;
+        if (t[k][1] < t[bf][1]) bf = k;
+        if (t[k][2] < t[bs][2]) bs = k;
+    }
+    best.density_threads = sph_tune_candidates[bd].density_threads;
+    best.force_threads = sph_tune_candidates[bf].force_threads;
+    best.scan_tile_cells = sph_tune_candidates[bs].scan_tile_cells;
+    return best;
+}
+
+
 extern "C" {
 
 #define SPH_STR_(x) #x
@@ -501,7 +552,7 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->cell_start, C1 * 4);
     ALLOC(c->cell_end, C1 * 4);
     ALLOC(c->cell_count, C1 * 4);
-    ALLOC(c->cell_tile_total, (size_t)sphk::cell_scan_tiles((int)C1) * 4);
+    ALLOC(c->cell_tile_total, (size_t)sphk::cell_scan_tiles((int)C1, sphk::kScanTileMin) * 4);
     ALLOC(c->cell_entries, N * 8);
     ALLOC(c->info, sizeof(int) * sphk::kInfoSlots);
     // point sources: kMaxGravitySources float4 positions, then masses, then alphas
@@ -1058,11 +1109,11 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_count(c->pos_u, c->keys_b, c->idx_b, c->cell_count, c->info, c->P, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, (uint32_t)c->gp.nb_cells + 1u, st);
+        sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, (uint32_t)c->gp.nb_cells + 1u,
+                                 c->lc.scan_tile_cells, st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info,
-                               (uint32_t)c->gp.nb_cells + 1u,
-                               st);
+                               (uint32_t)c->gp.nb_cells + 1u, c->lc.scan_tile_cells, st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
@@ -1097,6 +1148,103 @@ const char* sph_profile_kernel_name(sph_ctx* c, int k) {
                                   "k_force(fused collision+leapfrog)"};
     if (!c || k < 0 || k >= 8) return "";
     return names[k];
+}
+
+// --- launch shapes and the autotuner ----------------------------------------
+
+int sph_get_launch_config(sph_ctx* c, sph_launch_config* cfg) {
+    if (!c || !cfg) return SPH_EINVAL;
+    *cfg = c->lc;
+    return SPH_OK;
+}
+
+int sph_set_launch_config(sph_ctx* c, const sph_launch_config* cfg) {
+    if (!c || !cfg) return SPH_EINVAL;
+    if (!sph_launch_config_valid(*cfg))
+        return set_err(c, SPH_EINVAL, "sph_set_launch_config: shape (%d, %d, %d) not among the candidates",
+                       cfg->density_threads, cfg->force_threads, cfg->scan_tile_cells);
+    c->lc = *cfg;
+    c->params_version++;  // the step graph is captured anew
+    return SPH_OK;
+}
+
+int sph_autotune(sph_ctx* c, float dt, int steps, int flags, sph_launch_config* chosen) {
+    int rc = check_ctx(c);
+    if (rc) return rc;
+    if (steps < 1 || !std::isfinite(dt)) return set_err(c, SPH_EINVAL, "sph_autotune: bad arguments");
+    const SphTuneKey key{0, c->max_num, c->gp.nb_cells, c->exact};
+    sph_launch_config best;
+    if (!(flags & SPH_TUNE_RETIME) && sph_tune_cache_get(key, best)) {
+        c->lc = best;
+        c->params_version++;
+        if (chosen) *chosen = best;
+        return SPH_OK;
+    }
+    if (c->n_tri > 0 || !c->hoses.empty())
+        return set_err(c, SPH_ESTATE, "sph_autotune times the fused step without a triangle mesh or hoses");
+    if ((rc = read_info(c))) return rc;
+    const int num = c->host_info[sphk::kNum];
+    if (num <= 0 || c->num_hint <= 0) return set_err(c, SPH_ESTATE, "sph_autotune: no particles");
+    // Save the state the steps change: pos/vel/veleval, the device counters
+    // and the last deletion's particles.
+    int saved_info[sphk::kInfoSlots];
+    std::memcpy(saved_info, c->host_info, sizeof(saved_info));
+    const int ndel = std::min(std::max(saved_info[sphk::kDeleted], 0), c->max_num);
+    const size_t bytes = (size_t)num * 16, dbytes = (size_t)ndel * 16;
+    float4* save = nullptr;
+    if (cudaMalloc((void**)&save, 3 * bytes + 2 * dbytes + 16) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(c, SPH_ENOMEM, "sph_autotune: %zu bytes of scratch", 3 * bytes + 2 * dbytes);
+    }
+    float4* const fields[5] = {c->pos_u, c->vel_u, c->veleval_u, c->del_pos, c->del_vel};
+    const size_t sizes[5] = {bytes, bytes, bytes, dbytes, dbytes};
+    auto copy_all = [&](bool to_save) -> cudaError_t {
+        size_t off = 0;
+        for (int f = 0; f < 5; ++f) {
+            if (sizes[f] == 0) continue;
+            char* sp = reinterpret_cast<char*>(save) + off;
+            cudaError_t e = to_save ? cudaMemcpyAsync(sp, fields[f], sizes[f], cudaMemcpyDeviceToDevice, c->stream)
+                                    : cudaMemcpyAsync(fields[f], sp, sizes[f], cudaMemcpyDeviceToDevice, c->stream);
+            if (e != cudaSuccess) return e;
+            off += sizes[f];
+        }
+        if (!to_save) {
+            std::memcpy(c->host_info, saved_info, sizeof(saved_info));
+            return cudaMemcpyAsync(c->info, c->host_info, sizeof(saved_info), cudaMemcpyHostToDevice, c->stream);
+        }
+        return cudaSuccess;
+    };
+    const sph_launch_config keep = c->lc;
+    double t[3][3] = {{0}};
+    cudaError_t e = copy_all(true);
+    for (int k = 0; k < 3 && e == cudaSuccess && rc == SPH_OK; ++k) {
+        c->lc = sph_tune_candidates[k];
+        float ms[8];
+        int nk = 0;
+        // one untimed step per candidate (first launches), then the timed ones
+        if ((e = copy_all(false)) != cudaSuccess) break;
+        if ((rc = sph_step_profile(c, dt, 1, ms, 8, &nk))) break;
+        if ((e = copy_all(false)) != cudaSuccess) break;
+        if ((rc = sph_step_profile(c, dt, steps, ms, 8, &nk))) break;
+        t[k][0] = ms[5];
+        t[k][1] = ms[7];
+        t[k][2] = (double)ms[1] + ms[2];
+    }
+    if (e == cudaSuccess) e = copy_all(false);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(save);
+    if (rc || e != cudaSuccess) {
+        c->lc = keep;
+        c->params_version++;
+        if (rc) return rc;
+        return set_err(c, SPH_ECUDA, "sph_autotune: %s", cudaGetErrorString(e));
+    }
+    best = sph_tune_pick(t);
+    c->lc = best;
+    c->params_version++;
+    sph_tune_cache_put(key, best);
+    if (chosen) *chosen = best;
+    return SPH_OK;
 }
 
 int sph_sync(sph_ctx* c) {

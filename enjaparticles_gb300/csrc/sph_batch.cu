@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "sph_batch.cuh"
+#include "sph_queue.cuh"
 
 using sphk::StepParams;
 
@@ -79,7 +80,8 @@ __global__ void __launch_bounds__(256) k_bplace(const uint32_t* __restrict__ key
 }
 
 // Scenes' first sorted indices: the exclusive scan of the particle counts
-// (scene after scene in sorted order), and the batch's particle total.
+// (scene after scene in sorted order; seg[nscenes] = the batch's particle
+// total, also the step's info[kNum]).
 __global__ void __launch_bounds__(1024) k_bscene_scan(const int* __restrict__ num, uint32_t* __restrict__ seg,
                                                       int* __restrict__ info, int nscenes) {
     __shared__ uint32_t s_warp[32];
@@ -112,7 +114,10 @@ __global__ void __launch_bounds__(1024) k_bscene_scan(const int* __restrict__ nu
         if (t == 1023) s_carry = before + v;
         __syncthreads();
     }
-    if (t == 0) info[sphk::kNum] = (int)s_carry;
+    if (t == 0) {
+        info[sphk::kNum] = (int)s_carry;
+        seg[nscenes] = s_carry;
+    }
 }
 
 // Permute: rank within the cell, sorted keys (the scene resolver reads them),
@@ -200,7 +205,8 @@ static void batch_free(sph_batch* b) {
     void* ptrs[] = {b->pos_u, b->vel_u, b->veleval_u, b->pos_s, b->veleval_s, b->rec_pd, b->rec_vi, b->density,
                     b->mask, b->keys_a, b->idx_a, b->keys_b, b->idx_b, b->cell_start, b->cell_end, b->scene_of,
                     b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->info_nb, b->cell_count, b->cell_tile_total,
-                    b->cell_entries, b->pos_xy, b->pos_z, b->vel_s, b->d_seg, b->d_del};
+                    b->cell_entries, b->pos_xy, b->pos_z, b->vel_s, b->d_seg, b->d_del, b->nbr, b->q_state,
+                    b->q_tiles};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->host_info) cudaFreeHost(b->host_info);
@@ -225,7 +231,7 @@ int batch_refresh_num(sph_batch* b) {
     return SPH_OK;
 }
 
-int batch_enqueue_step(sph_batch* b, float dt) {
+int batch_enqueue_step(sph_batch* b, float dt, cudaEvent_t* ev) {
     cudaStream_t st = b->stream;
     const int blocks = (b->nslots + 255) / 256;
     const uint32_t cells = (uint32_t)b->ncells_total;
@@ -234,8 +240,13 @@ int batch_enqueue_step(sph_batch* b, float dt) {
                                                        b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->nslots,
                                                        b->cell_bits, b->invalid_key);
     k_bscene_scan<<<1, 1024, 0, st>>>(b->d_num, b->d_seg, b->info_nb, b->nscenes);
-    sphk::launch_cell_totals(b->cell_count, b->cell_tile_total, nullptr, cells, st);
-    sphk::launch_cell_scan(b->cell_count, b->cell_start, b->cell_end, b->cell_tile_total, nullptr, cells, st);
+    // ev (nullable, sph_batch_autotune): events around the cell totals+scan,
+    // the density pass and the force pass
+    if (ev) BCK(b, cudaEventRecord(ev[0], st));
+    sphk::launch_cell_totals(b->cell_count, b->cell_tile_total, nullptr, cells, b->lc.scan_tile_cells, st);
+    sphk::launch_cell_scan(b->cell_count, b->cell_start, b->cell_end, b->cell_tile_total, nullptr, cells,
+                           b->lc.scan_tile_cells, st);
+    if (ev) BCK(b, cudaEventRecord(ev[1], st));
     k_bplace<<<blocks < 1 ? 1 : blocks, 256, 0, st>>>(b->keys_b, b->idx_b, b->cell_start, b->d_cbase, b->cell_entries,
                                                        b->nslots, b->cell_bits, b->invalid_key);
     const int cb = (b->nvalid + 255) / 256;
@@ -244,12 +255,35 @@ int batch_enqueue_step(sph_batch* b, float dt) {
                                                 b->info_nb, b->cell_bits, reinterpret_cast<float*>(b->pos_xy),
                                                 reinterpret_cast<float*>(b->pos_z), b->vel_u, b->vel_s);
     const sphk::ManyScenes scenes = batch_scenes(b);
-    sphk::launch_density_batch(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, nullptr, b->mask,
+    if (ev) BCK(b, cudaEventRecord(ev[2], st));
+    if (b->sched == SPH_SCHED_QUEUE) {
+        // persistent blocks over (scene, tile) items (sph_queue.cuh)
+        BCK(b, cudaMemsetAsync(b->q_state, 0, 8 * sizeof(unsigned), st));
+        sphk::BatchQueue Q{b->q_state, b->q_tiles, b->d_seg, b->d_slot_off, b->cell_start, b->d_cbase,
+                           b->d_table, b->d_num, b->d_del, b->vel_s, b->info_nb + sphk::kError, b->nscenes,
+                           b->q_spin, b->q_hold};
+        sphk::launch_density_queue(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, b->nbr, b->mask,
+                                   (size_t)b->nslots, b->cell_start, b->cell_end, b->pos_xy, b->pos_z, Q,
+                                   b->unit != 0, b->exact, b->lc.density_threads, st);
+        if (ev) BCK(b, cudaEventRecord(ev[3], st));
+        Q.state = b->q_state + 4;
+        Q.tile_off = b->q_tiles + (b->nscenes + 1);
+        sphk::launch_force_queue(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->nbr, b->cell_start,
+                                 b->cell_end, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, b->keep_f, b->keep_v, Q,
+                                 b->unit != 0, dt, b->exact, b->lc.force_threads, st);
+        if (ev) BCK(b, cudaEventRecord(ev[4], st));
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return berr(b, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
+        return SPH_OK;
+    }
+    sphk::launch_density_batch(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, b->nbr, b->mask,
                                (size_t)b->nslots, b->cell_start, b->cell_end, b->info_nb, scenes, b->unit != 0,
-                               b->exact, b->nvalid, b->pos_xy, b->pos_z, false, st);
-    sphk::launch_force_batch(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->cell_start, b->cell_end,
+                               b->exact, b->nvalid, b->pos_xy, b->pos_z, false, b->lc.density_threads, st);
+    if (ev) BCK(b, cudaEventRecord(ev[3], st));
+    sphk::launch_force_batch(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->nbr, b->cell_start, b->cell_end,
                              b->info_nb, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, b->keep_f, b->keep_v, scenes,
-                             b->unit != 0, dt, b->exact, b->nvalid, st);
+                             b->unit != 0, dt, b->exact, b->nvalid, b->lc.force_threads, st);
+    if (ev) BCK(b, cudaEventRecord(ev[4], st));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return berr(b, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
     return SPH_OK;
@@ -322,10 +356,13 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     BALLOC(b->rec_vi, N * 16);
     BALLOC(b->pos_xy, (N / 2 + 1) * 16);
     BALLOC(b->vel_s, N * 16);
-    BALLOC(b->d_seg, nscenes * 4);
+    BALLOC(b->q_state, 8 * sizeof(unsigned));
+    BALLOC(b->q_tiles, 2 * (nscenes + 1) * 4);
+    BALLOC(b->d_seg, (nscenes + 1) * 4);
     BALLOC(b->d_del, nscenes * 4);
     BALLOC(b->pos_z, (N / 2 + 1) * 8);
     BALLOC(b->density, N * 4);
+    BALLOC(b->nbr, N * 4);
     BALLOC(b->mask, N * 4 * sphk::kMaskWords);
     BALLOC(b->keys_a, N * 4);
     BALLOC(b->idx_a, N * 4);
@@ -340,7 +377,7 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     BALLOC(b->d_table, nscenes * sizeof(StepParams));
     BALLOC(b->info_nb, sizeof(int) * sphk::kInfoSlots);
     BALLOC(b->cell_count, cells * 4);
-    BALLOC(b->cell_tile_total, (size_t)sphk::cell_scan_tiles((int)cells) * 4);
+    BALLOC(b->cell_tile_total, (size_t)sphk::cell_scan_tiles((int)cells, sphk::kScanTileMin) * 4);
     BALLOC(b->cell_entries, N * 8);
 #undef BALLOC
     if (rc == SPH_OK && cudaMallocHost((void**)&b->host_info, sizeof(int) * sphk::kInfoSlots) != cudaSuccess)
@@ -363,7 +400,7 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     if (e == cudaSuccess) e = cudaMemcpy(b->d_table, b->P.data(), nscenes * sizeof(StepParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_num, 0, nscenes * 4);
     if (e == cudaSuccess) e = cudaMemset(b->d_del, 0, nscenes * 4);
-    if (e == cudaSuccess) e = cudaMemset(b->d_seg, 0, nscenes * 4);
+    if (e == cudaSuccess) e = cudaMemset(b->d_seg, 0, (nscenes + 1) * 4);
     if (e == cudaSuccess) e = cudaMemset(b->info_nb, 0, sizeof(int) * sphk::kInfoSlots);
     if (e == cudaSuccess) e = cudaMemset(b->cell_count, 0, cells * 4);
     if (e == cudaSuccess) e = cudaMemset(b->cell_entries, 0, N * 8);
@@ -483,14 +520,15 @@ int sph_batch_step(sph_batch* b, float dt, int nsteps) {
     if (!b || nsteps < 0 || !std::isfinite(dt)) return berr(b, SPH_EINVAL, "sph_batch_step: bad arguments");
     cudaSetDevice(b->device);
     if (nsteps == 0 || b->nvalid == 0) return SPH_OK;
-    if (!b->graph || b->graph_dt != dt || b->graph_valid != b->nvalid || b->graph_exact != b->exact) {
+    if (!b->graph || b->graph_dt != dt || b->graph_valid != b->nvalid || b->graph_exact != b->exact ||
+        b->graph_sched != b->sched || std::memcmp(&b->graph_lc, &b->lc, sizeof(b->lc)) != 0) {
         if (b->graph) {
             cudaGraphExecDestroy(b->graph);
             b->graph = nullptr;
         }
         cudaGraph_t g = nullptr;
         BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = batch_enqueue_step(b, dt);
+        const int rc = batch_enqueue_step(b, dt, nullptr);
         cudaError_t e = cudaStreamEndCapture(b->stream, &g);
         if (rc != SPH_OK) {
             if (g) cudaGraphDestroy(g);
@@ -506,6 +544,8 @@ int sph_batch_step(sph_batch* b, float dt, int nsteps) {
         b->graph_dt = dt;
         b->graph_valid = b->nvalid;
         b->graph_exact = b->exact;
+        b->graph_lc = b->lc;
+        b->graph_sched = b->sched;
     }
     for (int k = 0; k < nsteps; ++k) BCK(b, cudaGraphLaunch(b->graph, b->stream));
     return SPH_OK;
@@ -514,6 +554,35 @@ int sph_batch_step(sph_batch* b, float dt, int nsteps) {
 int sph_batch_sync(sph_batch* b) {
     if (!b) return SPH_EINVAL;
     BCK(b, cudaStreamSynchronize(b->stream));
+    // a bounded wait of the queue scheduler that ran out (sph_queue.cuh)
+    int err = 0;
+    BCK(b, cudaMemcpy(&err, b->info_nb + sphk::kError, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        BCK(b, cudaMemset(b->info_nb + sphk::kError, 0, sizeof(int)));
+        return berr(b, SPH_ETIMEOUT, "a bounded wait of the queue scheduler expired (error word %d); the steps "
+                    "since the last sync are invalid", err);
+    }
+    return SPH_OK;
+}
+
+int sph_batch_set_scheduler(sph_batch* b, int scheduler) {
+    if (!b || (scheduler != SPH_SCHED_GRID && scheduler != SPH_SCHED_QUEUE))
+        return berr(b, SPH_EINVAL, "sph_batch_set_scheduler: %d is not a scheduler", scheduler);
+    b->sched = scheduler;
+    return SPH_OK;
+}
+
+int sph_batch_get_scheduler(sph_batch* b, int* scheduler) {
+    if (!b || !scheduler) return SPH_EINVAL;
+    *scheduler = b->sched;
+    return SPH_OK;
+}
+
+int sph_batch_queue_test_hold(sph_batch* b, int hold, unsigned spin_limit) {
+    if (!b || spin_limit == 0) return berr(b, SPH_EINVAL, "sph_batch_queue_test_hold: bad arguments");
+    b->q_hold = hold ? 1 : 0;
+    b->q_spin = spin_limit;
+    b->graph_valid = -1;  // captured anew with the new queue arguments
     return SPH_OK;
 }
 
@@ -523,6 +592,96 @@ int sph_batch_out_of_grid(sph_batch* b, int* count) {
     BCK(b, cudaMemcpyAsync(&v, b->info_nb + kBatchFrozen, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
     *count = v;
+    return SPH_OK;
+}
+
+int sph_batch_get_launch_config(sph_batch* b, sph_launch_config* cfg) {
+    if (!b || !cfg) return SPH_EINVAL;
+    *cfg = b->lc;
+    return SPH_OK;
+}
+
+int sph_batch_set_launch_config(sph_batch* b, const sph_launch_config* cfg) {
+    if (!b || !cfg) return SPH_EINVAL;
+    if (!sph_launch_config_valid(*cfg))
+        return berr(b, SPH_EINVAL, "sph_batch_set_launch_config: shape (%d, %d, %d) not among the candidates",
+                    cfg->density_threads, cfg->force_threads, cfg->scan_tile_cells);
+    b->lc = *cfg;
+    return SPH_OK;
+}
+
+int sph_batch_autotune(sph_batch* b, float dt, int steps, int flags, sph_launch_config* chosen) {
+    if (!b || steps < 1 || !std::isfinite(dt)) return berr(b, SPH_EINVAL, "sph_batch_autotune: bad arguments");
+    cudaSetDevice(b->device);
+    int rc = batch_refresh_num(b);
+    if (rc) return rc;
+    const SphTuneKey key{1, b->nslots, (long long)b->ncells_total, b->exact};
+    sph_launch_config best;
+    if (!(flags & SPH_TUNE_RETIME) && sph_tune_cache_get(key, best)) {
+        b->lc = best;
+        if (chosen) *chosen = best;
+        return SPH_OK;
+    }
+    if (b->nvalid <= 0) return berr(b, SPH_ESTATE, "sph_batch_autotune: no particles");
+    // Save what the steps change: every slot's pos/vel/veleval, the scene
+    // counts and deletions, the counters.
+    const size_t fb = (size_t)b->nslots * 16, sb = (size_t)b->nscenes * 4, ib = sizeof(int) * sphk::kInfoSlots;
+    char* save = nullptr;
+    if (cudaMalloc((void**)&save, 3 * fb + 2 * sb + ib) != cudaSuccess) {
+        cudaGetLastError();
+        return berr(b, SPH_ENOMEM, "sph_batch_autotune: %zu bytes of scratch", 3 * fb + 2 * sb + ib);
+    }
+    void* const fields[6] = {b->pos_u, b->vel_u, b->veleval_u, b->d_num, b->d_del, b->info_nb};
+    const size_t sizes[6] = {fb, fb, fb, sb, sb, ib};
+    auto copy_all = [&](bool to_save) -> cudaError_t {
+        size_t off = 0;
+        for (int f = 0; f < 6; ++f) {
+            cudaError_t e = to_save ? cudaMemcpyAsync(save + off, fields[f], sizes[f], cudaMemcpyDeviceToDevice,
+                                                      b->stream)
+                                    : cudaMemcpyAsync(fields[f], save + off, sizes[f], cudaMemcpyDeviceToDevice,
+                                                      b->stream);
+            if (e != cudaSuccess) return e;
+            off += sizes[f];
+        }
+        return cudaSuccess;
+    };
+    cudaEvent_t ev[5];
+    for (auto& x : ev) x = nullptr;
+    cudaError_t e = cudaSuccess;
+    for (auto& x : ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&x);
+    const sph_launch_config keep = b->lc;
+    double t[3][3] = {{0}};
+    if (e == cudaSuccess) e = copy_all(true);
+    for (int k = 0; k < 3 && e == cudaSuccess && rc == SPH_OK; ++k) {
+        b->lc = sph_tune_candidates[k];
+        if ((e = copy_all(false)) != cudaSuccess) break;
+        if ((rc = batch_enqueue_step(b, dt, nullptr))) break;  // first launches, untimed
+        if ((e = copy_all(false)) != cudaSuccess) break;
+        for (int it = 0; it < steps && e == cudaSuccess && rc == SPH_OK; ++it) {
+            if ((rc = batch_enqueue_step(b, dt, ev))) break;
+            if ((e = cudaEventSynchronize(ev[4])) != cudaSuccess) break;
+            float ms[4];
+            for (int q = 0; q < 4 && e == cudaSuccess; ++q) e = cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]);
+            t[k][0] += ms[2];
+            t[k][1] += ms[3];
+            t[k][2] += ms[0];
+        }
+    }
+    if (e == cudaSuccess) e = copy_all(false);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
+    cudaFree(save);
+    if (rc || e != cudaSuccess) {
+        b->lc = keep;
+        if (rc) return rc;
+        return berr(b, SPH_ECUDA, "sph_batch_autotune: %s", cudaGetErrorString(e));
+    }
+    best = sph_tune_pick(t);
+    b->lc = best;
+    sph_tune_cache_put(key, best);
+    if (chosen) *chosen = best;
     return SPH_OK;
 }
 

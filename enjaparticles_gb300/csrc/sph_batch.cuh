@@ -22,6 +22,15 @@ struct sph_batch {
     std::vector<int> max_num, num;
     std::vector<uint32_t> slot_off, cbase;
     int nslots = 0, nvalid = 0, cell_bits = 0, scene_bits = 0, unit = 1;
+    sph_launch_config lc = {256, 128, 4096, 0};  // launch shapes (sph_batch_autotune)
+    // scheduler of the neighbour passes (SPH_SCHED_GRID / SPH_SCHED_QUEUE) and
+    // the queue's state: [0..3] density, [4..7] force (sph_queue.cuh), its
+    // tile tables, and the test hold of its table publication
+    int sched = 0;
+    unsigned* q_state = nullptr;
+    uint32_t* q_tiles = nullptr;
+    int q_hold = 0;
+    unsigned q_spin = 1u << 22;
     size_t ncells_total = 0;
     uint32_t invalid_key = 0;
     unsigned params_version = 1;
@@ -34,6 +43,7 @@ struct sph_batch {
     float4* pos_xy = nullptr;  // sorted positions as pairs (default arithmetic's density pass)
     float2* pos_z = nullptr;
     float* density = nullptr;
+    uint32_t* nbr = nullptr;   // neighbour counts (density pass) for the force pass
     uint32_t *mask = nullptr, *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
     uint32_t *cell_start = nullptr, *cell_end = nullptr;
     uint16_t* scene_of = nullptr;
@@ -50,7 +60,8 @@ struct sph_batch {
     float4 *keep_f = nullptr, *keep_v = nullptr;
     cudaGraphExec_t graph = nullptr;
     float graph_dt = 0.f;
-    int graph_valid = -1, graph_exact = -1;
+    int graph_valid = -1, graph_exact = -1, graph_sched = -1;
+    sph_launch_config graph_lc = {0, 0, 0, 0};
     sph_batch_adjoint* adj = nullptr;
     std::string err;
 };
@@ -60,7 +71,9 @@ int berr(sph_batch* b, int code, const char* fmt, ...);
 // particles that left its grid) into b->num and b->nvalid.  Blocking.
 int batch_refresh_num(sph_batch* b);
 sphk::ManyScenes batch_scenes(const sph_batch* b);
-int batch_enqueue_step(sph_batch* b, float dt);
+// ev (nullable): 5 events recorded around the cell totals+scan, the density
+// pass and the force pass.
+int batch_enqueue_step(sph_batch* b, float dt, cudaEvent_t* ev = nullptr);
 void sph_batch_adjoint_release(sph_batch* b);
 
 #define BCK(b, call)                                                                                  \

@@ -11,7 +11,8 @@
 //   count    the cell key of each particle (hash.cl, clamped to nb_cells like
 //            k_hash) and an atomic count per cell; the count a particle finds
 //            is its slot in the cell.
-//   totals   the number of particles in each tile of 4096 cells; the first
+//   totals   the number of particles in each tile of 4096 cells (2048 or
+//            8192 when the autotuner picks them); the first
 //            thread also applies the previous step's out-of-grid deletion to
 //            the particle count (count derives the same number on its own).
 //            Grids of more than kDirectTiles tiles then scan the totals in
@@ -46,15 +47,16 @@ namespace sphk {
 
 namespace {
 
-constexpr int kScanThreads = 256;
+// The totals and scan passes take tiles of ST * kScanItems cells, ST threads
+// per block: 2048, 4096 (the default) or 8192 cells, a launch shape the
+// autotuner picks (the results are the same integers).
 constexpr int kScanItems = 16;
-constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 cells per tile
 constexpr int kItems = 4;                               // particles per thread in count and place
 constexpr int kTileScanThreads = 1024;
 
 }  // namespace
 
-int cell_scan_tiles(int cells) { return (cells + kScanTile - 1) / kScanTile; }
+int cell_scan_tiles(int cells, int tile_cells) { return (cells + tile_cells - 1) / tile_cells; }
 
 // ---------------------------------------------------------------------------
 // Count: key and slot of every particle (original order).  A warp takes 4
@@ -118,10 +120,12 @@ __device__ __forceinline__ void load_counts(const uint32_t* __restrict__ count, 
 
 // Totals: block b sums the counts of tile b.  info may be null (batches: no
 // deletion).
-__global__ void __launch_bounds__(kScanThreads) k_cell_totals(const uint32_t* __restrict__ count,
-                                                              uint32_t* __restrict__ tile_total,
-                                                              int* __restrict__ info, uint32_t cells) {
-    __shared__ uint32_t s_warp[kScanThreads / 32];
+template <int ST>
+__global__ void __launch_bounds__(ST) k_cell_totals(const uint32_t* __restrict__ count,
+                                                    uint32_t* __restrict__ tile_total, int* __restrict__ info,
+                                                    uint32_t cells) {
+    constexpr int kScanTile = ST * kScanItems;
+    __shared__ uint32_t s_warp[ST / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (info != nullptr && blockIdx.x == 0 && tid == 0) {  // the step's particle count; the scan sets kOutStart anew
         const int out = info[kOutStart];
@@ -142,7 +146,7 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_totals(const uint32_t* __
     if (tid == 0) {
         uint32_t t = 0;
 #pragma unroll
-        for (int w = 0; w < kScanThreads / 32; ++w) t += s_warp[w];
+        for (int w = 0; w < ST / 32; ++w) t += s_warp[w];
         tile_total[blockIdx.x] = t;
     }
 }
@@ -183,20 +187,21 @@ __global__ void __launch_bounds__(kTileScanThreads) k_cell_tile_scan(uint32_t* _
 // of the totals of tiles 0..b-1, or from tile_total[b] when the totals were
 // scanned already (prescanned).  With info, the start of the last cell (the
 // out-of-grid key) goes to info[kOutStart].
-__global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict__ count,
-                                                            uint32_t* __restrict__ cell_start,
-                                                            uint32_t* __restrict__ cell_end,
-                                                            const uint32_t* __restrict__ tile_total,
-                                                            int* __restrict__ info, uint32_t cells, int prescanned) {
-    __shared__ uint32_t s_warp[kScanThreads / 32];
-    __shared__ uint32_t s_base[kScanThreads / 32];
+template <int ST>
+__global__ void __launch_bounds__(ST) k_cell_scan(uint32_t* __restrict__ count, uint32_t* __restrict__ cell_start,
+                                                  uint32_t* __restrict__ cell_end,
+                                                  const uint32_t* __restrict__ tile_total, int* __restrict__ info,
+                                                  uint32_t cells, int prescanned) {
+    constexpr int kScanTile = ST * kScanItems;
+    __shared__ uint32_t s_warp[ST / 32];
+    __shared__ uint32_t s_base[ST / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tile = blockIdx.x;
     uint32_t before = 0;
     if (prescanned)
         before = tid == 0 ? __ldg(tile_total + tile) : 0u;
     else
-        for (int t = tid; t < tile; t += kScanThreads) before += __ldg(tile_total + t);
+        for (int t = tid; t < tile; t += ST) before += __ldg(tile_total + t);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
     if (lane == 0) s_base[warp] = before;
@@ -221,7 +226,7 @@ __global__ void __launch_bounds__(kScanThreads) k_cell_scan(uint32_t* __restrict
     __syncthreads();
     uint32_t run = x - sum;
 #pragma unroll
-    for (int w = 0; w < kScanThreads / 32; ++w) run += (w < warp ? s_warp[w] : 0u) + s_base[w];
+    for (int w = 0; w < ST / 32; ++w) run += (w < warp ? s_warp[w] : 0u) + s_base[w];
     uint32_t st[kScanItems];
     const uint32_t last = cells - 1;  // the out-of-grid key
 #pragma unroll
@@ -338,16 +343,28 @@ void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of,
     k_cell_count<<<blocks, 256, 0, st>>>(pos_u, key_of, slot_of, count, info, p);
 }
 
-void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, uint32_t cells, cudaStream_t st) {
-    k_cell_totals<<<cell_scan_tiles((int)cells), kScanThreads, 0, st>>>(count, tile_total, info, cells);
+void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, uint32_t cells, int tile_cells,
+                        cudaStream_t st) {
+    const int tiles = cell_scan_tiles((int)cells, tile_cells);
+    if (tile_cells == 2048)
+        k_cell_totals<128><<<tiles, 128, 0, st>>>(count, tile_total, info, cells);
+    else if (tile_cells == 8192)
+        k_cell_totals<512><<<tiles, 512, 0, st>>>(count, tile_total, info, cells);
+    else
+        k_cell_totals<256><<<tiles, 256, 0, st>>>(count, tile_total, info, cells);
 }
 
 void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
-                      uint32_t cells, cudaStream_t st) {
-    const int tiles = cell_scan_tiles((int)cells);
+                      uint32_t cells, int tile_cells, cudaStream_t st) {
+    const int tiles = cell_scan_tiles((int)cells, tile_cells);
     const int prescanned = tiles > kDirectTiles;
     if (prescanned) k_cell_tile_scan<<<1, kTileScanThreads, 0, st>>>(tile_total, tiles);
-    k_cell_scan<<<tiles, kScanThreads, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
+    if (tile_cells == 2048)
+        k_cell_scan<128><<<tiles, 128, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
+    else if (tile_cells == 8192)
+        k_cell_scan<512><<<tiles, 512, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
+    else
+        k_cell_scan<256><<<tiles, 256, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
 }
 
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,

@@ -33,6 +33,8 @@ struct sph_ctx {
     int num_hint = 0;  // host upper bound of the particle count (grid sizing)
     int passes = 1;
     int exact = 0;
+    // launch shapes (sph_set_launch_config / sph_autotune)
+    sph_launch_config lc = {256, 128, 4096, 0};
     // device state
     float4 *pos_u = nullptr, *vel_u = nullptr, *veleval_u = nullptr;
     float4 *pos_s = nullptr, *vel_s = nullptr, *veleval_s = nullptr, *force_s = nullptr, *xsph_s = nullptr;

@@ -11,9 +11,9 @@
 // the separately rounded result, even with contraction disabled, which would
 // change |r|^2 and with it the neighbour sets.)
 //
-// nbr (neighbour counts) is optional: the fused step leaves it out.  The
-// fused step's out-of-grid bookkeeping is its own kernel (sph_integrate.cu),
-// so this pass reads no velocity.  veleval_s is optional too: without it the
+// nbr gets every particle's neighbour count (itself included): the force
+// pass's loop length.  The fused step's out-of-grid bookkeeping is its own
+// kernel (sph_integrate.cu), so this pass reads no velocity.  veleval_s is optional too: without it the
 // pass writes only the 1/rho lane of rec_vi, and the fused step's velocity
 // kernel fills the veleval lanes beside it.
 //
@@ -21,21 +21,41 @@
 // its first kMaskBits candidates (in walk order) are neighbours (self
 // excluded) as a bitmask, and the 32-byte record (position, rho),
 // (veleval, 1/rho) the force pass reads for every neighbour.
+#include "sph_queue.cuh"
 #include "sph_walk.cuh"
 
 namespace sphk {
 
-template <bool Exact, bool Unit, bool WantCount, class Scenes>
-__global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_s, const float4* __restrict__ veleval_s,
-                                                 float* __restrict__ density, float4* __restrict__ rec_pd,
-                                                 float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
-                                                 uint32_t* __restrict__ mask, const size_t mstride,
-                                                 const uint32_t* __restrict__ cs0, const uint32_t* __restrict__ ce0,
-                                                 const int* __restrict__ info, const Scenes R) {
-    int n_old, out;
-    const int n = effective_num(info, n_old, out);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// The arrays of the density pass (pxy / pz: the default arithmetic's pairs).
+struct DensityArgs {
+    const float4* pos_s;
+    const float4* pxy;
+    const float2* pz;
+    const float4* veleval_s;
+    float* density;
+    float4* rec_pd;
+    float4* rec_vi;
+    uint32_t* nbr;
+    uint32_t* mask;
+    size_t mstride;
+    const uint32_t* cs0;
+    const uint32_t* ce0;
+};
+
+// Sorted particle i, scalar candidates (every operation rounded on its own
+// in exact arithmetic).
+template <bool Exact, bool Unit, class Scenes>
+__device__ __forceinline__ void density_one(const int i, const DensityArgs& A, const Scenes& R) {
+    const float4* __restrict__ pos_s = A.pos_s;
+    const float4* __restrict__ veleval_s = A.veleval_s;
+    float* __restrict__ density = A.density;
+    float4* __restrict__ rec_pd = A.rec_pd;
+    float4* __restrict__ rec_vi = A.rec_vi;
+    uint32_t* __restrict__ nbr = A.nbr;
+    uint32_t* __restrict__ mask = A.mask;
+    const size_t mstride = A.mstride;
+    const uint32_t* __restrict__ cs0 = A.cs0;
+    const uint32_t* __restrict__ ce0 = A.ce0;
     const StepParams& P = R.params(i);
     const uint32_t* cs = cs0 + R.cell_base(i);
     const uint32_t* ce = ce0 + R.cell_base(i);
@@ -48,7 +68,7 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
             rec_vi[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         else
             reinterpret_cast<float*>(rec_vi + i)[3] = 0.f;
-        if (WantCount) nbr[i] = 0;
+        nbr[i] = 0;
         return;
     }
     const float rc2 = P.rcut2, h2 = P.h2;
@@ -80,7 +100,7 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
                     const float hr2 = __fsub_rn(h2, r2);
                     acc = Exact ? __fadd_rn(acc, __fmul_rn(__fmul_rn(hr2, hr2), hr2))
                                 : __fmaf_rn(__fmul_rn(hr2, hr2), hr2, acc);
-                    if (WantCount) ++cnt;
+                    ++cnt;
                     cur |= bit;
                 }
             }
@@ -111,7 +131,15 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
     } else {
         reinterpret_cast<float*>(rec_vi + i)[3] = __frcp_rn(rho);
     }
-    if (WantCount) nbr[i] = cnt;
+    nbr[i] = cnt;
+}
+
+template <int T, bool Exact, bool Unit, class Scenes>
+__global__ void __launch_bounds__(T) k_density(const DensityArgs A, const int* __restrict__ info, const Scenes R) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) density_one<Exact, Unit>(i, A, R);
 }
 
 // ---------------------------------------------------------------------------
@@ -131,20 +159,20 @@ __global__ void __launch_bounds__(256) k_density(const float4* __restrict__ pos_
 // appended to the word stream.
 constexpr int kPairSegment = 16;  // pairs per mask segment (32 bits)
 
-template <bool WantCount, class Scenes>
-__global__ void __launch_bounds__(256) k_density_pairs(const float4* __restrict__ pos_s,
-                                                       const float4* __restrict__ pxy, const float2* __restrict__ pz,
-                                                       const float4* __restrict__ veleval_s,
-                                                       float* __restrict__ density, float4* __restrict__ rec_pd,
-                                                       float4* __restrict__ rec_vi, uint32_t* __restrict__ nbr,
-                                                       uint32_t* __restrict__ mask, const size_t mstride,
-                                                       const uint32_t* __restrict__ cs0,
-                                                       const uint32_t* __restrict__ ce0, const int* __restrict__ info,
-                                                       const Scenes R) {
-    int n_old, out;
-    const int n = effective_num(info, n_old, out);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+template <class Scenes>
+__device__ __forceinline__ void density_pairs_one(const int i, const DensityArgs& A, const Scenes& R) {
+    const float4* __restrict__ pos_s = A.pos_s;
+    const float4* __restrict__ pxy = A.pxy;
+    const float2* __restrict__ pz = A.pz;
+    const float4* __restrict__ veleval_s = A.veleval_s;
+    float* __restrict__ density = A.density;
+    float4* __restrict__ rec_pd = A.rec_pd;
+    float4* __restrict__ rec_vi = A.rec_vi;
+    uint32_t* __restrict__ nbr = A.nbr;
+    uint32_t* __restrict__ mask = A.mask;
+    const size_t mstride = A.mstride;
+    const uint32_t* __restrict__ cs0 = A.cs0;
+    const uint32_t* __restrict__ ce0 = A.ce0;
     const StepParams& P = R.params(i);
     const uint32_t* cs = cs0 + R.cell_base(i);
     const uint32_t* ce = ce0 + R.cell_base(i);
@@ -156,7 +184,7 @@ __global__ void __launch_bounds__(256) k_density_pairs(const float4* __restrict_
             rec_vi[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         else
             reinterpret_cast<float*>(rec_vi + i)[3] = 0.f;
-        if (WantCount) nbr[i] = 0;
+        nbr[i] = 0;
         return;
     }
     const float rc2 = P.rcut2;
@@ -210,7 +238,7 @@ __global__ void __launch_bounds__(256) k_density_pairs(const float4* __restrict_
             for (; k < kin; ++k) pair_of(k, true, true, seg, 1u << (2u * (k - ks)));
             // the run's last pair (its element 2k+1 may be re)
             if (k < ke) pair_of(k, true, 2u * k + 1u < re, seg, 1u << (2u * (k - ks)));
-            if (WantCount) cnt += (uint32_t)__popc(seg);
+            cnt += (uint32_t)__popc(seg);
             const uint32_t e0 = 2u * ks;
             if ((uint32_t)i - e0 < 32u) seg &= ~(1u << ((uint32_t)i - e0));  // not itself
             const uint32_t lo = rs > e0 ? rs - e0 : 0u;
@@ -233,7 +261,16 @@ __global__ void __launch_bounds__(256) k_density_pairs(const float4* __restrict_
     } else {
         reinterpret_cast<float*>(rec_vi + i)[3] = __frcp_rn(rho);
     }
-    if (WantCount) nbr[i] = cnt;
+    nbr[i] = cnt;
+}
+
+template <int T, class Scenes>
+__global__ void __launch_bounds__(T) k_density_pairs(const DensityArgs A, const int* __restrict__ info,
+                                                       const Scenes R) {
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) density_pairs_one(i, A, R);
 }
 
 // Sorted positions as pairs (see k_density_pairs), for the passes whose
@@ -249,62 +286,125 @@ __global__ void k_pack_pairs(const float4* __restrict__ pos_s, float4* __restric
     pz[k] = make_float2(a.z, b.z);
 }
 
-template <class Scenes>
-void launch_density_t(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
-                      uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
-                      const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
-                      int grid_items, float4* pxy, float2* pz, bool pack, cudaStream_t st) {
-    const int threads = 256;
-    int blocks = (grid_items + threads - 1) / threads;
+template <int T, class Scenes>
+void launch_density_tt(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
+                       uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
+                       const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
+                       int grid_items, float4* pxy, float2* pz, bool pack, cudaStream_t st) {
+    int blocks = (grid_items + T - 1) / T;
     if (blocks < 1) blocks = 1;
+    const DensityArgs A{pos_s, pxy, pz, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
+                        cell_end};
     if (pxy != nullptr && pz != nullptr && unit && !exact) {
         if (pack) {
             const int pb = ((grid_items + 1) / 2 + 255) / 256;
             k_pack_pairs<<<pb < 1 ? 1 : pb, 256, 0, st>>>(pos_s, pxy, pz, info);
         }
-        if (nbr)
-            k_density_pairs<true, Scenes><<<blocks, threads, 0, st>>>(pos_s, pxy, pz, veleval_s, density, rec_pd,
-                                                                      rec_vi, nbr, mask, mask_stride, cell_start,
-                                                                      cell_end, info, R);
-        else
-            k_density_pairs<false, Scenes><<<blocks, threads, 0, st>>>(pos_s, pxy, pz, veleval_s, density, rec_pd,
-                                                                       rec_vi, nbr, mask, mask_stride, cell_start,
-                                                                       cell_end, info, R);
+        k_density_pairs<T, Scenes><<<blocks, T, 0, st>>>(A, info, R);
         return;
     }
-#define SPH_DENSITY_LAUNCH(E, U, W)                                                                               \
-    k_density<E, U, W, Scenes><<<blocks, threads, 0, st>>>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, \
-                                                           mask_stride, cell_start, cell_end, info, R)
-#define SPH_DENSITY_LAUNCH_E(E)                                                                \
-    if (unit) {                                                                                \
-        if (nbr) SPH_DENSITY_LAUNCH(E, true, true); else SPH_DENSITY_LAUNCH(E, true, false);   \
-    } else {                                                                                   \
-        if (nbr) SPH_DENSITY_LAUNCH(E, false, true); else SPH_DENSITY_LAUNCH(E, false, false); \
-    }
+#define SPH_DENSITY_LAUNCH(E, U) k_density<T, E, U, Scenes><<<blocks, T, 0, st>>>(A, info, R)
     if (exact) {
-        SPH_DENSITY_LAUNCH_E(true)
+        if (unit) SPH_DENSITY_LAUNCH(true, true); else SPH_DENSITY_LAUNCH(true, false);
     } else {
-        SPH_DENSITY_LAUNCH_E(false)
+        if (unit) SPH_DENSITY_LAUNCH(false, true); else SPH_DENSITY_LAUNCH(false, false);
     }
-#undef SPH_DENSITY_LAUNCH_E
 #undef SPH_DENSITY_LAUNCH
+}
+
+// The density pass with `threads` threads per block (128, 256 or 512: the
+// same results bit for bit, a launch shape the autotuner picks).
+template <class Scenes>
+void launch_density_t(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
+                      uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
+                      const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
+                      int grid_items, float4* pxy, float2* pz, bool pack, int threads, cudaStream_t st) {
+    switch (threads) {
+        case 128:
+            launch_density_tt<128>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st);
+            break;
+        case 512:
+            launch_density_tt<512>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st);
+            break;
+        default:
+            launch_density_tt<256>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st);
+    }
+}
+
+// The batch's density pass under the queue scheduler (sph_queue.cuh): the
+// same per-particle work as k_density_pairs / k_density, scene by scene.
+template <int T, bool Pairs, bool Exact, bool Unit>
+__global__ void __launch_bounds__(T) k_density_queue(const DensityArgs A, const BatchQueue Q) {
+    __shared__ QueueShared<T> S;
+    if (!queue_start<T>(Q, S)) return;
+    while (queue_next<T>(Q, S)) {
+        const TileScene R = queue_scene<T>(Q, S);
+        if (threadIdx.x < S.count) {
+            const int i = (int)(S.first + threadIdx.x);
+            if constexpr (Pairs)
+                density_pairs_one(i, A, R);
+            else
+                density_one<Exact, Unit>(i, A, R);
+        }
+    }
+}
+
+template <int T, bool Pairs, bool Exact, bool Unit>
+void density_queue_launch(const DensityArgs& A, const BatchQueue& Q, cudaStream_t st) {
+    static int per_sm = -1, sms = 0;  // resident blocks per SM and SMs of the current device
+    if (per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_density_queue<T, Pairs, Exact, Unit>, T, 0);
+        if (per_sm < 1) per_sm = 1;
+    }
+    k_density_queue<T, Pairs, Exact, Unit><<<per_sm * sms, T, 0, st>>>(A, Q);
+}
+
+template <int T>
+void density_queue_t(const DensityArgs& A, const BatchQueue& Q, bool unit, bool exact, cudaStream_t st) {
+    if (unit && !exact && A.pxy != nullptr)
+        density_queue_launch<T, true, false, true>(A, Q, st);
+    else if (exact)
+        unit ? density_queue_launch<T, false, true, true>(A, Q, st) : density_queue_launch<T, false, true, false>(A, Q, st);
+    else
+        unit ? density_queue_launch<T, false, false, true>(A, Q, st)
+             : density_queue_launch<T, false, false, false>(A, Q, st);
+}
+
+void launch_density_queue(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
+                          float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
+                          const uint32_t* cell_start, const uint32_t* cell_end, float4* pxy, float2* pz,
+                          const BatchQueue& Q, bool unit, int exact, int threads, cudaStream_t st) {
+    const DensityArgs A{pos_s, pxy, pz, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
+                        cell_end};
+    if (threads == 128)
+        density_queue_t<128>(A, Q, unit, exact != 0, st);
+    else if (threads == 512)
+        density_queue_t<512>(A, Q, unit, exact != 0, st);
+    else
+        density_queue_t<256>(A, Q, unit, exact != 0, st);
 }
 
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
-                    float2* pz, bool pack, cudaStream_t st) {
+                    float2* pz, bool pack, int threads, cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, pxy, pz, pack, st);
+                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, pxy, pz, pack, threads, st);
 }
 
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                           const ManyScenes& scenes, bool unit, int exact, int grid_items, float4* pxy, float2* pz,
-                          bool pack, cudaStream_t st) {
+                          bool pack, int threads, cudaStream_t st) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     scenes, unit, exact != 0, grid_items, pxy, pz, pack, st);
+                     scenes, unit, exact != 0, grid_items, pxy, pz, pack, threads, st);
 }
 
 }  // namespace sphk

@@ -90,6 +90,7 @@ constexpr int kMaxTriangles = 1 << 20;
 //   particles, re-indexed in sorted order, and the removed ones go to the
 //   slots after them.
 struct OneScene {
+    static constexpr bool kBatch = false;
     StepParams P;
     __device__ __forceinline__ const StepParams& params(int) const { return P; }
     __device__ __forceinline__ uint32_t cell_base(int) const { return 0u; }
@@ -97,6 +98,7 @@ struct OneScene {
     __device__ __forceinline__ uint32_t scene(int) const { return 0u; }
 };
 struct ManyScenes {
+    static constexpr bool kBatch = true;
     const StepParams* table;
     const uint32_t* cbase;
     const uint32_t* keys;
@@ -165,16 +167,20 @@ void launch_radix_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
 int radix_tiles(int n);
 // Counting sort on the cell key (sph_cellsort.cu): count, totals, scan,
 // place, then permute (which reads veleval_u/vel_u: after any upload join).
-int cell_scan_tiles(int cells);
+int cell_scan_tiles(int cells, int tile_cells);
 void launch_cell_count(const float4* pos_u, uint32_t* key_of, uint32_t* slot_of, uint32_t* count, const int* info,
                        const StepParams& p, int grid_items, cudaStream_t st);
 // totals and scan over cells [0, cells); info null for a batch.  Above
 // kDirectTiles tiles of 4096 cells the scan first scans the tile totals in
 // one block (one more launch) instead of summing them in every block.
 constexpr int kDirectTiles = 2048;
-void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, uint32_t cells, cudaStream_t st);
+// tile_cells: cells per scan tile (2048, 4096 or 8192); tile_total holds
+// cell_scan_tiles(cells, 2048) words, enough for any of them.
+constexpr int kScanTileMin = 2048;
+void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, uint32_t cells, int tile_cells,
+                        cudaStream_t st);
 void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
-                      uint32_t cells, cudaStream_t st);
+                      uint32_t cells, int tile_cells, cudaStream_t st);
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
                        const int* info, int grid_items, cudaStream_t st);
 // pxy / pz (nullable): the sorted positions also as pairs (launch_density).
@@ -193,7 +199,7 @@ void launch_cells_permute(const uint32_t* keys, const uint32_t* idx, uint32_t* c
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
-                    float2* pz, bool pack, cudaStream_t st);
+                    float2* pz, bool pack, int threads, cudaStream_t st);
 // The fused step's velocity pass, beside density and before force (the first
 // passes that need the uploaded velocities): the veleval lanes of rec_vi in
 // sorted order, and the out-of-grid bookkeeping (kept velocities into vel_s
@@ -204,22 +210,36 @@ void launch_step_velocities(const float4* pos_s, const uint32_t* idx, const floa
                             int grid_items, cudaStream_t st);
 // keep_f / keep_v (fused only, nullable): per sorted particle, the SPH force
 // before the walls and the velocity the step integrates.
+// nbr: the density pass's neighbour counts (itself included), which give the
+// force pass the length of its neighbour loop.
 void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
-                  size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                  size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                   float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
                   float4* veleval_u, float4* keep_f, float4* keep_v, const StepParams& p, float dt, int fused,
-                  int exact, int grid_items, cudaStream_t st);
+                  int exact, int grid_items, int threads, cudaStream_t st);
 // Batch forms of the neighbour passes (fused force only).
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                           const ManyScenes& scenes, bool unit, int exact, int grid_items, float4* pxy, float2* pz,
-                          bool pack, cudaStream_t st);
+                          bool pack, int threads, cudaStream_t st);
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
-                        size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                        size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                         uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,
                         float4* keep_v, const ManyScenes& scenes, bool unit, float dt, int exact, int grid_items,
-                        cudaStream_t st);
+                        int threads, cudaStream_t st);
+// The batch's neighbour passes under the queue scheduler (sph_queue.cuh):
+// persistent blocks taking (scene, tile) items from Q.
+struct BatchQueue;
+void launch_density_queue(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
+                          float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
+                          const uint32_t* cell_start, const uint32_t* cell_end, float4* pxy, float2* pz,
+                          const BatchQueue& Q, bool unit, int exact, int threads, cudaStream_t st);
+void launch_force_queue(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                        size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start,
+                        const uint32_t* cell_end, uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u,
+                        float4* keep_f, float4* keep_v, const BatchQueue& Q, bool unit, float dt, int exact,
+                        int threads, cudaStream_t st);
 void launch_collision(const float4* pos_s, const float4* vel_s, float4* force_s, const int* info,
                       const StepParams& p, int grid_items, cudaStream_t st);
 void launch_leapfrog(const float4* pos_s, const float4* vel_s, const float4* force_s, const float4* xsph_s,
@@ -248,6 +268,25 @@ void launch_permute_only(const uint32_t* idx, const float4* pos_u, const float4*
 
 // Host helpers shared by the single-system and batch APIs (sph_api.cu).
 #include <string>
+#include <tuple>
+
+// The autotuner's candidate launch shapes, its per-process results keyed by
+// (kind: 0 one system, 1 batch; particle slots; cells; arithmetic mode), and
+// its choice per knob from the candidates' times t[k] = (density, force,
+// cell totals + scan).
+struct SphTuneKey {
+    int kind;
+    long long slots, cells;
+    int exact;
+    bool operator<(const SphTuneKey& o) const {
+        return std::tie(kind, slots, cells, exact) < std::tie(o.kind, o.slots, o.cells, o.exact);
+    }
+};
+extern const sph_launch_config sph_tune_candidates[3];
+bool sph_launch_config_valid(const sph_launch_config& g);
+bool sph_tune_cache_get(const SphTuneKey& k, sph_launch_config& out);
+void sph_tune_cache_put(const SphTuneKey& k, const sph_launch_config& v);
+sph_launch_config sph_tune_pick(const double t[3][3]);
 int sph_make_step_params(const SPHParams& s, const GridParams& gp, const GridParams& gps, sphk::StepParams& P,
                          std::string& err);
 GridParams sph_scaled_grid(const GridParams& g, float sc);

@@ -5,6 +5,7 @@
 // it; the exact variant spells every operation with a rounding intrinsic.
 #include <type_traits>
 
+#include "sph_queue.cuh"
 #include "sph_walk.cuh"
 
 namespace sphk {
@@ -23,6 +24,8 @@ namespace sphk {
 // lists.  Neighbour data is the 32-byte record (x, y, z, rho),
 // (veleval.xyz, 1/rho) written by the density pass and the velocity pass,
 // read through L1.
+// Threads per block: 64, 128 (the default) or 256, a launch shape the
+// autotuner picks; every shape gives the same results bit for bit.
 constexpr int kForceThreads = 128;
 
 struct ForceSums {
@@ -58,9 +61,12 @@ __device__ __forceinline__ void force_pair(ForceSums& a, const float4& pi, const
         a.fy = __fadd_rn(a.fy, __fmul_rn(dy, kern));
         a.fz = __fadd_rn(a.fz, __fmul_rn(dz, kern));
     } else {
-        // r2 == 0 (coincident particles) gives NaN here and is caught by the
-        // same clamp as rlen < EPSILON.
-        const float inv_r = rsqrtf(r2);
+        // 1/|r| and 1/(rho_i + rho_j) by the approximate reciprocal (square
+        // root) instructions with denormals flushed (a few ulp, inside the
+        // default mode's tolerance).  r2 == 0 (coincident particles) gives
+        // NaN in rlen and is caught by the same clamp as rlen < EPSILON.
+        float inv_r;
+        asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(inv_r) : "f"(r2));
         float rlen = r2 * inv_r;
         float irl = inv_r;
         if (!(rlen >= P.eps)) {
@@ -73,9 +79,10 @@ __device__ __forceinline__ void force_pair(ForceSums& a, const float4& pi, const
         a.vx = fmaf(dvx, vh, a.vx);
         a.vy = fmaf(dvy, vh, a.vy);
         a.vz = fmaf(dvz, vh, a.vz);
-        // the fast division (a few ulp): the XSPH weight is a smoothing term,
-        // far inside the default mode's 1e-5 tolerance
-        const float wx = __fdividef(w6, dsum);
+        // the XSPH weight is a smoothing term, far inside the tolerance
+        float rd;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rd) : "f"(dsum));
+        const float wx = w6 * rd;
         a.xx = fmaf(wx, dvx, a.xx);
         a.xy = fmaf(wx, dvy, a.xy);
         a.xz = fmaf(wx, dvz, a.xz);
@@ -85,32 +92,65 @@ __device__ __forceinline__ void force_pair(ForceSums& a, const float4& pi, const
     }
 }
 
-template <bool Fused, bool Exact, bool Unit, class Scenes>
-__global__ void __launch_bounds__(kForceThreads) k_force(
-    const float4* __restrict__ pos_s, const float4* __restrict__ rec_pd, const float4* __restrict__ rec_vi,
-    const uint32_t* __restrict__ mask, const size_t mstride, const uint32_t* __restrict__ cs0,
-    const uint32_t* __restrict__ ce0, const int* __restrict__ info, float4* __restrict__ force_s,
-    float4* __restrict__ xsph_s, uint32_t* __restrict__ idx, const float4* __restrict__ vel_s,
-    float4* __restrict__ pos_u, float4* __restrict__ vel_u, float4* __restrict__ veleval_u,
-    float4* __restrict__ keep_f, float4* __restrict__ keep_v, const Scenes R, const float dt) {
-    // Row table of each thread: walk-order offset of the run's first
-    // candidate, and sorted index minus walk-order position over the run
-    // (j = p + delta, modulo 2^32); rows without candidates are left out.
-    __shared__ uint32_t s_delta[9][kForceThreads];
-    __shared__ uint32_t s_off[10][kForceThreads];
-    int n_old, out;
-    const int n = effective_num(info, n_old, out);
+// The arrays of the force pass (force_s, xsph_s: the staged pass's outputs;
+// the rest of the second half: the fused integration's).
+struct ForceArgs {
+    const float4* pos_s;
+    const float4* rec_pd;
+    const float4* rec_vi;
+    const uint32_t* mask;
+    size_t mstride;
+    const uint32_t* nbr;
+    const uint32_t* cs0;
+    const uint32_t* ce0;
+    float4* force_s;
+    float4* xsph_s;
+    uint32_t* idx;
+    const float4* vel_s;
+    float4* pos_u;
+    float4* vel_u;
+    float4* veleval_u;
+    float4* keep_f;
+    float4* keep_v;
+    float dt;
+};
+
+// Sorted particle i (in_range: i below the step's particle count) with the
+// thread's column of the row tables: walk-order offset of each run's first
+// candidate, and sorted index minus walk-order position over the run
+// (j = p + delta, modulo 2^32); rows without candidates are left out.  Every
+// lane of the warp calls it (the neighbour loop is warp-wide).
+template <int T, bool Fused, bool Exact, bool Unit, class Scenes>
+__device__ __forceinline__ void force_one(const int i, const bool in_range, const int out, const ForceArgs& G,
+                                          const Scenes& R, uint32_t (*s_delta)[T], uint32_t (*s_off)[T]) {
+    const float4* __restrict__ pos_s = G.pos_s;
+    const float4* __restrict__ rec_pd = G.rec_pd;
+    const float4* __restrict__ rec_vi = G.rec_vi;
+    const uint32_t* __restrict__ mask = G.mask;
+    const size_t mstride = G.mstride;
+    const uint32_t* __restrict__ nbr = G.nbr;
+    const uint32_t* __restrict__ cs0 = G.cs0;
+    const uint32_t* __restrict__ ce0 = G.ce0;
+    float4* __restrict__ force_s = G.force_s;
+    float4* __restrict__ xsph_s = G.xsph_s;
+    uint32_t* __restrict__ idx = G.idx;
+    const float4* __restrict__ vel_s = G.vel_s;
+    float4* __restrict__ pos_u = G.pos_u;
+    float4* __restrict__ vel_u = G.vel_u;
+    float4* __restrict__ veleval_u = G.veleval_u;
+    float4* __restrict__ keep_f = G.keep_f;
+    float4* __restrict__ keep_v = G.keep_v;
+    const float dt = G.dt;
     const int t = threadIdx.x;
-    const int i = blockIdx.x * kForceThreads + t;
-    const bool live = i < n && !R.frozen(i);
-    if constexpr (std::is_same<Scenes, ManyScenes>::value) {
+    const bool live = in_range && !R.frozen(i);
+    if constexpr (Scenes::kBatch) {
         // A batch particle outside its scene's grid: removed from the scene
         // (SPH.cpp:220-250), stored after the scene's kept particles (in
         // sorted order, as a lone system's deleted list); the first one sets
         // the scene's new count.  The scene's kept particles read their
         // velocities from vel_s and are re-indexed below, so no slot written
         // here is read by this pass.
-        if (Fused && i < n && !live) {
+        if (Fused && in_range && !live) {
             const uint32_t sc = R.scene(i), os = R.out_start(sc), kept = os - __ldg(R.seg + sc);
             const uint32_t j = (uint32_t)i - os, dst = __ldg(R.slot_off + sc) + kept + j;
             pos_u[dst] = __ldg(pos_s + i);
@@ -163,12 +203,11 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     uint32_t w = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
     // the next mask word, in flight while this one's neighbours are processed
     uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
-    uint32_t q = (uint32_t)kMaskBits;  // next candidate past the bitmask to test
     int r = 0;
     // One scene: row r's end and index offset in registers, reloaded when the
     // cursor changes row.  Batches read them from shared memory: with the
     // scene lookups the registers would spill (measured slower).
-    constexpr bool kRegCursor = std::is_same<Scenes, OneScene>::value;
+    constexpr bool kRegCursor = !Scenes::kBatch;
     uint32_t next_off = 0, delta = 0;
     if constexpr (kRegCursor) {
         next_off = s_off[1][t];
@@ -188,38 +227,67 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
             return p + s_delta[r][t];
         }
     };
-    for (;;) {
-        // next neighbour of this lane, as its walk-order position p
-        bool have = false;
-        uint32_t p = 0;
-        while (m == 0 && (w + 1) * 32u < mbits) {
+    // the lane's next neighbour from the bitmask (one is left)
+    auto next_bit = [&]() -> uint32_t {
+        while (m == 0) {
             ++w;
             m = m_next;
             m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
         }
-        if (m != 0) {
-            p = w * 32u + (uint32_t)(__ffs(m) - 1);
-            m &= m - 1u;
-            have = true;
-        } else {
-            while (q < M) {
-                const uint32_t pp = q++;
-                const uint32_t j = index_of(pp);
-                const float4 pj = __ldg(rec_pd + j);
-                const float r2 = dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
-                // The self term is multiplied by iej = 0 in the reference
-                // (force.cl:67,113,131,137): it adds a signed zero, so it is skipped.
-                if (r2 <= rc2 && j != (uint32_t)i) {
-                    p = pp;
-                    have = true;
-                    break;
-                }
+        const uint32_t p = w * 32u + (uint32_t)(__ffs(m) - 1);
+        m &= m - 1u;
+        return p;
+    };
+    if (!__any_sync(wmask, M > (uint32_t)kMaskBits)) {
+        // Every lane's candidates fit the bitmask: the density pass counted
+        // the lane's neighbours (itself included), so the warp runs a loop of
+        // known length, each lane taking its next set bit while it has one.
+        const uint32_t cnt = M > 0 ? __ldg(nbr + i) - 1u : 0u;
+        const uint32_t kmax = __reduce_max_sync(wmask, cnt);
+        for (uint32_t k = 0; k < kmax; ++k) {
+            if (k < cnt) {
+                const uint32_t j = index_of(next_bit());
+                force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
             }
         }
-        if (!__any_sync(wmask, have)) break;
-        if (have) {
-            const uint32_t j = index_of(p);
-            force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
+    } else {
+        // Some lane has candidates past the bitmask (crowded cells): the
+        // general loop, which also tests those.
+        uint32_t q = (uint32_t)kMaskBits;  // next candidate past the bitmask to test
+        for (;;) {
+            // next neighbour of this lane, as its walk-order position p
+            bool have = false;
+            uint32_t p = 0;
+            while (m == 0 && (w + 1) * 32u < mbits) {
+                ++w;
+                m = m_next;
+                m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
+            }
+            if (m != 0) {
+                p = w * 32u + (uint32_t)(__ffs(m) - 1);
+                m &= m - 1u;
+                have = true;
+            } else {
+                while (q < M) {
+                    const uint32_t pp = q++;
+                    const uint32_t j = index_of(pp);
+                    const float4 pj = __ldg(rec_pd + j);
+                    const float r2 =
+                        dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
+                    // The self term is multiplied by iej = 0 in the reference
+                    // (force.cl:67,113,131,137): it adds a signed zero, so it is skipped.
+                    if (r2 <= rc2 && j != (uint32_t)i) {
+                        p = pp;
+                        have = true;
+                        break;
+                    }
+                }
+            }
+            if (!__any_sync(wmask, have)) break;
+            if (have) {
+                const uint32_t j = index_of(p);
+                force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
+            }
         }
     }
 
@@ -247,7 +315,7 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     uint32_t orig;
     float4 v;
     bool reindex = out >= 0;
-    if constexpr (std::is_same<Scenes, ManyScenes>::value) {
+    if constexpr (Scenes::kBatch) {
         // a scene that deletes keeps its particles in sorted order
         const uint32_t sc = R.scene(i);
         if (R.out_start(sc) != kEmpty) {
@@ -287,26 +355,34 @@ __global__ void __launch_bounds__(kForceThreads) k_force(
     pos_u[orig] = po;
 }
 
-template <class Scenes>
-void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
-                    size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
-                    float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
-                    float4* veleval_u, float4* keep_f, float4* keep_v, const Scenes& R, bool unit, float dt, int fused,
-                    int exact, int grid_items, cudaStream_t st) {
-    int blocks = (grid_items + kForceThreads - 1) / kForceThreads;
+template <int T, bool Fused, bool Exact, bool Unit, class Scenes>
+__global__ void __launch_bounds__(T) k_force(const ForceArgs A, const int* __restrict__ info, const Scenes R) {
+    __shared__ uint32_t s_delta[9][T];
+    __shared__ uint32_t s_off[10][T];
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int i = blockIdx.x * T + threadIdx.x;
+    force_one<T, Fused, Exact, Unit>(i, i < n, out, A, R, s_delta, s_off);
+}
+
+template <int T, class Scenes>
+void launch_force_tt(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                     size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end,
+                     const int* info, float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s,
+                     float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f, float4* keep_v, const Scenes& R,
+                     bool unit, float dt, int fused, int exact, int grid_items, cudaStream_t st) {
+    int blocks = (grid_items + T - 1) / T;
     if (blocks < 1) blocks = 1;
-#define SPH_FORCE_LAUNCH(F, E, U)                                                                                   \
-    k_force<F, E, U, Scenes><<<blocks, kForceThreads, 0, st>>>(pos_s, rec_pd, rec_vi, mask, mask_stride,           \
-                                                               cell_start, cell_end, info, force_s, xsph_s, idx,  \
-                                                               vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, \
-                                                               R, dt)
+    const ForceArgs A{pos_s, rec_pd,  rec_vi, mask,      mask_stride, nbr,    cell_start, cell_end, force_s,
+                      xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, dt};
+#define SPH_FORCE_LAUNCH(F, E, U) k_force<T, F, E, U, Scenes><<<blocks, T, 0, st>>>(A, info, R)
     if (fused) {
         if (exact) {
             if (unit) SPH_FORCE_LAUNCH(true, true, true); else SPH_FORCE_LAUNCH(true, true, false);
         } else {
             if (unit) SPH_FORCE_LAUNCH(true, false, true); else SPH_FORCE_LAUNCH(true, false, false);
         }
-    } else {
+    } else if constexpr (T == kForceThreads) {
         if (exact) {
             if (unit) SPH_FORCE_LAUNCH(false, true, true); else SPH_FORCE_LAUNCH(false, true, false);
         } else {
@@ -316,23 +392,95 @@ void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec
 #undef SPH_FORCE_LAUNCH
 }
 
+template <class Scenes>
+void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                    size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end,
+                    const int* info, float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s,
+                    float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f, float4* keep_v, const Scenes& R,
+                    bool unit, float dt, int fused, int exact, int grid_items, int threads, cudaStream_t st) {
+    // the staged (unfused) pass keeps the default shape
+    if (fused && threads == 64)
+        launch_force_tt<64>(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, force_s,
+                            xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, R, unit, dt, fused, exact,
+                            grid_items, st);
+    else if (fused && threads == 256)
+        launch_force_tt<256>(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, force_s,
+                             xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, R, unit, dt, fused, exact,
+                             grid_items, st);
+    else
+        launch_force_tt<kForceThreads>(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info,
+                                       force_s, xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, R, unit,
+                                       dt, fused, exact, grid_items, st);
+}
+
+// The batch's fused force pass under the queue scheduler (sph_queue.cuh).
+template <int T, bool Exact, bool Unit>
+__global__ void __launch_bounds__(T) k_force_queue(const ForceArgs A, const BatchQueue Q) {
+    __shared__ QueueShared<T> S;
+    __shared__ uint32_t s_delta[9][T];
+    __shared__ uint32_t s_off[10][T];
+    if (!queue_start<T>(Q, S)) return;
+    while (queue_next<T>(Q, S)) {
+        const TileScene R = queue_scene<T>(Q, S);
+        const int i = (int)(S.first + threadIdx.x);
+        force_one<T, true, Exact, Unit>(i, threadIdx.x < S.count, -1, A, R, s_delta, s_off);
+    }
+}
+
+template <int T, bool Exact, bool Unit>
+void force_queue_launch(const ForceArgs& A, const BatchQueue& Q, cudaStream_t st) {
+    static int per_sm = -1, sms = 0;  // resident blocks per SM and SMs of the current device
+    if (per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_queue<T, Exact, Unit>, T, 0);
+        if (per_sm < 1) per_sm = 1;
+    }
+    k_force_queue<T, Exact, Unit><<<per_sm * sms, T, 0, st>>>(A, Q);
+}
+
+template <int T>
+void force_queue_t(const ForceArgs& A, const BatchQueue& Q, bool unit, bool exact, cudaStream_t st) {
+    if (exact)
+        unit ? force_queue_launch<T, true, true>(A, Q, st) : force_queue_launch<T, true, false>(A, Q, st);
+    else
+        unit ? force_queue_launch<T, false, true>(A, Q, st) : force_queue_launch<T, false, false>(A, Q, st);
+}
+
+void launch_force_queue(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
+                        size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start,
+                        const uint32_t* cell_end, uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u,
+                        float4* keep_f, float4* keep_v, const BatchQueue& Q, bool unit, float dt, int exact,
+                        int threads, cudaStream_t st) {
+    const ForceArgs A{pos_s, rec_pd,  rec_vi, mask,      mask_stride, nbr,    cell_start, cell_end, nullptr,
+                      nullptr, idx,   nullptr, pos_u,    vel_u,       veleval_u, keep_f, keep_v,     dt};
+    if (threads == 64)
+        force_queue_t<64>(A, Q, unit, exact != 0, st);
+    else if (threads == 256)
+        force_queue_t<256>(A, Q, unit, exact != 0, st);
+    else
+        force_queue_t<kForceThreads>(A, Q, unit, exact != 0, st);
+}
+
 void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
-                  size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                  size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                   float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
                   float4* veleval_u, float4* keep_f, float4* keep_v, const StepParams& p, float dt, int fused,
-                  int exact, int grid_items, cudaStream_t st) {
-    launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, cell_end, info, force_s, xsph_s, idx, vel_s,
+                  int exact, int grid_items, int threads, cudaStream_t st) {
+    launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, force_s, xsph_s, idx, vel_s,
                    pos_u, vel_u, veleval_u, keep_f, keep_v, OneScene{p}, p.unit_scale != 0, dt, fused, exact,
-                   grid_items, st);
+                   grid_items, threads, st);
 }
 
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
-                        size_t mask_stride, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
+                        size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                         uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,
                         float4* keep_v, const ManyScenes& scenes, bool unit, float dt, int exact, int grid_items,
-                        cudaStream_t st) {
-    launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, cell_start, cell_end, info, nullptr, nullptr, idx,
-                   nullptr, pos_u, vel_u, veleval_u, keep_f, keep_v, scenes, unit, dt, 1, exact, grid_items, st);
+                        int threads, cudaStream_t st) {
+    launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, nullptr, nullptr, idx,
+                   nullptr, pos_u, vel_u, veleval_u, keep_f, keep_v, scenes, unit, dt, 1, exact, grid_items, threads,
+                   st);
 }
 
 }  // namespace sphk

@@ -57,6 +57,23 @@ class SPH:
         self._ck(self.lib.sph_get_params(self.ctx, C.byref(sp), C.byref(g), C.byref(gs)))
         return sp, g, gs
 
+    # -- launch shapes ----------------------------------------------------
+    def launch_config(self):
+        cfg = abi.sph_launch_config()
+        self._ck(self.lib.sph_get_launch_config(self.ctx, C.byref(cfg)))
+        return cfg.as_tuple()
+
+    def set_launch_config(self, density_threads, force_threads, scan_tile_cells):
+        cfg = abi.sph_launch_config(int(density_threads), int(force_threads), int(scan_tile_cells), 0)
+        self._ck(self.lib.sph_set_launch_config(self.ctx, C.byref(cfg)))
+
+    def autotune(self, dt=0.001, steps=3, retime=False):
+        """Times the candidate launch shapes (state unchanged), keeps the fastest."""
+        cfg = abi.sph_launch_config()
+        self._ck(self.lib.sph_autotune(self.ctx, float(dt), int(steps), abi.SPH_TUNE_RETIME if retime else 0,
+                                       C.byref(cfg)))
+        return cfg.as_tuple()
+
     # -- particles --------------------------------------------------------
     @staticmethod
     def _f4(a, n=None):

@@ -404,6 +404,36 @@ int sph_step_eager(sph_ctx* ctx, float dt, int nsteps);
 int sph_step_profile(sph_ctx* ctx, float dt, int nsteps, float* kernel_ms, int cap, int* nkernels);
 const char* sph_profile_kernel_name(sph_ctx* ctx, int k);
 
+/* Launch shapes of the step's kernels.  No counterpart in the reference,
+ * whose work-group sizes are constants of its host code
+ * (rtpslib/system/sph/Density.cpp:80, Force.cpp:82).  Every shape gives the
+ * same results bit for bit; only the time differs. */
+typedef struct {
+    int density_threads; /* threads per block of the density pass: 128, 256 (default) or 512 */
+    int force_threads;   /* of the fused force pass: 64, 128 (default) or 256 */
+    int scan_tile_cells; /* cells per block of the cell totals and scan: 2048, 4096 (default) or 8192 */
+    int reserved;        /* 0 */
+} sph_launch_config;
+
+/* The context's launch shapes.  set: SPH_EINVAL for a value outside the
+ * listed ones (the context keeps its shapes). */
+int sph_get_launch_config(sph_ctx* ctx, sph_launch_config* cfg);
+int sph_set_launch_config(sph_ctx* ctx, const sph_launch_config* cfg);
+
+#define SPH_TUNE_RETIME 1 /* time the candidates even when the process has a result for this key */
+
+/* Autotuner.  Times the candidate shapes of the density pass, the force
+ * pass and the cell scan over `steps` fused steps each, from the current
+ * state (saved before and restored after, so the simulation does not
+ * advance), keeps the fastest of each and sets them on the context.  The
+ * result is remembered in the process per (max_num, nb_cells, arithmetic
+ * mode): a later call on any context with the same key takes it without
+ * timing, unless flags has SPH_TUNE_RETIME.  chosen (nullable) receives the
+ * shapes.  Needs particles (SPH_ESTATE without); times the step without a
+ * triangle mesh or hoses (SPH_ESTATE with one).  Blocking; allocates
+ * 48 bytes per particle of scratch while it runs. */
+int sph_autotune(sph_ctx* ctx, float dt, int steps, int flags, sph_launch_config* chosen);
+
 /* Force-stage arithmetic.  0 (default): FMA and reciprocals, within the
  * FP32 tolerance of the oracle.  1: the oracle's exact operation sequence
  * (IEEE divisions and square roots, no contraction), bitwise equal to the
@@ -486,6 +516,29 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
 int sph_batch_destroy(sph_batch* batch);
 int sph_batch_set_stream(sph_batch* batch, void* stream);
 int sph_batch_set_exact(sph_batch* batch, int exact);
+/* Launch shapes and autotuner of the batched step (sph_launch_config): the
+ * same as for one system, keyed per (total particle slots, total cells,
+ * arithmetic mode) of the batch. */
+int sph_batch_get_launch_config(sph_batch* batch, sph_launch_config* cfg);
+int sph_batch_set_launch_config(sph_batch* batch, const sph_launch_config* cfg);
+int sph_batch_autotune(sph_batch* batch, float dt, int steps, int flags, sph_launch_config* chosen);
+
+/* Scheduler of the batch's neighbour passes (no counterpart in the
+ * reference).  SPH_SCHED_GRID (default): one thread per sorted particle of
+ * every scene, one grid per pass, each particle's scene looked up from its
+ * key.  SPH_SCHED_QUEUE: as many blocks as fit on the GPU, each taking
+ * (scene, tile) items from a device counter; a block's scene parameters sit
+ * in shared memory.  The results are the same bits either way. */
+#define SPH_SCHED_GRID 0
+#define SPH_SCHED_QUEUE 1
+int sph_batch_set_scheduler(sph_batch* batch, int scheduler);
+int sph_batch_get_scheduler(sph_batch* batch, int* scheduler);
+/* Test support for the queue scheduler's bounded waits: with hold set the
+ * block that builds the queue's item table never publishes it, so every
+ * block's wait for it runs out after spin_limit polls (a poll is about
+ * 0.25 us; the default limit is 2^22) and the next sph_batch_sync returns
+ * SPH_ETIMEOUT; the batch stays usable.  hold = 0 restores normal steps. */
+int sph_batch_queue_test_hold(sph_batch* batch, int hold, unsigned spin_limit);
 /* Replace scene `scene`'s particles (veleval NULL: zero).  Blocking. */
 int sph_batch_upload(sph_batch* batch, int scene, const sph_float4* pos, const sph_float4* vel,
                      const sph_float4* veleval, int n);

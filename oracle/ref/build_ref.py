@@ -108,13 +108,23 @@ def build(reference, verbose=False):
     return OUT_LIB
 
 
+def default_reference():
+    """RTPS_REFERENCE_TREE when set, else a directory named `reference` beside
+    the repository (None when neither exists)."""
+    env = os.environ.get("RTPS_REFERENCE_TREE")
+    if env:
+        return env
+    beside = os.path.join(os.path.dirname(os.path.dirname(ORACLE)), "reference")
+    return beside if os.path.isdir(beside) else None
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=default_reference())
     ap.add_argument("-v", "--verbose", action="store_true")
     a = ap.parse_args()
-    if not os.path.isdir(a.reference):
-        print("reference tree not found at %s; nothing built" % a.reference)
+    if not a.reference or not os.path.isdir(a.reference):
+        print("reference tree not found (%s); nothing built" % a.reference)
         return 0
     print(build(a.reference, a.verbose))
     return 0
