@@ -51,8 +51,8 @@ FALLBACK_HBM_GBS = 6800.0
 # at the state named here; reported as roofline.traffic (with that state) for
 # the dominant kernel at that workload.
 TRAFFIC_STATE = "one launch at step 6 of the 2,097,152-particle dam break from the lattice at rest (ncu)"
-MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 203.607552e6 + 72.219392e6,
-                    "k_density": 55.70176e6 + 74.822144e6}
+MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 211.974656e6 + 72.460032e6,
+                    "k_density": 81.818624e6 + 85.036544e6}
 
 
 def parse():
@@ -398,19 +398,34 @@ def bench_calibration(args, torch):
     targets = record_targets(b, hidden, steps, args.cal_k, DT, torch)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    last = {}
+
+    def keep_last(k, losses, mus, dmu):
+        last["dmu"], last["mus"] = np.asarray(dmu, np.float64), np.asarray(mus, np.float64)
+
     mu, hist = calibrate_viscosity(b, targets, [0.02] * S, iterations=args.cal_iters, nsteps=steps, K=args.cal_k,
-                                   dt=DT)
+                                   dt=DT, on_iteration=keep_last)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
     b.close()
     hidden = np.asarray(hidden)
     err = np.abs(mu - hidden)
+    # the scenes recovered least well, with what the descent saw of them at
+    # its last iteration: the loss (0 at the hidden viscosity, the targets
+    # being that scene's own run) and its slope dL/dlog(mu)
+    rel = err / hidden
+    worst = []
+    for s_ in np.argsort(rel)[::-1][:3]:
+        worst.append({"scene": int(s_), "particles": int(ns[s_]), "hidden_mu": float(hidden[s_]),
+                      "recovered_mu": float(mu[s_]), "rel_err": float(rel[s_]),
+                      "loss_first": float(hist[0][0][s_]), "loss_last": float(hist[-1][0][s_]),
+                      "dL_dlogmu_last": float(last["dmu"][s_] * last["mus"][s_]) if last else None})
     return {"metric": "scenes*iterations/s", "value": S * args.cal_iters / el, "scenes": S,
             "particles": int(sum(ns)), "iterations": args.cal_iters, "steps": steps, "checkpoint_every": args.cal_k,
             "seconds": el, "mu_abs_err_mean": float(err.mean()), "mu_abs_err_max": float(err.max()),
             "mu_rel_err_median": float(np.median(err / hidden)), "mu_rel_err_max": float((err / hidden).max()),
             "loss_first_median": float(np.median(hist[0][0])), "loss_last_median": float(np.median(hist[-1][0])),
-            "start_mu": 0.02,
+            "start_mu": 0.02, "worst_scenes": worst,
             "note": "host wall clock around the whole loop (rollouts, losses, backward passes, iRprop- steps on log mu)"}
 
 
