@@ -528,6 +528,31 @@ def bench_surface(args, torch, peak):
     return out
 
 
+def host_link(stream, pin, n, reps=10):
+    """Copy rates of the host link on the e2e loop's own pinned buffers, with
+    plain stream copies: the position upload (16 B per particle) that the step
+    waits for, and the three state downloads (48 B per particle) that wait for
+    the step.  The velocity uploads overlap the step and are not counted."""
+    import torch
+
+    dev = [torch.empty((n, 4), dtype=torch.float32, device="cuda") for _ in pin]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    up = down = float("inf")
+    for _ in range(reps):
+        ev[0].record(stream)
+        dev[0].copy_(pin[0], non_blocking=True)
+        ev[1].record(stream)
+        for d, h in zip(dev, pin):
+            h.copy_(d, non_blocking=True)
+        ev[2].record(stream)
+        ev[2].synchronize()
+        up = min(up, ev[0].elapsed_time(ev[1]))
+        down = min(down, ev[1].elapsed_time(ev[2]))
+    b = 16.0 * n
+    return {"h2d_gbs": b / (up / 1e3) / 1e9, "d2h_gbs": len(pin) * b / (down / 1e3) / 1e9,
+            "upload_pos_ms": up, "download_state_ms": down}
+
+
 def config_block(n, c, warmup, steps):
     return {"workload": "SPH dam break, %d particles FP32, lattice spacing (0.125/N)^(1/3), h=2s, dt=0.001; "
                         "timed: steps %d..%d of the rollout from the lattice at rest" % (n, warmup, warmup + steps),
@@ -631,6 +656,7 @@ def main():
         abi.check(lib, s.ctx, lib.sph_sync(s.ctx))
     t_e2e = max_over_ranks(time.perf_counter() - t0)
     barrier()
+    link = host_link(stream, pin, n)
     # --- the same step later in the rollout (the fluid has collapsed: more
     # neighbours per particle than near the lattice at rest) ------------------
     steady = None
@@ -662,15 +688,21 @@ def main():
     achieved = ab[dom] / (kern_ms[dom] / 1e3) / 1e9
     b_step = sum(ab.values())
     step_ms = t_ms / steps
+    # the e2e loop's floor on this host link: the position upload, the step
+    # and the three downloads run one after the other
+    e2e_value = n * args.e2e_steps * world / t_e2e
+    link["bound_value"] = n * world / ((link["upload_pos_ms"] + step_ms + link["download_state_ms"]) / 1e3)
+    link["frac"] = e2e_value / link["bound_value"]
     line = {
         "metric": "particle-updates/s at 2M SPH", "value": value, "unit": "particle-updates/s", "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break lattice, zero initial velocity)",
         "config": config_block(n, c, args.warmup, steps),
-        "e2e": {"value": n * args.e2e_steps * world / t_e2e, "unit": "particle-updates/s",
+        "e2e": {"value": e2e_value, "unit": "particle-updates/s",
                 "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n,
                 "note": "state (pos, vel, veleval) uploaded from and downloaded to pinned host memory every step; "
-                        "%d steps" % args.e2e_steps},
+                        "%d steps" % args.e2e_steps,
+                "link": link},
         "gpu_launches": nk.value * steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
