@@ -623,13 +623,13 @@ int sph_batch_adjoint_backward_traj(sph_batch* batch, const sph_float4* dL_dpos_
  *
  * Limit: n <= 1,048,576 (SPH_EINVAL above).  All scratch memory lives in one
  * statically sized device array of the library (about 9 MiB, held by every
- * GPU that loads the library until the process exits).  The first call on a
- * device looks up that array's device address; make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU (other
- * streams, other threads) race and corrupt each other; each call clears the
- * parts of it that must start at zero.  Blocking: every call copies its status
- * word back on the given stream and waits for that stream (and no other)
- * before it returns.  The address is cached per device for the life of the
+ * GPU that loads the library until the process exits).  Calls share the
+ * array: calls that overlap on the GPU (other streams, other threads) race and
+ * corrupt each other; each call clears the parts of it that must start at
+ * zero.  Blocking: every call copies its status word back on the given stream
+ * and waits for that stream (and no other) before it returns, so the call
+ * cannot be captured into a CUDA graph; make every call outside stream
+ * capture.  The address is cached per device for the life of the
  * process: a cudaDeviceReset invalidates it, so do not call this function
  * after resetting a device it was used on. */
 int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
