@@ -11,6 +11,8 @@ import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "librtps_sph.so")
+# the same library compiled with every kernel index bounds-checked (SPH_EBOUNDS)
+CHECKED_LIB_PATH = os.path.join(PKG, "librtps_sph_checked.so")
 
 
 class sph_float4(C.Structure):
@@ -51,12 +53,12 @@ SPH_SCHED_GRID, SPH_SCHED_QUEUE = 0, 1
 assert C.sizeof(SPHParams) == 144 and SPHParams.gravity.offset == 128
 assert C.sizeof(GridParams) == 128 and GridParams.nb_cells.offset == 112
 
-SPH_OK, SPH_EINVAL, SPH_ENOMEM, SPH_ECUDA, SPH_EOOB, SPH_ETIMEOUT, SPH_ESTATE = 0, -1, -2, -3, -4, -5, -6
+SPH_OK, SPH_EINVAL, SPH_ENOMEM, SPH_ECUDA, SPH_EOOB, SPH_ETIMEOUT, SPH_ESTATE, SPH_EBOUNDS = 0, -1, -2, -3, -4, -5, -6, -7
 SPH_INTEGRATOR_LEAPFROG, SPH_INTEGRATOR_EULER = 0, 1
 SPH_MAX_GRAVITY_SOURCES = 64
 SPH_MAX_TRIANGLES = 1 << 20
 STATUS_NAMES = {0: "SPH_OK", -1: "SPH_EINVAL", -2: "SPH_ENOMEM", -3: "SPH_ECUDA", -4: "SPH_EOOB",
-                -5: "SPH_ETIMEOUT", -6: "SPH_ESTATE"}
+                -5: "SPH_ETIMEOUT", -6: "SPH_ESTATE", -7: "SPH_EBOUNDS"}
 EMPTY_CELL = 0xFFFFFFFF
 
 FIELDS = {

@@ -8,9 +8,10 @@ from . import abi
 
 
 class Batch:
-    def __init__(self, params, max_num, exact=False):
-        """params: list of (SPHParams, GridParams, GridParams scaled) per scene."""
-        self.lib = abi.load_library()
+    def __init__(self, params, max_num, exact=False, lib=None):
+        """params: list of (SPHParams, GridParams, GridParams scaled) per scene;
+        lib: a loaded library (the default one when None)."""
+        self.lib = lib if lib is not None else abi.load_library()
         n = len(params)
         SP = (abi.SPHParams * n)(*[p[0] for p in params])
         G = (abi.GridParams * n)(*[p[1] for p in params])

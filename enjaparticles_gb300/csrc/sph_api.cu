@@ -187,6 +187,8 @@ int build_step_params(sph_ctx* c) {
     c->P.integrator = c->integrator;
     c->P.exact = c->exact;
     c->P.n_tri = c->n_tri;
+    c->P.chk_cap = (uint32_t)c->max_num;
+    c->P.chk_err = c->info ? c->info + sphk::kError : nullptr;
     if (c->tri) {
         c->P.tri_raw = c->tri;
         c->P.tri_geo = c->tri + 4 * (size_t)c->tri_cap;
@@ -398,6 +400,10 @@ int read_info(sph_ctx* c) {
     if (c->host_info[sphk::kError] & sphk::kErrLookbackTimeout) {
         return set_err(c, SPH_ETIMEOUT, "sort look-back wait expired; the step result is invalid");
     }
+    if (c->host_info[sphk::kError] & sphk::kErrBounds) {
+        return set_err(c, SPH_EBOUNDS, "an index of a kernel fell outside its array (bounds-checked library); "
+                       "the results are invalid");
+    }
     return SPH_OK;
 }
 
@@ -481,7 +487,11 @@ extern "C" {
 #define SPH_STR(x) SPH_STR_(x)
 const char* sph_build_info(void) {
     return "librtps_sph: GB300 sm_103a SPH step (hash, 8-bit LSD radix sort, cellindices+permute, density, "
-           "force+collision+leapfrog); CUDART " SPH_STR(CUDART_VERSION);
+           "force+collision+leapfrog); CUDART " SPH_STR(CUDART_VERSION)
+#ifdef SPH_CHECKED
+           "; bounds-checked (SPH_CHECKED)"
+#endif
+        ;
 }
 
 int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* grid_scaled, int max_num,
@@ -576,6 +586,7 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
         return rc;
     }
     c->stream = c->own_stream;
+    c->P.chk_err = c->info + sphk::kError;
     c->hist = c->scratch;
     c->status = c->scratch + 4 * 256;
     c->keys_cur = c->keys_a;

@@ -140,12 +140,16 @@ __global__ void __launch_bounds__(256) k_bpermute(const uint2* __restrict__ entr
     if (i >= nvalid) return;
     const uint2 e = __ldg(entries + i);
     const uint32_t id = e.x, key = e.y;
+    if (!sphk::in_bounds(id, table[0].chk_cap, table[0].chk_err)) return;
     const float4 pq = __ldg(pos_u + id);
     const float4 vq = __ldg(veleval_u + id);
     const uint32_t s = key >> cell_bits, cell = key & ((1u << cell_bits) - 1u);
     const uint32_t g = __ldg(cbase + s) + cell;
     const uint32_t cs = __ldg(cell_start + g), ce = __ldg(cell_end + g);
-    if (cs >= ce || ce > (uint32_t)nvalid) return;  // never write outside the cell
+    if (cs >= ce || ce > (uint32_t)nvalid) {  // never write outside the cell
+        if (sphk::kChecked) atomicOr(table[0].chk_err, sphk::kErrBounds);
+        return;
+    }
     const uint32_t* ids = reinterpret_cast<const uint32_t*>(entries);
     uint32_t rank = 0;
     for (uint32_t t = cs; t < ce; ++t) rank += __ldg(ids + 2 * t) < id ? 1u : 0u;
@@ -397,6 +401,10 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     cudaError_t e = cudaMemcpy(b->scene_of, sof.data(), N * 2, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_slot_off, b->slot_off.data(), nscenes * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b->d_cbase, b->cbase.data(), nscenes * 4, cudaMemcpyHostToDevice);
+    for (StepParams& P : b->P) {
+        P.chk_cap = (uint32_t)N;
+        P.chk_err = b->info_nb + sphk::kError;
+    }
     if (e == cudaSuccess) e = cudaMemcpy(b->d_table, b->P.data(), nscenes * sizeof(StepParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_num, 0, nscenes * 4);
     if (e == cudaSuccess) e = cudaMemset(b->d_del, 0, nscenes * 4);
@@ -454,6 +462,8 @@ int sph_batch_set_params(sph_batch* b, int scene, const SPHParams* sphp) {
     std::string e;
     if (sph_make_step_params(sp, b->gp[scene], b->gps[scene], P, e) != SPH_OK)
         return berr(b, SPH_EINVAL, "scene %d: %s", scene, e.c_str());
+    P.chk_cap = b->P[scene].chk_cap;
+    P.chk_err = b->P[scene].chk_err;
     b->sp[scene] = sp;
     b->P[scene] = P;
     BCK(b, cudaMemcpyAsync(b->d_table + scene, &b->P[scene], sizeof(StepParams), cudaMemcpyHostToDevice, b->stream));
@@ -554,11 +564,15 @@ int sph_batch_step(sph_batch* b, float dt, int nsteps) {
 int sph_batch_sync(sph_batch* b) {
     if (!b) return SPH_EINVAL;
     BCK(b, cudaStreamSynchronize(b->stream));
-    // a bounded wait of the queue scheduler that ran out (sph_queue.cuh)
+    // a bounded wait of the queue scheduler that ran out (sph_queue.cuh), or
+    // an index out of bounds (bounds-checked library)
     int err = 0;
     BCK(b, cudaMemcpy(&err, b->info_nb + sphk::kError, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
         BCK(b, cudaMemset(b->info_nb + sphk::kError, 0, sizeof(int)));
+        if (err & sphk::kErrBounds)
+            return berr(b, SPH_EBOUNDS, "an index of a kernel fell outside its array (bounds-checked library, "
+                        "error word %d); the steps since the last sync are invalid", err);
         return berr(b, SPH_ETIMEOUT, "a bounded wait of the queue scheduler expired (error word %d); the steps "
                     "since the last sync are invalid", err);
     }

@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(256) k_cells_permute(const uint32_t* __restric
     }
     if (Gather == 0) return;
     const uint32_t o = __ldg(idx + i);
+    if (!in_bounds(o, (uint32_t)n, info + kError)) return;
     pos_s[i] = __ldg(pos_u + o);
     veleval_s[i] = __ldg(veleval_u + o);
     if (Gather == 2) vel_s[i] = __ldg(vel_u + o);
@@ -79,6 +80,7 @@ __global__ void __launch_bounds__(256) k_permute(const uint32_t* __restrict__ id
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t o = __ldg(idx + i);
+    if (!in_bounds(o, (uint32_t)n, const_cast<int*>(info) + kError)) return;
     pos_s[i] = __ldg(pos_u + o);
     vel_s[i] = __ldg(vel_u + o);
     veleval_s[i] = __ldg(veleval_u + o);

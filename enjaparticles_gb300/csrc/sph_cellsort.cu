@@ -278,7 +278,8 @@ __global__ void __launch_bounds__(256) k_cell_place(const uint32_t* __restrict__
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const int i = i0 + k * (int)blockDim.x;
-        if (i < n) entries[cs[k] + slot[k]] = make_uint2((uint32_t)i, key[k]);
+        if (i < n && in_bounds(cs[k] + slot[k], (uint32_t)n, const_cast<int*>(info) + kError))
+            entries[cs[k] + slot[k]] = make_uint2((uint32_t)i, key[k]);
     }
 }
 
@@ -302,6 +303,8 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
     if (s >= n) return;
     const uint2 e = __ldg(entries + s);
     const uint32_t id = e.x, key = e.y;
+    int* err = const_cast<int*>(info) + kError;
+    if (!in_bounds(id, (uint32_t)n, err)) return;
     // the gathers do not depend on the rank: in flight during the ranking
     const float4 pq = __ldg(pos_u + id);
     float4 vq = make_float4(0.f, 0.f, 0.f, 0.f), wq = vq;
@@ -310,7 +313,10 @@ __global__ void __launch_bounds__(256) k_cell_permute(const uint2* __restrict__ 
     const uint32_t cs = __ldg(cell_start + key), ce = __ldg(cell_end + key);
     // every entry lies in a cell of [cs, ce) within [0, n) when the counts
     // were zero at the start of the step; never write outside it
-    if (cs >= ce || ce > (uint32_t)n) return;
+    if (cs >= ce || ce > (uint32_t)n) {
+        if (kChecked) atomicOr(err, kErrBounds);
+        return;
+    }
     const uint32_t* ids = reinterpret_cast<const uint32_t*>(entries);
     uint32_t rank = 0;
     for (uint32_t t = cs; t < ce; ++t) rank += __ldg(ids + 2 * t) < id ? 1u : 0u;

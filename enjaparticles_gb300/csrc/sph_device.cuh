@@ -33,6 +33,31 @@ enum InfoSlot : int {
     kInfoSlots = 16
 };
 constexpr int kErrLookbackTimeout = 1;
+// Bit of the error word: a bounds-checked build found an index outside the
+// array it addresses (the access was skipped).
+constexpr int kErrBounds = 4;
+
+// Bounds-checked builds (-DSPH_CHECKED: librtps_sph_checked.so).  Every
+// gather and scatter index of the step's kernels is tested against the array
+// it addresses before the access; a failed test sets kErrBounds in the
+// context's error word and skips the access, so that an indexing error shows
+// up as a status (SPH_EBOUNDS) where the default build would read or write
+// out of bounds.  In the default build in_bounds is the constant true and the
+// tests compile away.
+#ifdef SPH_CHECKED
+constexpr bool kChecked = true;
+#else
+constexpr bool kChecked = false;
+#endif
+__device__ __forceinline__ bool in_bounds(uint32_t i, uint32_t bound, int* err) {
+    if constexpr (!kChecked) {
+        return true;
+    } else {
+        if (i < bound) return true;
+        atomicOr(err, kErrBounds);
+        return false;
+    }
+}
 
 // Neighbour bitmask written by the density pass: bit b of particle i says
 // whether its b-th candidate (in walk order) is a neighbour other than itself;
@@ -72,6 +97,10 @@ struct StepParams {
     float4* tri_geo;              // 4 float4 per triangle (sph_triangles.cu)
     float4* tri_box;              // 2 float4 per triangle
     float4* tri_tile;             // 2 float4 per 256 triangles
+    // bounds-checked builds: slots of the particle arrays (a batch: of all
+    // scenes) and the error word that in_bounds reports to
+    uint32_t chk_cap;
+    int* chk_err;
 };
 constexpr int kIntegratorLeapfrog = 0;
 constexpr int kIntegratorEuler = 1;

@@ -153,8 +153,11 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
         if (Fused && in_range && !live) {
             const uint32_t sc = R.scene(i), os = R.out_start(sc), kept = os - __ldg(R.seg + sc);
             const uint32_t j = (uint32_t)i - os, dst = __ldg(R.slot_off + sc) + kept + j;
-            pos_u[dst] = __ldg(pos_s + i);
-            vel_u[dst] = __ldg(R.vel_s + i);
+            const StepParams& Q = R.params(i);
+            if (in_bounds(dst, Q.chk_cap, Q.chk_err)) {
+                pos_u[dst] = __ldg(pos_s + i);
+                vel_u[dst] = __ldg(R.vel_s + i);
+            }
             if (j == 0) {
                 R.del[sc] = R.num[sc] - (int)kept;
                 R.num[sc] = (int)kept;
@@ -246,8 +249,11 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
         const uint32_t kmax = __reduce_max_sync(wmask, cnt);
         for (uint32_t k = 0; k < kmax; ++k) {
             if (k < cnt) {
-                const uint32_t j = index_of(next_bit());
-                force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
+                const uint32_t p = next_bit();
+                if (!in_bounds(p, M, P.chk_err)) continue;  // a mask bit past the walk's candidates
+                const uint32_t j = index_of(p);
+                if (in_bounds(j, P.chk_cap, P.chk_err))
+                    force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
             }
         }
     } else {
@@ -271,6 +277,7 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
                 while (q < M) {
                     const uint32_t pp = q++;
                     const uint32_t j = index_of(pp);
+                    if (!in_bounds(j, P.chk_cap, P.chk_err)) continue;
                     const float4 pj = __ldg(rec_pd + j);
                     const float r2 =
                         dist2_exact(__fsub_rn(pi.x, pj.x), __fsub_rn(pi.y, pj.y), __fsub_rn(pi.z, pj.z));
@@ -284,9 +291,10 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
                 }
             }
             if (!__any_sync(wmask, have)) break;
-            if (have) {
+            if (have && in_bounds(p, M, P.chk_err)) {
                 const uint32_t j = index_of(p);
-                force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
+                if (in_bounds(j, P.chk_cap, P.chk_err))
+                    force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
             }
         }
     }
@@ -327,6 +335,7 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     }
     if (!reindex) {
         orig = __ldg(idx + i);
+        if (!in_bounds(orig, P.chk_cap, P.chk_err)) return;
         v = vel_u[orig];
     } else if (out >= 0) {
         orig = (uint32_t)i;
@@ -337,6 +346,7 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
         keep_f[i] = f;
         keep_v[i] = v;
     }
+    if (!in_bounds(orig, P.chk_cap, P.chk_err)) return;
     const float4 pp = __ldg(pos_s + i);
     // point sources after force (SPH.cpp:289-296), then the walls
     if (P.n_grav > 0) f = gravity_add<Exact>(f, pp, P);

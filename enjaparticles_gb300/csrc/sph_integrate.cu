@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(256) k_leapfrog(const float4* __restrict__ pos
     float4 po, vo, eo;
     leapfrog_core(p, __ldg(vel_s + i), __ldg(force_s + i), __ldg(xsph_s + i), dt, P, po, vo, eo);
     const uint32_t o = __ldg(idx + i);
+    if (!in_bounds(o, P.chk_cap, P.chk_err)) return;
     vel_u[o] = vo;
     veleval_u[o] = eo;
     pos_u[o] = po;
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(256) k_euler(const float4* __restrict__ pos_s,
     float4 po, vo;
     euler_core(scaled(__ldg(pos_s + i), P), __ldg(vel_s + i), __ldg(force_s + i), dt, P, po, vo);
     const uint32_t o = __ldg(idx + i);
+    if (!in_bounds(o, P.chk_cap, P.chk_err)) return;
     vel_u[o] = vo;
     pos_u[o] = po;
 }
@@ -119,6 +121,7 @@ __global__ void __launch_bounds__(256) k_step_velocities(const float4* __restric
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_old) return;
     const uint32_t o = __ldg(idx + i);
+    if (!in_bounds(o, (uint32_t)n_old, info + kError)) return;  // original indices are below the step's count
     if (i < n) {
         const float4 ve = __ldg(veleval_u + o);
         float* r = reinterpret_cast<float*>(rec_vi + i);

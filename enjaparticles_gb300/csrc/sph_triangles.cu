@@ -322,6 +322,7 @@ __global__ void __launch_bounds__(kTriThreads) k_triangles(const float4* __restr
     } else {
         o = S.idx[i];
     }
+    if (!in_bounds(o, P.chk_cap, P.chk_err)) return;
     float4 po, vo, eo;
     if (P.integrator == kIntegratorEuler) {
         euler_core(pos, vel, ff, S.dt, P, po, vo);

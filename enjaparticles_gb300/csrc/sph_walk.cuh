@@ -22,6 +22,12 @@
 
 namespace sphk {
 
+// A run [rs, re) of sorted indices: non-empty and inside the particle arrays
+// (bounds-checked builds; always true otherwise).
+__device__ __forceinline__ bool run_ok(const StepParams& P, uint32_t rs, uint32_t re) {
+    return in_bounds(rs, re, P.chk_err) && in_bounds(re - 1u, P.chk_cap, P.chk_err);
+}
+
 // Integer row hashing applies: every intermediate of the float hash formula is
 // an integer below 2^24 for cells within one cell of the grid.
 __device__ __forceinline__ bool cell_fast(const StepParams& P, const int3& c) {
@@ -51,7 +57,10 @@ __device__ __forceinline__ void walk_rows_fast(const StepParams& P, const uint32
                     }
                 }
             }
-            if (rs != kEmpty) f(rs, __ldg(ce + last));
+            if (rs != kEmpty) {
+                const uint32_t re = __ldg(ce + last);
+                if (run_ok(P, rs, re)) f(rs, re);
+            }
         }
     }
 }
@@ -92,7 +101,7 @@ __device__ __forceinline__ void walk_rows_fast_batched(const StepParams& P, cons
     }
 #pragma unroll
     for (int r = 0; r < 9; ++r)
-        if (rs[r] != kEmpty) f(rs[r], re[r]);
+        if (rs[r] != kEmpty && run_ok(P, rs[r], re[r])) f(rs[r], re[r]);
 }
 
 // The 27 cells one by one with the reference's float hash (up to 27 calls).
@@ -109,7 +118,10 @@ __device__ __forceinline__ void walk_rows_slow(const StepParams& P, const uint32
                 const uint32_t h = (uint32_t)grid_hash_f(x, y, z, P.gs_res);
                 if (h >= C) continue;
                 const uint32_t s = __ldg(cs + h);
-                if (s != kEmpty) f(s, __ldg(ce + h));
+                if (s != kEmpty) {
+                    const uint32_t e = __ldg(ce + h);
+                    if (run_ok(P, s, e)) f(s, e);
+                }
             }
 }
 

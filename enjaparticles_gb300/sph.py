@@ -13,8 +13,10 @@ from . import abi
 
 
 class SPH:
-    def __init__(self, sphp, grid, max_num, grid_scaled=None, exact=False):
-        self.lib = abi.load_library()
+    def __init__(self, sphp, grid, max_num, grid_scaled=None, exact=False, lib=None):
+        """lib: a loaded library (abi.load_library(path)), e.g. the
+        bounds-checked one; the default library when None."""
+        self.lib = lib if lib is not None else abi.load_library()
         self.ctx = C.c_void_p()
         gs = C.byref(grid_scaled) if grid_scaled is not None else None
         abi.check(self.lib, None, self.lib.sph_create(C.byref(sphp), C.byref(grid), gs, int(max_num),

@@ -114,6 +114,8 @@ _Static_assert(sizeof(GridParams) == 128, "GridParams must be 128 bytes");
 #define SPH_EOOB      -4  /* particles left the grid (reported, not trapped) */
 #define SPH_ETIMEOUT  -5  /* a bounded device-side wait expired; the step is invalid */
 #define SPH_ESTATE    -6  /* call not valid in the context's current state */
+#define SPH_EBOUNDS   -7  /* bounds-checked library only: a kernel index fell outside its array (the access
+                             was skipped); the results since the last check are invalid */
 
 /* Value of an empty cell in cell_start (CellIndices.cpp:58-62). */
 #define SPH_EMPTY_CELL 0xffffffffu

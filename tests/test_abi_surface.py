@@ -19,9 +19,15 @@ HEADER = os.path.join(ROOT, "include", "rtps_sph.h")
 
 @pytest.fixture(scope="module")
 def lib():
-    if not (os.path.exists(abi.LIB_PATH) and os.path.exists(build_ext.DRIVER)):
+    if not (os.path.exists(abi.LIB_PATH) and os.path.exists(abi.CHECKED_LIB_PATH) and
+            os.path.exists(build_ext.DRIVER)):
         build_ext.build()
     return abi.load_library()
+
+
+@pytest.fixture(scope="module")
+def checked_lib(lib):
+    return abi.load_library(abi.CHECKED_LIB_PATH)
 
 
 def declared_functions():
@@ -44,6 +50,14 @@ def test_every_declared_function_is_exported_and_bound(lib):
     assert not missing, missing
     unbound = [f for f in declared_functions() if f not in abi.SIGNATURES]
     assert not unbound, unbound
+
+
+def test_bounds_checked_library_exports_the_same_boundary(lib, checked_lib):
+    missing = [f for f in declared_functions() if not hasattr(checked_lib, f)]
+    assert not missing, missing
+    assert "bounds-checked" in checked_lib.sph_build_info().decode()
+    assert "bounds-checked" not in lib.sph_build_info().decode()
+    assert abi.STATUS_NAMES[abi.SPH_EBOUNDS] == "SPH_EBOUNDS"
 
 
 def test_parameter_helpers_without_gpu(lib):
