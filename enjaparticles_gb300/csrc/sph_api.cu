@@ -840,8 +840,10 @@ int sph_get_deleted(sph_ctx* c, sph_float4* pos, sph_float4* vel, int cap, int* 
     const int nd = c->host_info[sphk::kDeleted];
     if (count) *count = nd;
     const int k = nd < cap ? nd : cap;
-    if (k > 0 && pos) CK(c, cudaMemcpy(pos, c->del_pos, (size_t)k * 16, cudaMemcpyDeviceToHost));
-    if (k > 0 && vel) CK(c, cudaMemcpy(vel, c->del_vel, (size_t)k * 16, cudaMemcpyDeviceToHost));
+    // on the context's stream only: no wait for other streams of the device
+    if (k > 0 && pos) CK(c, cudaMemcpyAsync(pos, c->del_pos, (size_t)k * 16, cudaMemcpyDeviceToHost, c->stream));
+    if (k > 0 && vel) CK(c, cudaMemcpyAsync(vel, c->del_vel, (size_t)k * 16, cudaMemcpyDeviceToHost, c->stream));
+    if (k > 0 && (pos || vel)) CK(c, cudaStreamSynchronize(c->stream));
     return SPH_OK;
 }
 

@@ -563,13 +563,15 @@ int sph_batch_step(sph_batch* b, float dt, int nsteps) {
 
 int sph_batch_sync(sph_batch* b) {
     if (!b) return SPH_EINVAL;
-    BCK(b, cudaStreamSynchronize(b->stream));
     // a bounded wait of the queue scheduler that ran out (sph_queue.cuh), or
-    // an index out of bounds (bounds-checked library)
+    // an index out of bounds (bounds-checked library); read on the batch's
+    // stream, so that no other stream of the device is waited for
     int err = 0;
-    BCK(b, cudaMemcpy(&err, b->info_nb + sphk::kError, sizeof(int), cudaMemcpyDeviceToHost));
+    BCK(b, cudaMemcpyAsync(&err, b->info_nb + sphk::kError, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
     if (err) {
-        BCK(b, cudaMemset(b->info_nb + sphk::kError, 0, sizeof(int)));
+        BCK(b, cudaMemsetAsync(b->info_nb + sphk::kError, 0, sizeof(int), b->stream));
+        BCK(b, cudaStreamSynchronize(b->stream));
         if (err & sphk::kErrBounds)
             return berr(b, SPH_EBOUNDS, "an index of a kernel fell outside its array (bounds-checked library, "
                         "error word %d); the steps since the last sync are invalid", err);
