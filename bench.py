@@ -51,7 +51,7 @@ FALLBACK_HBM_GBS = 6800.0
 # at the state named here; reported as roofline.traffic (with that state) for
 # the dominant kernel at that workload.
 TRAFFIC_STATE = "one launch at step 6 of the 2,097,152-particle dam break from the lattice at rest (ncu)"
-MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 211.974656e6 + 72.460032e6,
+MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 212.000000e6 + 71.225088e6,
                     "k_density": 81.818624e6 + 85.036544e6}
 
 

@@ -365,8 +365,20 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     pos_u[orig] = po;
 }
 
+// Minimum resident blocks per SM the force kernel is compiled for.  One
+// system in the default arithmetic: 1280 threads per SM (10 blocks of 128),
+// which fits it in 48 registers without spills (the unbounded build took 56
+// with 8 B of spills at 128 threads, 48 with 60 B at 256) and measured 3 %
+// faster.  The exact and batched variants would spill at that bound: 0
+// leaves them unbounded.
+template <int T, bool Exact, class Scenes>
+constexpr int force_min_blocks() {
+    return (!Exact && !Scenes::kBatch) ? 1280 / T : 0;
+}
+
 template <int T, bool Fused, bool Exact, bool Unit, class Scenes>
-__global__ void __launch_bounds__(T) k_force(const ForceArgs A, const int* __restrict__ info, const Scenes R) {
+__global__ void __launch_bounds__(T, (force_min_blocks<T, Exact, Scenes>()))
+    k_force(const ForceArgs A, const int* __restrict__ info, const Scenes R) {
     __shared__ uint32_t s_delta[9][T];
     __shared__ uint32_t s_off[10][T];
     int n_old, out;
