@@ -264,9 +264,12 @@ __device__ __forceinline__ void density_pairs_one(const int i, const DensityArgs
     nbr[i] = cnt;
 }
 
+// One system: compiled for 1536 resident threads per SM (6 blocks of 256),
+// 39 registers without spills instead of 48 (5 blocks): 1 % faster.  A
+// batch's variant (scene lookups) stays unbounded (0).
 template <int T, class Scenes>
-__global__ void __launch_bounds__(T) k_density_pairs(const DensityArgs A, const int* __restrict__ info,
-                                                       const Scenes R) {
+__global__ void __launch_bounds__(T, (Scenes::kBatch ? 0 : 1536 / T))
+    k_density_pairs(const DensityArgs A, const int* __restrict__ info, const Scenes R) {
     int n_old, out;
     const int n = effective_num(info, n_old, out);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
