@@ -325,10 +325,12 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
 // position pairs of the default arithmetic are written from pos_s first
 // (the stage API's permutes do not write them; the counting sort's does).
 void density_launch(sph_ctx* c, bool fused, cudaStream_t st, bool pack = false) {
+    // the fused step's sort leaves the sorted cell keys in keys_a, which the
+    // default arithmetic's cell-pair pass reads
     sphk::launch_density(c->pos_s, fused ? nullptr : c->veleval_s, c->density, c->rec_pd, c->rec_vi,
                          c->nbr, c->mask,
                          (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, c->pos_xy,
-                         c->pos_z, pack, c->lc.density_threads, st);
+                         c->pos_z, pack, c->lc.density_threads, st, fused ? c->keys_a : nullptr);
 }
 
 void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {

@@ -21,6 +21,8 @@
 // its first kMaskBits candidates (in walk order) are neighbours (self
 // excluded) as a bitmask, and the 32-byte record (position, rho),
 // (veleval, 1/rho) the force pass reads for every neighbour.
+#include <type_traits>
+
 #include "sph_queue.cuh"
 #include "sph_walk.cuh"
 
@@ -40,6 +42,9 @@ struct DensityArgs {
     size_t mstride;
     const uint32_t* cs0;
     const uint32_t* ce0;
+    // sorted cell keys (the counting sort's), for the cell-pair pass; null
+    // where the pass is not used
+    const uint32_t* keys;
 };
 
 // Sorted particle i, scalar candidates (every operation rounded on its own
@@ -276,6 +281,242 @@ __global__ void __launch_bounds__(T, (Scenes::kBatch ? 0 : 1536 / T))
     if (i < n) density_pairs_one(i, A, R);
 }
 
+// ---------------------------------------------------------------------------
+// Two particles of one cell per thread (default arithmetic, unit scale, one
+// system, the step's counting sort).  Particles of one cell walk the same
+// 9 row runs, so a thread that takes two of them loads each candidate pair
+// once and runs the pair arithmetic for both: the loads, the loop and the
+// row lookups, most of the pass's instructions, are paid once for two
+// particles.  Each block takes T consecutive sorted particles and pairs them
+// within their cells (the part of a cell inside the block's range: the
+// particles at even rank from its first one, each with the next one when it
+// lies in the same cell), compacts the pairs and the lone particles into its
+// first threads, and every such thread runs the same walk, the second
+// particle of a lone one switched off.  Each particle keeps its own sums,
+// count and mask stream and meets its candidates in its own walk order with
+// the pair alignment of density_pairs_one, so its results are those of
+// density_pairs_one bit for bit.
+struct CellPairLane {
+    float2 px, py, pz;  // the particle's coordinates in both lanes
+    float2 acc;         // poly6 sums of the even and the odd candidates
+    uint32_t cnt;       // neighbours, itself included
+    uint32_t cur, fill, wo;  // mask word stream: `cur` holds `fill` bits of word `wo`
+    uint32_t self;      // its sorted index
+};
+
+__device__ __forceinline__ void cellpair_append(CellPairLane& L, uint32_t* __restrict__ mrow, size_t mstride,
+                                                uint32_t v, uint32_t len, bool store) {
+    L.cur |= v << L.fill;
+    if (L.fill + len >= 32u) {
+        if (store && L.wo < (uint32_t)kMaskWords) mrow[(size_t)L.wo * mstride] = L.cur;
+        ++L.wo;
+        L.cur = L.fill ? (v >> (32u - L.fill)) : 0u;
+        L.fill = L.fill + len - 32u;
+    } else {
+        L.fill += len;
+    }
+}
+
+// One candidate pair (xy = (x, x', y, y'), zz = (z, z')) for one particle:
+// the neighbour bits of both elements into seg, the weights into L.acc.
+__device__ __forceinline__ void cellpair_pair(CellPairLane& L, const float4& xy, const float2& zz, bool v0, bool v1,
+                                              float rc2, float2 h2, uint32_t& seg, uint32_t bit) {
+    const float2 neg1 = make_float2(-1.f, -1.f);
+    const float2 dx = __ffma2_rn(make_float2(xy.x, xy.y), neg1, L.px);
+    const float2 dy = __ffma2_rn(make_float2(xy.z, xy.w), neg1, L.py);
+    const float2 dz = __ffma2_rn(zz, neg1, L.pz);
+    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+    float2 hr = __ffma2_rn(r2, neg1, h2);
+    const bool n0 = v0 && r2.x <= rc2, n1 = v1 && r2.y <= rc2;
+    hr.x = n0 ? hr.x : 0.f;
+    hr.y = n1 ? hr.y : 0.f;
+    L.acc = __ffma2_rn(__fmul2_rn(hr, hr), hr, L.acc);
+    if (n0) seg |= bit;
+    if (n1) seg |= bit << 1;
+}
+
+__device__ __forceinline__ void cellpair_finish(const CellPairLane& L, const float4& p, const DensityArgs& A,
+                                                const StepParams& P, uint32_t* __restrict__ mrow) {
+    const uint32_t i = L.self;
+    if (L.fill != 0 && L.wo < (uint32_t)kMaskWords) mrow[(size_t)L.wo * A.mstride] = L.cur;
+    const float rho = P.dens_coef * (L.acc.x + L.acc.y);
+    A.density[i] = rho;
+    A.rec_pd[i] = make_float4(p.x, p.y, p.z, rho);
+    if (A.veleval_s != nullptr) {
+        const float4 ve = __ldg(A.veleval_s + i);
+        A.rec_vi[i] = make_float4(ve.x, ve.y, ve.z, __frcp_rn(rho));
+    } else {
+        reinterpret_cast<float*>(A.rec_vi + i)[3] = __frcp_rn(rho);
+    }
+    A.nbr[i] = L.cnt;
+}
+
+// Sorted particles a and, when has_b, a + 1 of the same cell.
+__device__ __forceinline__ void density_cellpair(const uint32_t a, const bool has_b, const DensityArgs& A,
+                                                 const OneScene& R) {
+    const StepParams& P = R.P;
+    const float4 pa = __ldg(A.pos_s + a);
+    const int3 c = grid_cell(pa.x, pa.y, pa.z, P.gs_min, P.gs_delta);
+    if (!cell_fast(P, c)) {
+        density_pairs_one((int)a, A, R);
+        if (has_b) density_pairs_one((int)a + 1, A, R);
+        return;
+    }
+    const float4 pb = has_b ? __ldg(A.pos_s + a + 1) : pa;
+    const uint32_t* __restrict__ cs = A.cs0;
+    const uint32_t* __restrict__ ce = A.ce0;
+    const float4* __restrict__ pxy = A.pxy;
+    const float2* __restrict__ pz = A.pz;
+    const uint32_t C = (uint32_t)P.nb_cells;
+    const float rc2 = P.rcut2;
+    const float2 h2 = make_float2(P.h2, P.h2);
+    CellPairLane La, Lb;
+    La.px = make_float2(pa.x, pa.x), La.py = make_float2(pa.y, pa.y), La.pz = make_float2(pa.z, pa.z);
+    Lb.px = make_float2(pb.x, pb.x), Lb.py = make_float2(pb.y, pb.y), Lb.pz = make_float2(pb.z, pb.z);
+    La.acc = Lb.acc = make_float2(0.f, 0.f);
+    La.cnt = Lb.cnt = 0;
+    La.cur = La.fill = La.wo = 0;
+    Lb.cur = Lb.fill = Lb.wo = 0;
+    La.self = a;
+    Lb.self = a + 1u;
+    uint32_t* mrow_a = A.mask + a;
+    uint32_t* mrow_b = mrow_a + 1;
+    const size_t ms = A.mstride;
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; ++dz) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int base = ((c.z + dz) * P.res_y + (c.y + dy)) * P.res_x + c.x;
+            uint32_t rs = kEmpty, last = 0;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                const uint32_t h = (uint32_t)(base + dx);
+                if (h < C) {
+                    const uint32_t s0 = __ldg(cs + h);
+                    if (s0 != kEmpty) {
+                        if (rs == kEmpty) rs = s0;
+                        last = h;
+                    }
+                }
+            }
+            if (rs == kEmpty) continue;
+            const uint32_t re = __ldg(ce + last);
+            if (!run_ok(P, rs, re)) continue;  // bounds-checked builds
+            const uint32_t kend = (re + 1u) >> 1;
+            for (uint32_t ks = rs >> 1; ks < kend; ks += kPairSegment) {
+                const uint32_t ke = ks + kPairSegment < kend ? ks + kPairSegment : kend;
+                uint32_t sa = 0, sb = 0;
+                uint32_t k = ks;
+                if (2u * k < rs) {  // the run's first pair (its element 2k precedes rs)
+                    const float4 xy = __ldg(pxy + k);
+                    const float2 zz = __ldg(pz + k);
+                    const bool v1 = 2u * k + 1u < re;
+                    cellpair_pair(La, xy, zz, false, v1, rc2, h2, sa, 1u);
+                    cellpair_pair(Lb, xy, zz, false, v1, rc2, h2, sb, 1u);
+                    ++k;
+                }
+                const uint32_t kin = (2u * ke <= re) ? ke : ke - 1u;
+#pragma unroll 2
+                for (; k < kin; ++k) {
+                    const float4 xy = __ldg(pxy + k);
+                    const float2 zz = __ldg(pz + k);
+                    const uint32_t bit = 1u << (2u * (k - ks));
+                    cellpair_pair(La, xy, zz, true, true, rc2, h2, sa, bit);
+                    cellpair_pair(Lb, xy, zz, true, true, rc2, h2, sb, bit);
+                }
+                if (k < ke) {  // the run's last pair (its element 2k+1 may be re)
+                    const float4 xy = __ldg(pxy + k);
+                    const float2 zz = __ldg(pz + k);
+                    const uint32_t bit = 1u << (2u * (k - ks));
+                    const bool v1 = 2u * k + 1u < re;
+                    cellpair_pair(La, xy, zz, true, v1, rc2, h2, sa, bit);
+                    cellpair_pair(Lb, xy, zz, true, v1, rc2, h2, sb, bit);
+                }
+                const uint32_t e0 = 2u * ks;
+                const uint32_t lo = rs > e0 ? rs - e0 : 0u;
+                const uint32_t hi = (re < 2u * ke ? re : 2u * ke) - e0;
+                La.cnt += (uint32_t)__popc(sa);
+                Lb.cnt += (uint32_t)__popc(sb);
+                if (a - e0 < 32u) sa &= ~(1u << (a - e0));
+                if (a + 1u - e0 < 32u) sb &= ~(1u << (a + 1u - e0));
+                cellpair_append(La, mrow_a, ms, sa >> lo, hi - lo, true);
+                cellpair_append(Lb, mrow_b, ms, sb >> lo, hi - lo, has_b);
+            }
+        }
+    }
+    cellpair_finish(La, pa, A, P, mrow_a);
+    if (has_b) cellpair_finish(Lb, pb, A, P, mrow_b);
+}
+
+// Particles per block of the cell-pair pass: about two per thread, less the
+// lone particles a block's range holds at 8 to 12 particles per cell, so that
+// the items (pairs and lone particles) about fill the block's threads.
+template <int T>
+constexpr int cellpair_chunk() {
+    return T * 7 / 4;
+}
+
+// Block b takes sorted particles [bC, bC + C): the particle at an even rank
+// of its cell's part in that range starts an item (with the next particle
+// when it is in the same cell and the range); the items are compacted in
+// order and the block's threads take them in turn.
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T) k_density_cellpairs(const DensityArgs A, const int* __restrict__ info,
+                                                         const OneScene R) {
+    constexpr int Cp = cellpair_chunk<T>();
+    __shared__ uint32_t s_item[Cp];
+    __shared__ uint32_t s_warp[2][T / 32];
+    int n_old, out;
+    const int n = effective_num(info, n_old, out);
+    const int base = blockIdx.x * Cp;
+    if (base >= n) return;  // the whole block
+    const int end = base + Cp < n ? base + Cp : n;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    // item flags of the block's particles base + tid and base + T + tid
+    bool start[2], has_b[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int p = base + h * T + (int)threadIdx.x;
+        start[h] = has_b[h] = false;
+        if (p < end) {
+            const uint32_t key = __ldg(A.keys + p);
+            const uint32_t cs = __ldg(A.cs0 + key);
+            const uint32_t first = cs > (uint32_t)base ? cs : (uint32_t)base;  // the cell's first particle in range
+            start[h] = (((uint32_t)p - first) & 1u) == 0u;
+            has_b[h] = start[h] && p + 1 < end && __ldg(A.keys + p + 1) == key;
+        }
+    }
+    unsigned bal[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        bal[h] = __ballot_sync(0xffffffffu, start[h]);
+        if (lane == 0) s_warp[h][warp] = (uint32_t)__popc(bal[h]);
+    }
+    __syncthreads();
+    uint32_t before0 = 0, total0 = 0, before1 = 0, total1 = 0;
+#pragma unroll
+    for (int w = 0; w < T / 32; ++w) {
+        const uint32_t c0 = s_warp[0][w], c1 = s_warp[1][w];
+        before0 += (unsigned)w < warp ? c0 : 0u;
+        before1 += (unsigned)w < warp ? c1 : 0u;
+        total0 += c0;
+        total1 += c1;
+    }
+    const uint32_t below = (1u << lane) - 1u;
+    if (start[0])
+        s_item[before0 + (uint32_t)__popc(bal[0] & below)] =
+            (uint32_t)(base + (int)threadIdx.x) | (has_b[0] ? 0x80000000u : 0u);
+    if (start[1])
+        s_item[total0 + before1 + (uint32_t)__popc(bal[1] & below)] =
+            (uint32_t)(base + T + (int)threadIdx.x) | (has_b[1] ? 0x80000000u : 0u);
+    __syncthreads();
+    const uint32_t total = total0 + total1;
+    for (uint32_t t = threadIdx.x; t < total; t += T) {
+        const uint32_t it = s_item[t];
+        density_cellpair(it & 0x7fffffffu, (it >> 31) != 0u, A, R);
+    }
+}
+
 // Sorted positions as pairs (see k_density_pairs), for the passes whose
 // permute does not write them.
 __global__ void k_pack_pairs(const float4* __restrict__ pos_s, float4* __restrict__ pxy, float2* __restrict__ pz,
@@ -293,15 +534,23 @@ template <int T, class Scenes>
 void launch_density_tt(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                        uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                        const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
-                       int grid_items, float4* pxy, float2* pz, bool pack, cudaStream_t st) {
+                       int grid_items, float4* pxy, float2* pz, bool pack, cudaStream_t st,
+                       const uint32_t* keys) {
     int blocks = (grid_items + T - 1) / T;
     if (blocks < 1) blocks = 1;
     const DensityArgs A{pos_s, pxy, pz, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                        cell_end};
+                        cell_end, keys};
     if (pxy != nullptr && pz != nullptr && unit && !exact) {
         if (pack) {
             const int pb = ((grid_items + 1) / 2 + 255) / 256;
             k_pack_pairs<<<pb < 1 ? 1 : pb, 256, 0, st>>>(pos_s, pxy, pz, info);
+        }
+        if constexpr (std::is_same<Scenes, OneScene>::value) {
+            if (A.keys != nullptr) {
+                const int cp_blocks = (grid_items + cellpair_chunk<T>() - 1) / cellpair_chunk<T>();
+                k_density_cellpairs<T><<<cp_blocks < 1 ? 1 : cp_blocks, T, 0, st>>>(A, info, R);
+                return;
+            }
         }
         k_density_pairs<T, Scenes><<<blocks, T, 0, st>>>(A, info, R);
         return;
@@ -321,19 +570,20 @@ template <class Scenes>
 void launch_density_t(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                       uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                       const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
-                      int grid_items, float4* pxy, float2* pz, bool pack, int threads, cudaStream_t st) {
+                      int grid_items, float4* pxy, float2* pz, bool pack, int threads, cudaStream_t st,
+                      const uint32_t* keys = nullptr) {
     switch (threads) {
         case 128:
             launch_density_tt<128>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st);
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys);
             break;
         case 512:
             launch_density_tt<512>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st);
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys);
             break;
         default:
             launch_density_tt<256>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st);
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys);
     }
 }
 
@@ -396,9 +646,9 @@ void launch_density_queue(const float4* pos_s, const float4* veleval_s, float* d
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
-                    float2* pz, bool pack, int threads, cudaStream_t st) {
+                    float2* pz, bool pack, int threads, cudaStream_t st, const uint32_t* keys) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, pxy, pz, pack, threads, st);
+                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, pxy, pz, pack, threads, st, keys);
 }
 
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,

@@ -228,7 +228,7 @@ void launch_cells_permute(const uint32_t* keys, const uint32_t* idx, uint32_t* c
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
-                    float2* pz, bool pack, int threads, cudaStream_t st);
+                    float2* pz, bool pack, int threads, cudaStream_t st, const uint32_t* keys = nullptr);
 // The fused step's velocity pass, beside density and before force (the first
 // passes that need the uploaded velocities): the veleval lanes of rec_vi in
 // sorted order, and the out-of-grid bookkeeping (kept velocities into vel_s
