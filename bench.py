@@ -52,7 +52,7 @@ FALLBACK_HBM_GBS = 6800.0
 # the dominant kernel at that workload.
 TRAFFIC_STATE = "one launch at step 6 of the 2,097,152-particle dam break from the lattice at rest (ncu)"
 MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 212.000000e6 + 71.225088e6,
-                    "k_density": 81.821952e6 + 84.743680e6}
+                    "k_density": 94.954240e6 + 84.894976e6}
 
 
 def parse():
