@@ -351,20 +351,21 @@ __device__ __forceinline__ void cellpair_finish(const CellPairLane& L, const flo
     A.nbr[i] = L.cnt;
 }
 
-// Sorted particles a and, when has_b, a + 1 of the same cell.
+// Sorted particles a and, when has_b, a + 1 of the same cell (of one scene).
+template <class Scenes>
 __device__ __forceinline__ void density_cellpair(const uint32_t a, const bool has_b, const DensityArgs& A,
-                                                 const OneScene& R) {
-    const StepParams& P = R.P;
+                                                 const Scenes& R) {
+    const StepParams& P = R.params((int)a);
     const float4 pa = __ldg(A.pos_s + a);
     const int3 c = grid_cell(pa.x, pa.y, pa.z, P.gs_min, P.gs_delta);
-    if (!cell_fast(P, c)) {
+    if (R.frozen((int)a) || !cell_fast(P, c)) {
         density_pairs_one((int)a, A, R);
         if (has_b) density_pairs_one((int)a + 1, A, R);
         return;
     }
     const float4 pb = has_b ? __ldg(A.pos_s + a + 1) : pa;
-    const uint32_t* __restrict__ cs = A.cs0;
-    const uint32_t* __restrict__ ce = A.ce0;
+    const uint32_t* __restrict__ cs = A.cs0 + R.cell_base((int)a);
+    const uint32_t* __restrict__ ce = A.ce0 + R.cell_base((int)a);
     const float4* __restrict__ pxy = A.pxy;
     const float2* __restrict__ pz = A.pz;
     const uint32_t C = (uint32_t)P.nb_cells;
@@ -460,9 +461,16 @@ constexpr int cellpair_chunk() {
 // of its cell's part in that range starts an item (with the next particle
 // when it is in the same cell and the range); the items are compacted in
 // order and the block's threads take them in turn.
-template <int T>
+// Index into the cell arrays of sorted key `key` (a batch: the scene's
+// segment of them).
+__device__ __forceinline__ uint32_t key_cell(const OneScene&, uint32_t key) { return key; }
+__device__ __forceinline__ uint32_t key_cell(const ManyScenes& R, uint32_t key) {
+    return __ldg(R.cbase + (key >> R.cell_bits)) + (key & ((1u << R.cell_bits) - 1u));
+}
+
+template <int T, class Scenes>
 __global__ void __launch_bounds__(T, 1024 / T) k_density_cellpairs(const DensityArgs A, const int* __restrict__ info,
-                                                         const OneScene R) {
+                                                         const Scenes R) {
     constexpr int Cp = cellpair_chunk<T>();
     __shared__ uint32_t s_item[Cp];
     __shared__ uint32_t s_warp[2][T / 32];
@@ -480,7 +488,7 @@ __global__ void __launch_bounds__(T, 1024 / T) k_density_cellpairs(const Density
         start[h] = has_b[h] = false;
         if (p < end) {
             const uint32_t key = __ldg(A.keys + p);
-            const uint32_t cs = __ldg(A.cs0 + key);
+            const uint32_t cs = __ldg(A.cs0 + key_cell(R, key));
             const uint32_t first = cs > (uint32_t)base ? cs : (uint32_t)base;  // the cell's first particle in range
             start[h] = (((uint32_t)p - first) & 1u) == 0u;
             has_b[h] = start[h] && p + 1 < end && __ldg(A.keys + p + 1) == key;
@@ -545,12 +553,10 @@ void launch_density_tt(const float4* pos_s, const float4* veleval_s, float* dens
             const int pb = ((grid_items + 1) / 2 + 255) / 256;
             k_pack_pairs<<<pb < 1 ? 1 : pb, 256, 0, st>>>(pos_s, pxy, pz, info);
         }
-        if constexpr (std::is_same<Scenes, OneScene>::value) {
-            if (A.keys != nullptr) {
-                const int cp_blocks = (grid_items + cellpair_chunk<T>() - 1) / cellpair_chunk<T>();
-                k_density_cellpairs<T><<<cp_blocks < 1 ? 1 : cp_blocks, T, 0, st>>>(A, info, R);
-                return;
-            }
+        if (A.keys != nullptr) {
+            const int cp_blocks = (grid_items + cellpair_chunk<T>() - 1) / cellpair_chunk<T>();
+            k_density_cellpairs<T, Scenes><<<cp_blocks < 1 ? 1 : cp_blocks, T, 0, st>>>(A, info, R);
+            return;
         }
         k_density_pairs<T, Scenes><<<blocks, T, 0, st>>>(A, info, R);
         return;
@@ -656,8 +662,9 @@ void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* d
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                           const ManyScenes& scenes, bool unit, int exact, int grid_items, float4* pxy, float2* pz,
                           bool pack, int threads, cudaStream_t st) {
+    // the batch's sort leaves every particle's (scene, cell) key in scenes.keys
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     scenes, unit, exact != 0, grid_items, pxy, pz, pack, threads, st);
+                     scenes, unit, exact != 0, grid_items, pxy, pz, pack, threads, st, scenes.keys);
 }
 
 }  // namespace sphk
