@@ -88,6 +88,11 @@ def parse():
                     help="also time --steady-steps steps from this step of the rollout (0: skip)")
     ap.add_argument("--steady-steps", type=int, default=100)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--dump-state", default=None,
+                    help="step the dam break --dump-at steps from the lattice, save pos/vel/veleval (npz) and exit")
+    ap.add_argument("--dump-at", type=int, default=1000)
+    ap.add_argument("--init-state", default=None,
+                    help="start the cfg1 sections from a state saved by --dump-state instead of the lattice")
     return ap.parse_args()
 
 
@@ -576,8 +581,27 @@ def main():
     n = args.n
     sp, g, gs = abi.dambreak_params(n)
     pos0, vel0 = scenes.dambreak(n)
+    ve0 = np.zeros_like(pos0)
     s = SPH(sp, g, n, gs, exact=args.exact)
     lib = s.lib
+    if args.init_state:
+        # the scene's parameters and capacity stay those of args.n; the
+        # particle count is the saved state's (particles may have left)
+        st0 = np.load(args.init_state)
+        pos0, vel0, ve0 = st0["pos"], st0["vel"], st0["veleval"]
+        n = pos0.shape[0]
+    if args.dump_state:
+        # a later state of the same rollout, for profiling it without
+        # stepping up to it under the profiler
+        s.upload(pos0, vel0, ve0)
+        s.step(DT, args.dump_at)
+        s.sync()
+        m = s.getNum()
+        np.savez(args.dump_state, pos=s.get("pos_u", m), vel=s.get("vel_u", m), veleval=s.get("veleval_u", m))
+        if reps.rank == 0:
+            print(json.dumps({"dumped": args.dump_state, "steps": args.dump_at, "particles": m}))
+        s.close()
+        return
     # The library launches on this stream and the timing events are recorded
     # on it (a dedicated stream: the legacy default stream cannot host graphs).
     stream = torch.cuda.Stream()
@@ -589,7 +613,7 @@ def main():
 
     sampler = ClockSampler(torch.cuda.current_device())
     # --- device-resident throughput (graph replay) --------------------------
-    s.upload(pos0, vel0)
+    s.upload(pos0, vel0, ve0)
     s.step(DT, args.warmup)
     s.sync()
     # launch shapes: the autotuner times its candidates on this state (which
@@ -613,7 +637,7 @@ def main():
     num_after = s.getNum()
     # --- per-kernel breakdown over the same trajectory ------------------------
     psteps = args.profile_steps or args.steps
-    s.upload(pos0, vel0)
+    s.upload(pos0, vel0, ve0)
     s.step(DT, args.warmup)
     s.sync()
     cap = 16
@@ -641,7 +665,7 @@ def main():
     host = [p.numpy() for p in pin]
     host[0][:] = pos0
     host[1][:] = vel0
-    host[2][:] = 0
+    host[2][:] = ve0
     f_pos, f_vel, f_ve = abi.FIELDS["pos_u"], abi.FIELDS["vel_u"], abi.FIELDS["veleval_u"]
     s.upload(host[0], host[1], host[2])
     s.step(DT, 3)
@@ -661,7 +685,7 @@ def main():
     # neighbours per particle than near the lattice at rest) ------------------
     steady = None
     if args.steady_at > 0 and args.steady_steps > 0:
-        s.upload(pos0, vel0)
+        s.upload(pos0, vel0, ve0)
         s.step(DT, args.steady_at)
         s.sync()
         barrier()
@@ -697,7 +721,9 @@ def main():
         "metric": "particle-updates/s at 2M SPH", "value": value, "unit": "particle-updates/s", "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break lattice, zero initial velocity)",
-        "config": config_block(n, c, args.warmup, steps),
+        "config": dict(config_block(n, c, args.warmup, steps),
+                       **({"init_state": "%s (a saved later state of the same rollout; steps count from it)"
+                           % args.init_state} if args.init_state else {})),
         "e2e": {"value": e2e_value, "unit": "particle-updates/s",
                 "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n,
                 "note": "state (pos, vel, veleval) uploaded from and downloaded to pinned host memory every step; "
