@@ -81,6 +81,8 @@ SIGNATURES = {
     "sph_settings_round": (_F, [_F]),
     "sph_kernel_coefficients": (_I, [_F, C.POINTER(SPHParams)]),
     "sph_dambreak_params": (_I, [_I, _F, _F, C.POINTER(SPHParams), C.POINTER(GridParams), C.POINTER(GridParams)]),
+    "sph_params_from_settings": (_I, [_I, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(SPHParams),
+                                      C.POINTER(GridParams), C.POINTER(GridParams), C.POINTER(_F)]),
     "sph_create": (_I, [C.POINTER(SPHParams), C.POINTER(GridParams), C.POINTER(GridParams), _I, C.POINTER(_P)]),
     "sph_destroy": (_I, [_P]),
     "sph_set_params": (_I, [_P, C.POINTER(SPHParams)]),
@@ -232,3 +234,29 @@ def dambreak_params(n, viscosity=0.01, spacing=None):
     s = lattice_spacing(n) if spacing is None else spacing
     check(lib, None, lib.sph_dambreak_params(n, s, viscosity, C.byref(sp), C.byref(g), C.byref(gs)))
     return sp, g, gs
+
+
+def settings_value(v):
+    """A value as RTPSSettings::SetSetting stores it (`ostringstream << v`):
+    strings as they are, numbers with 6 significant digits, float4-like
+    sequences as their four lanes separated by spaces."""
+    if isinstance(v, str):
+        return v
+    if isinstance(v, (list, tuple)):
+        return " ".join(settings_value(x) for x in v)
+    if isinstance(v, (int, np.integer)) and not isinstance(v, bool):
+        return str(int(v))
+    return "%.6g" % float(v)
+
+
+def params_from_settings(settings, lib=None):
+    """(SPHParams, GridParams, GridParams scaled, spacing) of the SPH system the
+    reference builds from this settings map (sph_params_from_settings)."""
+    lib = lib if lib is not None else load_library()
+    items = [(str(k), settings_value(v)) for k, v in settings.items()]
+    keys = (C.c_char_p * max(len(items), 1))(*[k.encode() for k, _ in items])
+    vals = (C.c_char_p * max(len(items), 1))(*[v.encode() for _, v in items])
+    sp, g, gs, spacing = SPHParams(), GridParams(), GridParams(), C.c_float()
+    check(lib, None, lib.sph_params_from_settings(len(items), keys, vals, C.byref(sp), C.byref(g), C.byref(gs),
+                                                  C.byref(spacing)))
+    return sp, g, gs, spacing.value

@@ -6,10 +6,14 @@
 //                           (rtpslib/RTPSSettings.h:65-85)
 //   sph_kernel_coefficients SPH::calculate (rtpslib/system/SPHSettings.cpp:104-119)
 //   sph_dambreak_params     the dam-break parameter block of the benchmark scenes
+//   sph_params_from_settings the parameter block and grids an RTPSSettings
+//                           map gives an SPH system (SPH::SPH, SPH.cpp:50-58)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <string>
 
 #include "../../include/rtps_sph.h"
 
@@ -149,6 +153,143 @@ int sph_dambreak_params(int num, float spacing, float viscosity, SPHParams* sp, 
     rc = sph_setup_domain(&lo, &hi, p.smoothing_distance / p.simulation_scale, p.simulation_scale, grid, grid_scaled);
     if (rc) return rc;
     *sp = p;
+    return SPH_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The settings store of the reference (rtpslib/RTPSSettings.h:43-106): every
+// value is a string; SetSetting writes `ostringstream << value` (6
+// significant digits for float and double), GetSettingAs reads it back with
+// `istringstream >> T`, a missing key reading as "0".
+class SettingsMap {
+public:
+    void set(const std::string& k, const std::string& v) { m_[k] = v; }
+    void set_float(const std::string& k, float v) { m_[k] = fmt(v); }
+    void set_double(const std::string& k, double v) { m_[k] = fmt(v); }
+    const char* raw(const std::string& k) const {
+        auto it = m_.find(k);
+        return it == m_.end() ? "0" : it->second.c_str();
+    }
+    float f(const std::string& k) const { return std::strtof(raw(k), nullptr); }
+    long long i(const std::string& k) const { return std::strtoll(raw(k), nullptr, 10); }
+    // float4 reads four whitespace-separated floats (structs.h:549-553);
+    // components that are not there read as 0
+    sph_float4 f4v(const std::string& k) const {
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        const char* p = raw(k);
+        for (int c = 0; c < 4; ++c) {
+            char* end = nullptr;
+            const float x = std::strtof(p, &end);
+            if (end == p) break;
+            v[c] = x;
+            p = end;
+        }
+        return f4(v[0], v[1], v[2], v[3]);
+    }
+
+private:
+    static std::string fmt(double v) {
+        char buf[64];
+        std::snprintf(buf, sizeof(buf), "%.6g", v);
+        return buf;
+    }
+    std::map<std::string, std::string> m_;
+};
+
+}  // namespace
+
+extern "C" {
+
+int sph_params_from_settings(int count, const char* const* keys, const char* const* values, SPHParams* sp,
+                             GridParams* grid, GridParams* grid_scaled, float* spacing) {
+    if (count < 0 || (count > 0 && (!keys || !values)) || !sp || !grid) return SPH_EINVAL;
+    SettingsMap S;
+    for (int k = 0; k < count; ++k) {
+        if (!keys[k] || !values[k]) return SPH_EINVAL;
+        S.set(keys[k], values[k]);  // a later entry of a key replaces an earlier one
+    }
+    // SPH::calculate (SPHSettings.cpp:30-144).  Its file sees std:: through a
+    // using-directive, so log and pow are the float overloads.
+    const float rho0 = S.f("rest_density");
+    const long long max_ll = S.i("max_num_particles");
+    if (!(rho0 > 0.f) || max_ll < 2 || max_ll > 0x7fffffffLL) return SPH_EINVAL;
+    const unsigned max_num = (unsigned)max_ll;
+    const int log2n = (int)(std::log((float)max_num) / std::log(2.0f));
+    const float mass = (float)(0.0256 / log2n);
+    const float VP = mass / rho0;
+    const float rest_distance = (float)(.87 * std::pow(mass / rho0, 1.f / 3.f));
+    const float smoothing_distance = 2.0f * rest_distance;
+    // the domain of System::System (System.cpp:62): the boundary box
+    const sph_float4 dmin = S.f4v("domain_min"), dmax = S.f4v("domain_max");
+    const float domain_vol = ((dmax.x - dmin.x) * (dmax.y - dmin.y) * (dmax.z - dmin.z)) / 2;
+    if (!(domain_vol > 0.f) || !std::isfinite(domain_vol)) return SPH_EINVAL;
+    const float simulation_scale = std::pow(.5f * VP * (float)max_num / domain_vol, 1.f / 3.f);
+    S.set_float("mass", mass);
+    S.set_float("rest_distance", rest_distance);
+    S.set_float("smoothing_distance", smoothing_distance);
+    S.set_float("simulation_scale", simulation_scale);
+    S.set_float("boundary_distance", .5f * rest_distance);
+    S.set_float("spacing", rest_distance / simulation_scale);
+    {
+        // the kernel coefficients from the unrounded smoothing distance
+        if (!(smoothing_distance > 0.f) || !std::isfinite(smoothing_distance)) return SPH_EINVAL;
+        const float pi = (float)M_PI;
+        const float h9 = std::pow(smoothing_distance, 9.f), h6 = std::pow(smoothing_distance, 6.f),
+                    h3 = std::pow(smoothing_distance, 3.f);
+        S.set_float("wpoly6", 315.f / 64.0f / pi / h9);
+        S.set_float("wpoly6_d", -945.f / (32.0f * pi * h9));
+        S.set_float("wpoly6_dd", -945.f / (32.0f * pi * h9));
+        S.set_float("wspiky", 15.f / pi / h6);
+        S.set_float("wspiky_d", -45.f / (pi * h6));
+        S.set_double("wspiky_dd", 15. / (2. * pi * h3));
+        S.set_double("wvisc", 15. / (2. * pi * h3));
+        S.set_double("wvisc_d", 15. / (2. * pi * h3));
+        S.set_double("wvisc_dd", 45. / (pi * h6));
+    }
+    S.set_double("epsilon", 1E-6);
+    S.set("num_particles", "0");
+    // SPH::updateParams (SPHSettings.cpp:150-199)
+    SPHParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.rest_density = S.f("rest_density");
+    p.mass = S.f("mass");
+    p.rest_distance = S.f("rest_distance");
+    p.smoothing_distance = S.f("smoothing_distance");
+    p.simulation_scale = S.f("simulation_scale");
+    p.boundary_stiffness = S.f("boundary_stiffness");
+    p.boundary_dampening = S.f("boundary_dampening");
+    p.boundary_distance = S.f("boundary_distance");
+    p.K = S.f("gas_constant");
+    p.viscosity = S.f("viscosity");
+    p.velocity_limit = S.f("velocity_limit");
+    p.xsph_factor = S.f("xsph_factor");
+    p.gravity = S.f4v("gravity");
+    p.friction_coef = S.f("friction_kinetic");
+    p.restitution_coef = S.f("restitution");
+    p.shear = S.f("shear");
+    p.attraction = S.f("attraction");
+    p.spring = S.f("spring");
+    p.EPSILON = S.f("epsilon");
+    p.wpoly6_coef = S.f("wpoly6");
+    p.wpoly6_d_coef = S.f("wpoly6_d");
+    p.wpoly6_dd_coef = S.f("wpoly6_dd");
+    p.wspiky_coef = S.f("wspiky");
+    p.wspiky_d_coef = S.f("wspiky_d");
+    p.wspiky_dd_coef = S.f("wspiky_dd");
+    p.wvisc_coef = S.f("wvisc");
+    p.wvisc_d_coef = S.f("wvisc_d");
+    p.wvisc_dd_coef = S.f("wvisc_dd");
+    p.num = (int)S.i("num_particles");
+    p.max_num = (int)S.i("max_num_particles");
+    // System::setupDomain(h / scale, scale) (SPH.cpp:58, System.cpp:294-329)
+    const int rc = sph_setup_domain(&dmin, &dmax, p.smoothing_distance / p.simulation_scale, p.simulation_scale,
+                                    grid, grid_scaled);
+    if (rc) return rc;
+    *sp = p;
+    if (spacing) *spacing = S.f("spacing");  // SPH::spacing (SPH.cpp:66)
     return SPH_OK;
 }
 

@@ -20,6 +20,13 @@
 //   sph_bench --add-rect NUM SPACING SCALE LX LY LZ HX HY HZ FILE: write
 //             rtps::addRect(NUM, lo, hi, SPACING, SCALE) (k x 4 float32) to
 //             FILE and exit (no GPU needed).
+//   sph_bench --settings FILE --box NUM LX LY LZ HX HY HZ [--steps S]
+//             [--out-init FILE] [--out FILE]: the reference's construction
+//             path: an RTPSSettings filled from FILE (one setting per line,
+//             the key then its value), rtps::SPH(&settings), addBox(NUM, lo,
+//             hi), then S frames of update()+integrate(); writes the
+//             positions after addBox and after the frames (N x 4 float32) and
+//             prints the derived parameters and a checksum.
 //   sph_bench --n N --add-box NUM SCALE LX LY LZ HX HY HZ FILE: a system with
 //             the dam-break parameters of N particles and simulation_scale
 //             SCALE, filled by SPH::addBox(NUM, lo, hi, false); writes its
@@ -110,6 +117,7 @@ int main(int argc, char** argv) {
     float dt = 0.001f, mu = 0.01f;
     std::string dump, box_file;
     int box_num = -1, rect_only = 0;
+    std::string settings_file, out_init, out_final;
     float box_spacing = 0.f, box_scale = 1.f;
     rtps::float4 box_lo = rtps::make_float4(0, 0, 0, 0), box_hi = box_lo;
     for (int i = 1; i < argc; ++i) {
@@ -131,6 +139,16 @@ int main(int argc, char** argv) {
         else if (a == "--dump-scene") dump = next();
         else if (a == "--mesh") mesh = 1;
         else if (a == "--post-process") post_res = std::atoi(next());
+        else if (a == "--settings") settings_file = next();
+        else if (a == "--out-init") out_init = next();
+        else if (a == "--out") out_final = next();
+        else if (a == "--box") {
+            box_num = std::atoi(next());
+            float v[6];
+            for (float& x : v) x = (float)std::atof(next());
+            box_lo = rtps::make_float4(v[0], v[1], v[2], 0.f);
+            box_hi = rtps::make_float4(v[3], v[4], v[5], 0.f);
+        }
         else if (a == "--add-rect" || a == "--add-box") {
             rect_only = a == "--add-rect";
             box_num = std::atoi(next());
@@ -161,6 +179,46 @@ int main(int argc, char** argv) {
         return std::fclose(f) == 0 && ok;
     };
     if (rect_only) return write_f4(box_file, rtps::addRect(box_num, box_lo, box_hi, box_spacing, box_scale)) ? 0 : 1;
+    if (!settings_file.empty()) {
+        // the reference's test applications: settings from a file, the
+        // system RTPS::generateSystemInstance makes of them, one box of
+        // particles, then the frame loop
+        rtps::RTPSSettings settings;
+        FILE* f = std::fopen(settings_file.c_str(), "r");
+        if (!f) return 1;
+        char line[1024];
+        while (std::fgets(line, sizeof(line), f)) {
+            std::string l(line);
+            while (!l.empty() && (l.back() == '\n' || l.back() == '\r')) l.pop_back();
+            const size_t sp0 = l.find(' ');
+            if (l.empty() || sp0 == std::string::npos) continue;
+            settings.SetSetting(l.substr(0, sp0), l.substr(sp0 + 1));
+        }
+        std::fclose(f);
+        try {
+            rtps::SPH sph(&settings);
+            const int added = sph.addBox(box_num, box_lo, box_hi, false);
+            if (!out_init.empty() && !write_f4(out_init, sph.getPositions())) return 1;
+            for (int s = 0; s < steps; ++s) {
+                sph.update();
+                sph.integrate();
+            }
+            const std::vector<rtps::float4> p = sph.getPositions();
+            if (!out_final.empty() && !write_f4(out_final, p)) return 1;
+            double sum = 0.0;
+            for (const rtps::float4& q : p) sum += (double)q.x + 2.0 * q.y + 3.0 * q.z;
+            const SPHParams prm = sph.params();
+            std::printf("{\"added\": %d, \"num\": %d, \"spacing\": %.9g, \"mass\": %.9g, \"rest_distance\": %.9g, "
+                        "\"smoothing_distance\": %.9g, \"simulation_scale\": %.9g, \"max_num\": %d, "
+                        "\"checksum\": %.17g}\n",
+                        added, sph.getNum(), (double)sph.getSpacing(), (double)prm.mass, (double)prm.rest_distance,
+                        (double)prm.smoothing_distance, (double)prm.simulation_scale, prm.max_num, sum);
+        } catch (const rtps::SPHError& e) {
+            std::fprintf(stderr, "error %d: %s\n", e.code(), e.what());
+            return 1;
+        }
+        return 0;
+    }
     SPHParams sp;
     GridParams g, gs;
     if (sph_dambreak_params(n, lattice_spacing(n), mu, &sp, &g, &gs) != SPH_OK) {

@@ -170,6 +170,22 @@ int sph_kernel_coefficients(float h, SPHParams* sphp);
 int sph_dambreak_params(int num, float spacing, float viscosity,
                         SPHParams* sphp, GridParams* grid, GridParams* grid_scaled);
 
+/* The parameter block and grids the reference gives an SPH system built from
+ * its settings map (RTPS::generateSystemInstance -> SPH::SPH, SPH.cpp:50-58):
+ * SPH::calculate (SPHSettings.cpp:30-144), SPH::updateParams (:150-199) and
+ * System::setupDomain (System.cpp:294-329), with every derived value passed
+ * through the map's 6-significant-digit strings (RTPSSettings.h:65-85).
+ * keys/values: count (key, value) strings as an RTPSSettings holds them (a
+ * later entry of a key replaces an earlier one; a missing key reads as "0").
+ * The path reads rest_density, max_num_particles (>= 2), domain_min and
+ * domain_max ("x y z w"), gas_constant, viscosity, velocity_limit,
+ * xsph_factor, gravity ("x y z w"), boundary_stiffness, boundary_dampening,
+ * friction_kinetic, restitution, shear, attraction, spring.  spacing
+ * (nullable) receives SPH::spacing, the lattice spacing System::addBox
+ * uses.  SPH_EINVAL for a non-positive rest density or domain volume. */
+int sph_params_from_settings(int count, const char* const* keys, const char* const* values, SPHParams* sphp,
+                             GridParams* grid, GridParams* grid_scaled, float* spacing);
+
 /* ---------------------------------------------------------------------------
  * Context lifetime (System::System / SPH::SPH / prepareSorted,
  * System.cpp:47-89,198-291, SPH.cpp:50-99,482-520).

@@ -11,6 +11,8 @@
 #ifndef RTPS_SPH_HPP
 #define RTPS_SPH_HPP
 
+#include <map>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -65,6 +67,51 @@ inline std::vector<float4> addRect(int num, float4 min, float4 max, float spacin
     return rvec;
 }
 
+// The reference's settings store (rtpslib/RTPSSettings.h:43-106): every
+// value is a string, SetSetting writes `ostringstream << value`, GetSettingAs
+// reads it with `istringstream >> T`, and a missing key reads as the default
+// ("0").  A float4 is written and read as its four lanes, space separated.
+class RTPSSettings {
+public:
+    template <class T>
+    void SetSetting(const std::string& key, const T& value) {
+        std::ostringstream os;
+        os << value;
+        settings_[key] = os.str();
+        changed_ = true;
+    }
+    void SetSetting(const std::string& key, const float4& v) {
+        std::ostringstream os;
+        os << v.x << " " << v.y << " " << v.z << " " << v.w;
+        settings_[key] = os.str();
+        changed_ = true;
+    }
+    template <class T>
+    T GetSettingAs(const std::string& key, const std::string& defaultval = "0") const {
+        auto it = settings_.find(key);
+        std::istringstream is(it == settings_.end() ? defaultval : it->second);
+        T v{};
+        is >> v;
+        return v;
+    }
+    bool Exists(const std::string& key) const { return settings_.count(key) != 0; }
+    bool hasChanged() const { return changed_; }
+    void updated() { changed_ = false; }
+    const std::map<std::string, std::string>& entries() const { return settings_; }
+
+private:
+    std::map<std::string, std::string> settings_;
+    bool changed_ = false;
+};
+template <>
+inline float4 RTPSSettings::GetSettingAs<float4>(const std::string& key, const std::string& defaultval) const {
+    auto it = settings_.find(key);
+    std::istringstream is(it == settings_.end() ? defaultval : it->second);
+    float4 v = make_float4(0, 0, 0, 0);
+    is >> v.x >> v.y >> v.z >> v.w;
+    return v;
+}
+
 class SPH {
 public:
     // The reference builds its parameters from a settings map
@@ -76,6 +123,30 @@ public:
         check(sph_create(&sphp, &grid, grid_scaled, max_num, &ctx_), nullptr);
         max_num_ = max_num;
     }
+    // SPH::SPH(RTPSSettings*, CL*) (SPH.cpp:50-98), as
+    // RTPS::generateSystemInstance builds it for system "sph": the
+    // parameters of SPH::calculate / updateParams and the grid of
+    // System::setupDomain from the settings (sph_params_from_settings), the
+    // integrator of the "integrator" setting and the "time_step" setting's dt.
+    explicit SPH(const RTPSSettings* settings) {
+        std::vector<const char*> keys, values;
+        for (const auto& kv : settings->entries()) {
+            keys.push_back(kv.first.c_str());
+            values.push_back(kv.second.c_str());
+        }
+        SPHParams sphp;
+        GridParams grid, grid_scaled;
+        float spacing = 0.f;
+        check(sph_params_from_settings((int)keys.size(), keys.data(), values.data(), &sphp, &grid, &grid_scaled,
+                                       &spacing),
+              nullptr);
+        check(sph_create(&sphp, &grid, &grid_scaled, sphp.max_num, &ctx_), nullptr);
+        max_num_ = sphp.max_num;
+        spacing_ = spacing;
+        dt_ = settings->GetSettingAs<float>("time_step");
+        const std::string integ = settings->GetSettingAs<std::string>("integrator", "");
+        if (integ == "euler") check(sph_set_integrator(ctx_, SPH_INTEGRATOR_EULER));
+    }
     ~SPH() {
         if (ctx_) sph_destroy(ctx_);
     }
@@ -85,6 +156,7 @@ public:
         : ctx_(o.ctx_),
           max_num_(o.max_num_),
           dt_(o.dt_),
+          spacing_(o.spacing_),
           color_field_(o.color_field_),
           color_field_res_(o.color_field_res_) {
         o.ctx_ = nullptr;
@@ -129,6 +201,7 @@ public:
     // SPH::calculate as rest_distance / simulation_scale (SPHSettings.cpp:
     // 94-96) and read back through the settings map (6 significant digits).
     float getSpacing() {
+        if (spacing_ > 0.f) return spacing_;  // built from settings: SPH::calculate's own value
         SPHParams p = params();
         return sph_settings_round(p.rest_distance / p.simulation_scale);
     }
@@ -232,6 +305,7 @@ private:
     sph_ctx* ctx_ = nullptr;
     int max_num_ = 0;
     float dt_ = 0.001f;
+    float spacing_ = 0.f;  // the "spacing" setting when built from settings
     bool color_field_ = false;
     int color_field_res_ = 2;
 };

@@ -24,7 +24,9 @@ plain arithmetic, though, so this recipe compiles them for the host with g++:
   3. compile them with clshim.hpp (vector types, built-ins, barrier) and the
      ref_*.cpp drivers, plus the reference's host Domain.cpp / IV.cpp /
      structs.cpp unchanged (and its Hose.cpp, included unchanged by
-     ref_hose.cpp), into oracle/_ref/librtps_ref.so.  -ffp-contract=off keeps
+     ref_hose.cpp; its RTPSSettings.cpp and a scratch copy of
+     system/SPHSettings.cpp, included unchanged by ref_settings.cpp, the
+     copy's SPH.h being sph_settings_shim.h), into oracle/_ref/librtps_ref.so.  -ffp-contract=off keeps
      every multiply and add separately rounded, as written.
 
 The temporary copies are deleted; only the shared library is kept, under
@@ -51,7 +53,11 @@ SPH = ["density.cl", "force.cl", "collision_wall.cl", "collision_tri.cl", "leapf
 DRIVERS = ["ref_runtime.cpp", "ref_hash.cpp", "ref_bitonic.cpp", "ref_cellindices.cpp", "ref_permute.cpp",
            "ref_density.cpp", "ref_force.cpp", "ref_collision.cpp", "ref_leapfrog.cpp", "ref_domain.cpp",
            "ref_gravity.cpp", "ref_euler.cpp", "ref_collision_tri.cpp", "ref_hose.cpp",
-           "ref_colorfield.cpp", "ref_marching_cubes.cpp"]
+           "ref_colorfield.cpp", "ref_marching_cubes.cpp", "ref_settings.cpp"]
+# SPH::calculate / updateParams: compiled from a scratch copy beside which
+# the shim below is written as SPH.h (the real SPH.h needs the OpenCL system)
+SETTINGS_SRC = os.path.join("system", "SPHSettings.cpp")
+SETTINGS_SHIM = "sph_settings_shim.h"
 
 VEC_LITERAL = re.compile(r"\((float4|int4|float3|int2)\)\s*\(")
 LOCAL_ARRAY = re.compile(r"^(\s*)__local(\s+\w+\s+\w+\s*\[)", re.M)
@@ -93,6 +99,8 @@ def build(reference, verbose=False):
                     text = f.read()
                 with open(os.path.join(tmp, sub, name), "w") as f:
                     f.write(rewrite(text))
+        shutil.copyfile(os.path.join(rtpslib, SETTINGS_SRC), os.path.join(tmp, "SPHSettings.cpp"))
+        shutil.copyfile(os.path.join(HERE, SETTINGS_SHIM), os.path.join(tmp, "SPH.h"))
         cxx = os.environ.get("CXX", "g++")
         cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
                "-w", "-I", tmp, "-I", HERE, "-I", rtpslib]

@@ -26,6 +26,12 @@ void ref_setup_domain(const float* bnd_min, const float* bnd_max, float cell_siz
                       void* grid_scaled);
 }
 
+// SPH::calculate + SPH::updateParams + System::setupDomain over a settings
+// map (rtpslib/system/SPHSettings.cpp, RTPSSettings.cpp); returns
+// sizeof(SPHParams) of the reference's struct.
+extern "C" int ref_params_from_settings(int count, const char* const* keys, const char* const* values, void* sphp,
+                                        void* grid, void* grid_scaled, float* spacing);
+
 // Hose (rtpslib/system/common/Hose.cpp): create, spray, update, refill.
 extern "C" void* ref_hose_create(float dt, int total_n, const float* center, const float* velocity, float radius,
                                  float spacing);

@@ -33,6 +33,12 @@ Fixtures
   addrect.npz        the reference's addRect (domain/IV.cpp) for the boxes of
                      tests/addrect_cases.py at the getSpacing() of each
                      system (System::addBox): the spacing and the points
+  settings.npz       the reference's settings path (RTPSSettings.cpp,
+                     SPHSettings.cpp SPH::calculate / updateParams,
+                     Domain::calculateCells as System::setupDomain drives
+                     it) for the settings maps of tests/settings_cases.py:
+                     the keys and values, the SPHParams and both GridParams
+                     bytes and the spacing
 Usage: python tests/golden/make_golden.py [--only NAME ...]
 """
 import ctypes as C
@@ -220,6 +226,21 @@ def hose_fixture():
     return out
 
 
+def settings_fixture():
+    import settings_cases
+    out = {}
+    for name, settings in settings_cases.CASES:
+        items = [(k, abi.settings_value(v)) for k, v in settings.items()]
+        sp, g, gs, spacing, size = ref_driver.params_from_settings(items)
+        out[name + "/keys"] = np.array([k for k, _ in items])
+        out[name + "/values"] = np.array([v for _, v in items])
+        out[name + "/sphp"] = np.frombuffer(sp, np.uint8).copy()
+        out[name + "/grid"] = np.frombuffer(g, np.uint8).copy()
+        out[name + "/grid_scaled"] = np.frombuffer(gs, np.uint8).copy()
+        out[name + "/spacing"] = np.float32(spacing)
+    return out
+
+
 def addrect_fixture():
     import addrect_cases
     import oracle_bind
@@ -242,6 +263,7 @@ FIXTURES = {
     "hose_sprays.npz": hose_fixture,
     "surface_n4096.npz": surface_fixture,
     "addrect.npz": addrect_fixture,
+    "settings.npz": settings_fixture,
 }
 
 

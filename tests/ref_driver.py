@@ -140,3 +140,18 @@ class RefSystem:
         for _ in range(nsteps):
             self.update()
             self.integrate(dt)
+
+
+def params_from_settings(items):
+    """The reference's settings path (ref_params_from_settings) for (key,
+    value) string pairs: SPHParams bytes (the reference struct's size), both
+    GridParams bytes, the spacing and the struct size."""
+    lib = ob.ref()
+    keys = (C.c_char_p * max(len(items), 1))(*[k.encode() for k, _ in items])
+    vals = (C.c_char_p * max(len(items), 1))(*[v.encode() for _, v in items])
+    sp = (C.c_uint8 * 256)()
+    g = (C.c_uint8 * 128)()
+    gs = (C.c_uint8 * 128)()
+    spacing = C.c_float()
+    size = lib.ref_params_from_settings(len(items), keys, vals, sp, g, gs, C.byref(spacing))
+    return bytes(sp)[:size], bytes(g), bytes(gs), spacing.value, size

@@ -75,6 +75,10 @@ def test_parameter_helpers_without_gpu(lib):
 
 def test_cpp_class_compiles():
     src = ("#include \"rtps_sph.hpp\"\nint main() { SPHParams p; GridParams g; rtps::SPH* s = nullptr;\n"
+           "rtps::RTPSSettings set; set.SetSetting(\"rest_density\", 1000.0f);\n"
+           "set.SetSetting(\"domain_min\", rtps::make_float4(0, 0, 0, 1));\n"
+           "(void)set.GetSettingAs<float>(\"rest_density\"); (void)set.GetSettingAs<rtps::float4>(\"domain_min\");\n"
+           "if (s) { rtps::SPH t(&set); (void)t.getSpacing(); }\n"
            "if (s) { s->update(); s->interact(); s->integrate(); s->postProcess(); s->acquireGLBuffers();\n"
            "s->releaseGLBuffers(); s->addBox(10, rtps::make_float4(0,0,0,1), rtps::make_float4(1,1,1,1), false);\n"
            "(void)s->getNum(); (void)s->getDeletedPos(); }\n(void)p; (void)g; return 0; }\n")
