@@ -26,6 +26,33 @@ class SPH:
         if exact:
             self.set_exact(True)
 
+    @classmethod
+    def from_settings(cls, settings, exact=False, lib=None):
+        """The system the reference builds from a settings map (SPH::SPH,
+        SPH.cpp:50-98; System::System, System.cpp:54-62, 260-272): the
+        parameter block and grid of SPH::calculate / updateParams /
+        System::setupDomain, the "integrator" setting and the point sources
+        of gravity_sources / gravity_mass / gravity_alphas.  Returns the
+        system and its "time_step"."""
+        sp, g, gs, spacing = abi.params_from_settings(settings, lib=lib)
+        s = cls(sp, g, sp.max_num, gs, exact=exact, lib=lib)
+        s.spacing = spacing
+        if str(settings.get("integrator", "")) == "euler":
+            s.setIntegrator("euler")
+        if "gravity_sources" in settings:
+            p = np.array(abi.settings_value(settings["gravity_sources"]).split(), np.float32)
+            m = np.array(abi.settings_value(settings.get("gravity_mass", "")).split(), np.float32)
+            a = np.array(abi.settings_value(settings.get("gravity_alphas", "")).split(), np.float32)
+            ns = len(p) // 4
+            if ns > 0:
+                mass = np.zeros(ns, np.float32)
+                alpha = np.zeros(ns, np.float32)
+                mass[:min(ns, len(m))] = m[:ns]
+                alpha[:min(ns, len(a))] = a[:ns]
+                s.setGravitySources(p[:4 * ns].reshape(ns, 4), mass, alpha)
+        dt = float(np.float32(abi.settings_value(settings.get("time_step", "0"))))
+        return s, dt
+
     # -- lifetime ---------------------------------------------------------
     def close(self):
         if self.ctx:

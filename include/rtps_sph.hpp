@@ -146,6 +146,25 @@ public:
         dt_ = settings->GetSettingAs<float>("time_step");
         const std::string integ = settings->GetSettingAs<std::string>("integrator", "");
         if (integ == "euler") check(sph_set_integrator(ctx_, SPH_INTEGRATOR_EULER));
+        // point sources (System::System, System.cpp:260-272): the settings
+        // gravity_sources (x y z w per source), gravity_mass, gravity_alphas
+        if (settings->Exists("gravity_sources")) {
+            const std::vector<float> p = floats(settings->entries().at("gravity_sources"));
+            const std::vector<float> m =
+                settings->Exists("gravity_mass") ? floats(settings->entries().at("gravity_mass")) : std::vector<float>();
+            const std::vector<float> a = settings->Exists("gravity_alphas")
+                                             ? floats(settings->entries().at("gravity_alphas"))
+                                             : std::vector<float>();
+            const int ns = (int)(p.size() / 4);
+            if (ns > 0) {
+                std::vector<float4> pts(ns);
+                for (int k = 0; k < ns; ++k) pts[k] = make_float4(p[4 * k], p[4 * k + 1], p[4 * k + 2], p[4 * k + 3]);
+                std::vector<float> mass(ns, 0.f), alpha(ns, 0.f);
+                for (int k = 0; k < ns && k < (int)m.size(); ++k) mass[k] = m[k];
+                for (int k = 0; k < ns && k < (int)a.size(); ++k) alpha[k] = a[k];
+                check(sph_set_gravity_sources(ctx_, ns, pts.data(), mass.data(), alpha.data()));
+            }
+        }
     }
     ~SPH() {
         if (ctx_) sph_destroy(ctx_);
@@ -303,6 +322,15 @@ private:
     }
 
     sph_ctx* ctx_ = nullptr;
+    // the whitespace-separated floats of a setting (structs.h:594-603)
+    static std::vector<float> floats(const std::string& text) {
+        std::istringstream is(text);
+        std::vector<float> v;
+        float x;
+        while (is >> x) v.push_back(x);
+        return v;
+    }
+
     int max_num_ = 0;
     float dt_ = 0.001f;
     float spacing_ = 0.f;  // the "spacing" setting when built from settings
