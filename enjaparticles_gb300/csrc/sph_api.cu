@@ -324,13 +324,17 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
 // pass.  pack: the
 // position pairs of the default arithmetic are written from pos_s first
 // (the stage API's permutes do not write them; the counting sort's does).
-void density_launch(sph_ctx* c, bool fused, cudaStream_t st, bool pack = false) {
-    // the fused step's sort leaves the sorted cell keys in keys_a, which the
-    // default arithmetic's cell-pair pass reads
+// sorted_keys: the cell key of every sorted particle, as the counting sort
+// of the same enqueue wrote it (keys_a), for the default arithmetic's
+// cell-pair pass; null where the keys are not known to match pos_s (the
+// stage API's density, which the caller may run after any stage), which
+// then takes the one-particle pass.
+void density_launch(sph_ctx* c, bool fused, cudaStream_t st, bool pack = false,
+                    const uint32_t* sorted_keys = nullptr) {
     sphk::launch_density(c->pos_s, fused ? nullptr : c->veleval_s, c->density, c->rec_pd, c->rec_vi,
                          c->nbr, c->mask,
                          (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, c->pos_xy,
-                         c->pos_z, pack, c->lc.density_threads, st, fused ? c->keys_a : nullptr);
+                         c->pos_z, pack, c->lc.density_threads, st, sorted_keys);
 }
 
 void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {
@@ -349,7 +353,7 @@ static int enqueue_to_force(sph_ctx* c) {
     if (rc) return rc;
     sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
                                c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
-    density_launch(c, false, c->stream);
+    density_launch(c, false, c->stream, false, c->keys_a);
     force_launch(c, c->idx_a, false, 0.f, c->stream);
     return SPH_OK;
 }
@@ -376,7 +380,7 @@ int enqueue_fused_step(sph_ctx* c, float dt) {
     // triangle kernel reads)
     CK(c, cudaEventRecord(c->side_fork, c->stream));
     CK(c, cudaStreamWaitEvent(c->side_stream, c->side_fork, 0));
-    density_launch(c, true, c->stream);
+    density_launch(c, true, c->stream, false, c->keys_a);
     if ((rc = join_upload_on(c, c->side_stream))) return rc;
     sphk::launch_step_velocities(c->pos_s, c->idx_a, c->vel_u, c->veleval_u, c->rec_vi, c->vel_s, c->del_pos,
                                  c->del_vel, c->info, mesh ? 1 : 0, c->num_hint, c->side_stream);
@@ -1136,7 +1140,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
                                   c->vel_u, c->veleval_u, c->pos_s, c->vel_s, c->veleval_s, c->info, c->num_hint, 0,
                                   c->pos_xy, c->pos_z, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        density_launch(c, true, st);
+        density_launch(c, true, st, false, c->keys_a);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_step_velocities(c->pos_s, c->idx_a, c->vel_u, c->veleval_u, c->rec_vi, c->vel_s, c->del_pos,
                                      c->del_vel, c->info, 0, c->num_hint, st);

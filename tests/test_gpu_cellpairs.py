@@ -1,7 +1,8 @@
-"""The fused step's density pass in the default arithmetic takes two particles
-of one cell per thread (k_density_cellpairs); the staged density pass takes
-one (k_density_pairs).  Both must give the same densities and neighbour
-counts bit for bit, whatever the cells hold: the dam-break lattice, odd and
+"""The density pass of the graph step and of sph_update takes, in the default
+arithmetic, two particles of one cell per thread (k_density_cellpairs); the
+stage API's density pass takes one (k_density_pairs).  They must give the
+same sorted positions, densities and neighbour counts bit for bit, whatever
+the cells hold: the dam-break lattice, odd and
 even cell counts, cells cut by the pass's 128/256/512-particle block
 ranges, a crowded cell (more candidates than the neighbour bitmask holds),
 particles outside the grid, and particle counts of 1, 2 and 3.  The neighbour
@@ -28,25 +29,53 @@ def _layout(n, seed, crowd):
     return pos, vel
 
 
-def _fused_and_staged(sp, g, gs, pos, vel, threads):
+def _density_by_path(sp, g, gs, pos, vel, threads):
+    """(pos_s, density_s, neighbour counts) of the in-grid particles after
+    the density pass of: the graph step and sph_update (two particles of a
+    cell per thread), and the stage API's passes run one by one (one
+    particle per thread)."""
     n = pos.shape[0]
-    out = []
-    for staged in (False, True):
+    out = {}
+    for path in ("step", "update", "stages"):
         s = SPH(sp, g, n, gs)
         cfg = list(s.launch_config())
         cfg[0] = threads
         s.set_launch_config(*cfg)
         s.upload(pos, vel)
-        if staged:
-            s.update()  # hash, sort, cellindices, permute, density (one particle per thread), force
+        if path == "step":
+            s.step(DT, 1)
+        elif path == "update":
+            s.update()
         else:
-            s.step(DT, 1)  # the graph step: density with two particles of a cell per thread
+            s.hash()
+            s.sort()
+            s.cellindices()
+            s.permute()
+            s.density()
         s.sync()
-        m = s.getNum() if staged else n
-        k = min(m, n)
-        out.append((s.get("pos_s", k), s.get("density_s", k), s.get("neighbor_count", k)))
+        out[path] = (s.get("pos_s", n), s.get("density_s", n), s.get("neighbor_count", n))
         s.close()
     return out
+
+
+def _in_grid(sp, g, gs, pos):
+    """Particles whose cell key is inside the grid (the ones the density
+    pass walks for)."""
+    s = SPH(sp, g, pos.shape[0], gs)
+    s.upload(pos, np.zeros_like(pos))
+    s.hash()
+    keys = s.get("sort_hashes", pos.shape[0])
+    s.close()
+    return int((keys < g.nb_cells).sum())
+
+
+def _check(sp, g, gs, pos, vel, threads):
+    k = _in_grid(sp, g, gs, pos)
+    out = _density_by_path(sp, g, gs, pos, vel, threads)
+    ref = out["stages"]
+    for path in ("step", "update"):
+        for got, want in zip(out[path], ref):
+            np.testing.assert_array_equal(got[:k], want[:k], err_msg=path)
 
 
 @pytest.mark.parametrize("threads", [128, 256, 512])
@@ -54,18 +83,11 @@ def test_dam_break_lattice(threads):
     n = 16384
     sp, g, gs = abi.dambreak_params(n)
     pos, vel = scenes.dambreak(n, velocity_sigma=0.1)
-    (p0, d0, c0), (p1, d1, c1) = _fused_and_staged(sp, g, gs, pos, vel, threads)
-    np.testing.assert_array_equal(p0, p1)
-    np.testing.assert_array_equal(d0, d1)
-    np.testing.assert_array_equal(c0, c1)
+    _check(sp, g, gs, pos, vel, threads)
 
 
 @pytest.mark.parametrize("n,crowd", [(60001, 7), (4097, 0), (3, 0), (2, 0), (1, 0)])
 def test_ragged_crowded_and_outside(n, crowd):
     sp, g, gs = abi.dambreak_params(max(n, 4096))
     pos, vel = _layout(n, 100 + n, crowd)
-    (p0, d0, c0), (p1, d1, c1) = _fused_and_staged(sp, g, gs, pos, vel, 256)
-    k = min(len(d0), len(d1))
-    np.testing.assert_array_equal(p0[:k], p1[:k])
-    np.testing.assert_array_equal(d0[:k], d1[:k])
-    np.testing.assert_array_equal(c0[:k], c1[:k])
+    _check(sp, g, gs, pos, vel, 256)
