@@ -53,6 +53,12 @@ FALLBACK_HBM_GBS = 6800.0
 TRAFFIC_STATE = "one launch at step 6 of the 2,097,152-particle dam break from the lattice at rest (ncu)"
 MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 212.000000e6 + 71.225088e6,
                     "k_density": 94.954240e6 + 84.894976e6}
+# The same captures' instruction-issue roofline, the bound these neighbour
+# passes meet first: warp instructions (smsp__inst_executed.sum) over the 4
+# an SM can issue per cycle in the launch's SM cycles (sm__cycles_elapsed.avg),
+# on 152 SMs.
+MEASURED_ISSUE = {"k_force(fused collision+leapfrog)": (270365581, 607770.96),
+                  "k_density": (197453326, 505033.82)}
 
 
 def parse():
@@ -734,6 +740,8 @@ def main():
                      "frac": achieved / peak,
                      "traffic": MEASURED_TRAFFIC.get(dom) if n == N_DEFAULT else None,
                      "traffic_state": TRAFFIC_STATE if n == N_DEFAULT else None, "peak_source": peak_kind,
+                     "issue_frac": (MEASURED_ISSUE[dom][0] / (152 * 4 * MEASURED_ISSUE[dom][1])
+                                    if n == N_DEFAULT and dom in MEASURED_ISSUE else None),
                      "algorithmic_bytes": ab[dom], "mean_launch_ms": kern_ms[dom]},
         "step_roofline": {"algorithmic_bytes": b_step, "achieved": b_step / (step_ms / 1e3) / 1e9, "peak": peak,
                           "frac": b_step / (step_ms / 1e3) / 1e9 / peak, "unit": "GB/s"},
