@@ -687,6 +687,16 @@ def main():
     t_e2e = max_over_ranks(time.perf_counter() - t0)
     barrier()
     link = host_link(stream, pin, n)
+    # the device-resident step over the e2e loop's own window (its steps
+    # start from the lattice), for the link floor below
+    s.upload(pos0, vel0, ve0)
+    s.sync()
+    barrier()
+    e0.record(stream)
+    s.step(DT, args.e2e_steps)
+    e1.record(stream)
+    e1.synchronize()
+    link["step_ms"] = max_over_ranks(e0.elapsed_time(e1)) / args.e2e_steps
     # --- the same step later in the rollout (the fluid has collapsed: more
     # neighbours per particle than near the lattice at rest) ------------------
     steady = None
@@ -719,9 +729,10 @@ def main():
     b_step = sum(ab.values())
     step_ms = t_ms / steps
     # the e2e loop's floor on this host link: the position upload, the step
-    # and the three downloads run one after the other
+    # (device-resident, the same steps) and the three downloads run one after
+    # the other
     e2e_value = n * args.e2e_steps * world / t_e2e
-    link["bound_value"] = n * world / ((link["upload_pos_ms"] + step_ms + link["download_state_ms"]) / 1e3)
+    link["bound_value"] = n * world / ((link["upload_pos_ms"] + link["step_ms"] + link["download_state_ms"]) / 1e3)
     link["frac"] = e2e_value / link["bound_value"]
     line = {
         "metric": "particle-updates/s at 2M SPH", "value": value, "unit": "particle-updates/s", "n_gpus": world,
