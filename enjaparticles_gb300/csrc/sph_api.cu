@@ -17,7 +17,8 @@
 
 using sphk::StepParams;
 
-static std::string g_create_error;
+// the message of the last failed sph_create on this host thread
+static thread_local std::string g_create_error;
 
 int set_err(sph_ctx* c, int code, const char* fmt, ...) {
     char buf[512];

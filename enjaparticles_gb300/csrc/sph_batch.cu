@@ -191,7 +191,8 @@ int bit_width_u(uint32_t v) {
 
 }  // namespace
 
-static std::string g_batch_create_error;
+// the message of the last failed sph_batch_create on this host thread
+static thread_local std::string g_batch_create_error;
 
 int berr(sph_batch* b, int code, const char* fmt, ...) {
     char buf[512];

@@ -613,15 +613,9 @@ __global__ void __launch_bounds__(T) k_density_queue(const DensityArgs A, const 
 
 template <int T, bool Pairs, bool Exact, bool Unit>
 void density_queue_launch(const DensityArgs& A, const BatchQueue& Q, cudaStream_t st) {
-    static int per_sm = -1, sms = 0;  // resident blocks per SM and SMs of the current device
-    if (per_sm < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_density_queue<T, Pairs, Exact, Unit>, T, 0);
-        if (per_sm < 1) per_sm = 1;
-    }
-    k_density_queue<T, Pairs, Exact, Unit><<<per_sm * sms, T, 0, st>>>(A, Q);
+    static std::atomic<int> grid[kQueueMaxDevices];
+    k_density_queue<T, Pairs, Exact, Unit>
+        <<<queue_grid(k_density_queue<T, Pairs, Exact, Unit>, T, grid), T, 0, st>>>(A, Q);
 }
 
 template <int T>

@@ -451,15 +451,8 @@ __global__ void __launch_bounds__(T) k_force_queue(const ForceArgs A, const Batc
 
 template <int T, bool Exact, bool Unit>
 void force_queue_launch(const ForceArgs& A, const BatchQueue& Q, cudaStream_t st) {
-    static int per_sm = -1, sms = 0;  // resident blocks per SM and SMs of the current device
-    if (per_sm < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_force_queue<T, Exact, Unit>, T, 0);
-        if (per_sm < 1) per_sm = 1;
-    }
-    k_force_queue<T, Exact, Unit><<<per_sm * sms, T, 0, st>>>(A, Q);
+    static std::atomic<int> grid[kQueueMaxDevices];
+    k_force_queue<T, Exact, Unit><<<queue_grid(k_force_queue<T, Exact, Unit>, T, grid), T, 0, st>>>(A, Q);
 }
 
 template <int T>

@@ -20,11 +20,34 @@
 // always set unless a test holds it back (hold).
 #pragma once
 
+#include <atomic>
+
 #include "sph_device.cuh"
 
 namespace sphk {
 
 constexpr int kErrQueueTimeout = 2;  // bit of info[kError]
+
+// Blocks of a persistent queue kernel: as many as fit on the current device
+// at once (resident blocks per SM times SMs), cached per kernel and device.
+// The cache entry is the one number, so host threads that fill it together
+// store the same value and none reads half of it.
+constexpr int kQueueMaxDevices = 64;
+template <class Kernel>
+int queue_grid(Kernel kernel, int threads, std::atomic<int> (&cache)[kQueueMaxDevices]) {
+    int dev = 0;
+    const bool cached = cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < kQueueMaxDevices;
+    if (cached) {
+        const int g = cache[dev].load(std::memory_order_relaxed);
+        if (g > 0) return g;
+    }
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    const int g = (per_sm < 1 ? 1 : per_sm) * (sms < 1 ? 1 : sms);
+    if (cached) cache[dev].store(g, std::memory_order_relaxed);
+    return g;
+}
 
 struct BatchQueue {
     unsigned* state;         // [0] next item, [1] blocks arrived, [2] table published; zeroed before a launch

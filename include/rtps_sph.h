@@ -468,8 +468,8 @@ int sph_get_deleted(sph_ctx* ctx, sph_float4* pos, sph_float4* vel, int cap, int
  * (SPH_ETIMEOUT) and out-of-grid deletions are visible through sph_get_num. */
 int sph_sync(sph_ctx* ctx);
 
-/* Copy the message of the last error on ctx (or of the last failed
- * sph_create when ctx is NULL) into buf. */
+/* Copy the message of the last error on ctx (or, when ctx is NULL, of the
+ * last failed sph_create on the calling thread) into buf. */
 int sph_last_error(sph_ctx* ctx, char* buf, int len);
 
 /* ---------------------------------------------------------------------------
@@ -576,6 +576,8 @@ int sph_batch_get_num(sph_batch* batch, int scene, int* n);
  * arrays.  Valid until the scene's next upload or deletion.  Blocking. */
 int sph_batch_get_deleted(sph_batch* batch, int scene, sph_float4* pos, sph_float4* vel, int cap, int* count);
 int sph_batch_sync(sph_batch* batch);
+/* The message of the last error on batch (or, when batch is NULL, of the
+ * last failed sph_batch_create on the calling thread). */
 int sph_batch_last_error(sph_batch* batch, char* buf, int len);
 /* Replace scene `scene`'s SPHParams (same simulation_scale; the grid stays).
  * Blocking. */

@@ -73,6 +73,34 @@ def test_parameter_helpers_without_gpu(lib):
     assert "sm_103a" in info
 
 
+def test_create_errors_are_per_thread(lib):
+    """A failed sph_create leaves its message for sph_last_error(NULL) on the
+    thread that called it; other threads keep their own (argument checks run
+    before any CUDA call, so this needs no GPU)."""
+    import threading
+
+    sp, g, gs = abi.dambreak_params(4096)
+    msgs = {}
+    barrier = threading.Barrier(4)
+
+    def worker(k):
+        out = C.c_void_p()
+        for _ in range(200):
+            rc = lib.sph_create(C.byref(sp), C.byref(g), C.byref(gs), -(k + 1), C.byref(out))
+            assert rc == abi.SPH_EINVAL
+        barrier.wait()  # every thread has failed before any reads its message
+        buf = C.create_string_buffer(256)
+        assert lib.sph_last_error(None, buf, 256) == abi.SPH_OK
+        msgs[k] = buf.value.decode()
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert msgs == {k: "max_num out of range: %d" % -(k + 1) for k in range(4)}
+
+
 def test_cpp_class_compiles():
     src = ("#include \"rtps_sph.hpp\"\nint main() { SPHParams p; GridParams g; rtps::SPH* s = nullptr;\n"
            "rtps::RTPSSettings set; set.SetSetting(\"rest_density\", 1000.0f);\n"
