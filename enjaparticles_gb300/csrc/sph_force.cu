@@ -243,18 +243,16 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     };
     if (!__any_sync(wmask, M > (uint32_t)kMaskBits)) {
         // Every lane's candidates fit the bitmask: the density pass counted
-        // the lane's neighbours (itself included), so the warp runs a loop of
-        // known length, each lane taking its next set bit while it has one.
+        // the lane's neighbours (itself included), so each lane loops over
+        // its own count, taking its next set bit each time (the warp runs
+        // while any lane has one left).
         const uint32_t cnt = M > 0 ? __ldg(nbr + i) - 1u : 0u;
-        const uint32_t kmax = __reduce_max_sync(wmask, cnt);
-        for (uint32_t k = 0; k < kmax; ++k) {
-            if (k < cnt) {
-                const uint32_t p = next_bit();
-                if (!in_bounds(p, M, P.chk_err)) continue;  // a mask bit past the walk's candidates
-                const uint32_t j = index_of(p);
-                if (in_bounds(j, P.chk_cap, P.chk_err))
-                    force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
-            }
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const uint32_t p = next_bit();
+            if (!in_bounds(p, M, P.chk_err)) continue;  // a mask bit past the walk's candidates
+            const uint32_t j = index_of(p);
+            if (in_bounds(j, P.chk_cap, P.chk_err))
+                force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
         }
     } else {
         // Some lane has candidates past the bitmask (crowded cells): the
