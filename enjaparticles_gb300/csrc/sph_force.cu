@@ -14,7 +14,7 @@ namespace sphk {
 // Force (+ collision + leapfrog when Fused).
 //
 // One thread per sorted particle.  The thread first lays out its 9 row runs
-// in shared memory (walk-order offset of each, and sorted index minus walk
+// in shared memory (walk-order end of each, and sorted index minus walk
 // position over it), from cell range loads issued together, then walks its
 // neighbours with a cursor over the density pass's bitmask (candidates past
 // kMaskBits are tested), the next mask word already in flight.  The warp
@@ -116,13 +116,14 @@ struct ForceArgs {
 };
 
 // Sorted particle i (in_range: i below the step's particle count) with the
-// thread's column of the row tables: walk-order offset of each run's first
-// candidate, and sorted index minus walk-order position over the run
-// (j = p + delta, modulo 2^32); rows without candidates are left out.  Every
+// thread's column of the row table: per run, the walk-order position just
+// past its last candidate and the sorted index minus walk-order position
+// over the run (j = p + delta, modulo 2^32), one 8-byte entry; rows without
+// candidates are left out.  Every
 // lane of the warp calls it (the neighbour loop is warp-wide).
 template <int T, bool Fused, bool Exact, bool Unit, class Scenes>
 __device__ __forceinline__ void force_one(const int i, const bool in_range, const int out, const ForceArgs& G,
-                                          const Scenes& R, uint32_t (*s_delta)[T], uint32_t (*s_off)[T]) {
+                                          const Scenes& R, uint2 (*s_row)[T]) {
     const float4* __restrict__ pos_s = G.pos_s;
     const float4* __restrict__ rec_pd = G.rec_pd;
     const float4* __restrict__ rec_vi = G.rec_vi;
@@ -182,8 +183,7 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     const int3 c = grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
     if (cell_fast(P, c)) {
         walk_rows_fast_batched(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {  // at most 9 runs
-            s_delta[nrows][t] = rs - M;
-            s_off[nrows][t] = M;
+            s_row[nrows][t] = make_uint2(M + (re - rs), rs - M);
             M += re - rs;
             ++nrows;
         });
@@ -198,7 +198,6 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
             }
         });
     }
-    s_off[nrows][t] = M;
 
     // Cursor: bit position p of the last neighbour taken, row r containing it.
     const uint32_t* mrow = mask + i;
@@ -213,21 +212,24 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     constexpr bool kRegCursor = !Scenes::kBatch;
     uint32_t next_off = 0, delta = 0;
     if constexpr (kRegCursor) {
-        next_off = s_off[1][t];
-        delta = s_delta[0][t];
+        const uint2 e = s_row[0][t];
+        next_off = e.x;
+        delta = e.y;
     }
     // sorted index of the candidate at walk position p, advancing row r
     auto index_of = [&](uint32_t p) -> uint32_t {
         if constexpr (kRegCursor) {
             while (p >= next_off) {
                 ++r;
-                next_off = s_off[r + 1][t];
-                delta = s_delta[r][t];
+                const uint2 e = s_row[r][t];
+                next_off = e.x;
+                delta = e.y;
             }
             return p + delta;
         } else {
-            while (p >= s_off[r + 1][t]) ++r;
-            return p + s_delta[r][t];
+            uint2 e = s_row[r][t];
+            while (p >= e.x) e = s_row[++r][t];
+            return p + e.y;
         }
     };
     // the lane's next neighbour from the bitmask (one is left)
@@ -377,12 +379,11 @@ constexpr int force_min_blocks() {
 template <int T, bool Fused, bool Exact, bool Unit, class Scenes>
 __global__ void __launch_bounds__(T, (force_min_blocks<T, Exact, Scenes>()))
     k_force(const ForceArgs A, const int* __restrict__ info, const Scenes R) {
-    __shared__ uint32_t s_delta[9][T];
-    __shared__ uint32_t s_off[10][T];
+    __shared__ uint2 s_row[9][T];
     int n_old, out;
     const int n = effective_num(info, n_old, out);
     const int i = blockIdx.x * T + threadIdx.x;
-    force_one<T, Fused, Exact, Unit>(i, i < n, out, A, R, s_delta, s_off);
+    force_one<T, Fused, Exact, Unit>(i, i < n, out, A, R, s_row);
 }
 
 template <int T, class Scenes>
@@ -437,13 +438,12 @@ void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec
 template <int T, bool Exact, bool Unit>
 __global__ void __launch_bounds__(T) k_force_queue(const ForceArgs A, const BatchQueue Q) {
     __shared__ QueueShared<T> S;
-    __shared__ uint32_t s_delta[9][T];
-    __shared__ uint32_t s_off[10][T];
+    __shared__ uint2 s_row[9][T];
     if (!queue_start<T>(Q, S)) return;
     while (queue_next<T>(Q, S)) {
         const TileScene R = queue_scene<T>(Q, S);
         const int i = (int)(S.first + threadIdx.x);
-        force_one<T, true, Exact, Unit>(i, threadIdx.x < S.count, -1, A, R, s_delta, s_off);
+        force_one<T, true, Exact, Unit>(i, threadIdx.x < S.count, -1, A, R, s_row);
     }
 }
 
