@@ -365,15 +365,18 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     pos_u[orig] = po;
 }
 
-// Minimum resident blocks per SM the force kernel is compiled for.  One
-// system in the default arithmetic: 1280 threads per SM (10 blocks of 128),
-// which fits it in 48 registers without spills (the unbounded build took 56
-// with 8 B of spills at 128 threads, 48 with 60 B at 256) and measured 3 %
-// faster.  The exact and batched variants would spill at that bound: 0
-// leaves them unbounded.
+// Minimum resident blocks per SM the force kernel is compiled for, in
+// threads per SM over T (each measured against the unbounded build):
+//   one system, default arithmetic: 1280 (10 blocks of 128, 48 registers,
+//     no spills), 3 % faster;
+//   one system, exact arithmetic: 1152 (9 blocks of 128, 56 registers, no
+//     spills; unbounded it took 56 with 24 B of spills), 2 % faster;
+//   a batch, default arithmetic: 1152 (56 registers, 40 B of spills against
+//     64 and 4 B), the batch step 2 % faster;
+//   a batch, exact arithmetic: unbounded.
 template <int T, bool Exact, class Scenes>
 constexpr int force_min_blocks() {
-    return (!Exact && !Scenes::kBatch) ? 1280 / T : 0;
+    return !Scenes::kBatch ? (Exact ? 1152 / T : 1280 / T) : (Exact ? 0 : 1152 / T);
 }
 
 template <int T, bool Fused, bool Exact, bool Unit, class Scenes>
