@@ -158,8 +158,10 @@ __global__ void __launch_bounds__(256) k_adj_integrate(int n, const Scenes R, fl
 // ---------------------------------------------------------------------------
 // Neighbours of sorted particle i as the forward density pass recorded them:
 // the bitmask over the first kMaskBits candidates in walk order, the rest
-// tested again.  Lanes advance in lock step, one neighbour each per
-// iteration (the forward force pass's scheme); fn(j) runs for each j != i.
+// tested again.  When every lane's candidates fit the bitmask each lane runs
+// through its own set bits; otherwise lanes advance in lock step, one
+// neighbour each per iteration, with a vote per iteration; fn(j) runs for
+// each j != i, in walk order either way.
 // Particles outside the integer-hash range walk the 27 cells directly.
 template <class Fn>
 __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const uint32_t* cs, const uint32_t* ce,
@@ -196,6 +198,26 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
     uint32_t q = (uint32_t)sphk::kMaskBits;
     int r = 0;
     uint32_t next_off = s_off[1][t], delta = s_rs[0][t];  // row r's end and index offset
+    if (!__any_sync(wmask, M > (uint32_t)sphk::kMaskBits)) {
+        // Every lane's candidates fit the bitmask: each lane runs through its
+        // own set bits, with no vote per neighbour.
+        for (;;) {
+            while (m == 0 && (w + 1) * 32u < mbits) {
+                ++w;
+                m = m_next;
+                m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
+            }
+            if (m == 0) return;
+            const uint32_t p = w * 32u + (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+            while (p >= next_off) {
+                ++r;
+                next_off = s_off[r + 1][t];
+                delta = s_rs[r][t];
+            }
+            fn(p + delta);
+        }
+    }
     for (;;) {
         bool have = false;
         uint32_t p = 0;
