@@ -245,7 +245,7 @@ void free_all(sph_ctx* c) {
                     c->del_pos, c->del_vel, c->density, c->rec_pd, c->rec_vi, c->nbr, c->mask, c->keys_a, c->idx_a, c->keys_b, c->idx_b,
                     c->cell_start, c->cell_end, c->info, c->scratch, c->grav, c->tri, c->cf, c->cf_inv,
                     c->mc_scan, c->mc_table, c->mesh, c->cell_count, c->cell_tile_total, c->cell_entries,
-                    c->pos_xy, c->pos_z};
+                    c->pos_xy, c->pos_z, c->cell_pre};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->host_info) cudaFreeHost(c->host_info);
@@ -304,7 +304,7 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
     const uint32_t cells = (uint32_t)c->gp.nb_cells + 1u;
     sphk::launch_cell_totals(c->cell_count, c->cell_tile_total, c->info, cells, c->lc.scan_tile_cells, st);
     sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info, cells,
-                           c->lc.scan_tile_cells, st);
+                           c->lc.scan_tile_cells, st, c->cell_pre);
     sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
     // the permute gathers the velocities when gather == 2
     if (gather == 2) {
@@ -329,20 +329,26 @@ int enqueue_cell_sort(sph_ctx* c, int gather) {
 // of the same enqueue wrote it (keys_a), for the default arithmetic's
 // cell-pair pass; null where the keys are not known to match pos_s (the
 // stage API's density, which the caller may run after any stage), which
-// then takes the one-particle pass.
+// then takes the one-particle pass.  The same enqueue's counting sort also
+// wrote cell_pre, which the cell-pair pass then takes its row runs from.
 void density_launch(sph_ctx* c, bool fused, cudaStream_t st, bool pack = false,
                     const uint32_t* sorted_keys = nullptr) {
     sphk::launch_density(c->pos_s, fused ? nullptr : c->veleval_s, c->density, c->rec_pd, c->rec_vi,
                          c->nbr, c->mask,
                          (size_t)c->max_num, c->cell_start, c->cell_end, c->info, c->P, c->num_hint, c->pos_xy,
-                         c->pos_z, pack, c->lc.density_threads, st, sorted_keys);
+                         c->pos_z, pack, c->lc.density_threads, st, sorted_keys,
+                         sorted_keys != nullptr ? c->cell_pre : nullptr);
 }
 
-void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st) {
+// cell_pre: the prefix of the cell counts when the same enqueue's counting
+// sort wrote it (null for the stage API, whose cell ranges come from its own
+// cellindices pass).
+void force_launch(sph_ctx* c, uint32_t* idx, bool fused, float dt, cudaStream_t st,
+                  const uint32_t* cell_pre = nullptr) {
     sphk::launch_force(c->pos_s, c->rec_pd, c->rec_vi, c->mask, (size_t)c->max_num, c->nbr, c->cell_start, c->cell_end,
                        c->info, c->force_s, c->xsph_s, idx, c->vel_s, c->pos_u, c->vel_u, c->veleval_u,
                        fused ? c->keep_f : nullptr, fused ? c->keep_v : nullptr, c->P, dt, fused ? 1 : 0, c->exact,
-                       c->num_hint, c->lc.force_threads, st);
+                       c->num_hint, c->lc.force_threads, st, cell_pre);
 }
 
 }  // namespace
@@ -355,7 +361,7 @@ static int enqueue_to_force(sph_ctx* c) {
     sphk::launch_delete_staged(c->pos_s, c->vel_s, c->veleval_s, c->idx_a, c->pos_u, c->vel_u, c->veleval_u,
                                c->del_pos, c->del_vel, c->info, c->num_hint, c->stream);
     density_launch(c, false, c->stream, false, c->keys_a);
-    force_launch(c, c->idx_a, false, 0.f, c->stream);
+    force_launch(c, c->idx_a, false, 0.f, c->stream, c->cell_pre);
     return SPH_OK;
 }
 
@@ -391,11 +397,11 @@ int enqueue_fused_step(sph_ctx* c, float dt) {
         // the triangle stage sits between the walls and the integrator: the
         // force pass without them, then one kernel for gravity, walls,
         // triangles and the integrator
-        force_launch(c, c->idx_a, false, 0.f, c->stream);
+        force_launch(c, c->idx_a, false, 0.f, c->stream, c->cell_pre);
         sphk::launch_triangles_step(c->pos_s, c->vel_s, c->force_s, c->xsph_s, c->idx_a, c->pos_u, c->vel_u,
                                     c->veleval_u, c->info, c->P, dt, c->num_hint, c->stream);
     } else {
-        force_launch(c, c->idx_a, true, dt, c->stream);
+        force_launch(c, c->idx_a, true, dt, c->stream, c->cell_pre);
     }
     CK_LAUNCH(c);
     return SPH_OK;
@@ -568,6 +574,7 @@ int sph_create(const SPHParams* sphp, const GridParams* grid, const GridParams* 
     ALLOC(c->idx_b, N * 4);
     ALLOC(c->cell_start, C1 * 4);
     ALLOC(c->cell_end, C1 * 4);
+    ALLOC(c->cell_pre, C1 * 4);
     ALLOC(c->cell_count, C1 * 4);
     ALLOC(c->cell_tile_total, (size_t)sphk::cell_scan_tiles((int)C1, sphk::kScanTileMin) * 4);
     ALLOC(c->cell_entries, N * 8);
@@ -1133,7 +1140,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
                                  c->lc.scan_tile_cells, st);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_scan(c->cell_count, c->cell_start, c->cell_end, c->cell_tile_total, c->info,
-                               (uint32_t)c->gp.nb_cells + 1u, c->lc.scan_tile_cells, st);
+                               (uint32_t)c->gp.nb_cells + 1u, c->lc.scan_tile_cells, st, c->cell_pre);
         CK(c, cudaEventRecord(ev[e++], st));
         sphk::launch_cell_place(c->keys_b, c->idx_b, c->cell_start, c->cell_entries, c->info, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
@@ -1146,7 +1153,7 @@ int sph_step_profile(sph_ctx* c, float dt, int nsteps, float* kernel_ms, int cap
         sphk::launch_step_velocities(c->pos_s, c->idx_a, c->vel_u, c->veleval_u, c->rec_vi, c->vel_s, c->del_pos,
                                      c->del_vel, c->info, 0, c->num_hint, st);
         CK(c, cudaEventRecord(ev[e++], st));
-        force_launch(c, c->idx_a, true, dt, st);
+        force_launch(c, c->idx_a, true, dt, st, c->cell_pre);
         CK(c, cudaEventRecord(ev[e++], st));
         CK_LAUNCH(c);
         CK(c, cudaEventSynchronize(ev[nk]));

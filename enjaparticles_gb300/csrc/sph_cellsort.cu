@@ -21,8 +21,10 @@
 //   scan     an exclusive scan of the counts, one block per tile, its base the
 //            sum of the totals of the tiles before it (no block waits on
 //            another), writes cell_start (kEmpty for an empty cell) and
-//            cell_end of the non-empty cells, records where the out-of-grid
-//            key nb_cells starts, and zeroes the counts for the next step.
+//            cell_end of the non-empty cells, the prefix of every cell (empty
+//            ones included) for the neighbour passes' row runs, records where
+//            the out-of-grid key nb_cells starts, and zeroes the counts for
+//            the next step.
 //   place    each particle's (index, key) at cell_start[key] + slot.
 //   permute  slots within a cell come in atomic order, so each sorted
 //            position ranks its particle index among the entries of its cell
@@ -191,7 +193,7 @@ template <int ST>
 __global__ void __launch_bounds__(ST) k_cell_scan(uint32_t* __restrict__ count, uint32_t* __restrict__ cell_start,
                                                   uint32_t* __restrict__ cell_end,
                                                   const uint32_t* __restrict__ tile_total, int* __restrict__ info,
-                                                  uint32_t cells, int prescanned) {
+                                                  uint32_t cells, int prescanned, uint32_t* __restrict__ pre) {
     constexpr int kScanTile = ST * kScanItems;
     __shared__ uint32_t s_warp[ST / 32];
     __shared__ uint32_t s_base[ST / 32];
@@ -209,7 +211,8 @@ __global__ void __launch_bounds__(ST) k_cell_scan(uint32_t* __restrict__ count, 
     // a recorded rollout's cell arrays are packed at a stride of nb_cells + 1
     // words, so their base need not be 16-byte aligned
     const bool vec = c0 + kScanItems <= cells &&
-                     ((reinterpret_cast<uintptr_t>(count) | reinterpret_cast<uintptr_t>(cell_start)) & 15u) == 0;
+                     ((reinterpret_cast<uintptr_t>(count) | reinterpret_cast<uintptr_t>(cell_start) |
+                       reinterpret_cast<uintptr_t>(pre)) & 15u) == 0;
     uint32_t v[kScanItems];
     load_counts(count, c0, cells, vec, v);
     uint32_t sum = 0;
@@ -227,10 +230,11 @@ __global__ void __launch_bounds__(ST) k_cell_scan(uint32_t* __restrict__ count, 
     uint32_t run = x - sum;
 #pragma unroll
     for (int w = 0; w < ST / 32; ++w) run += (w < warp ? s_warp[w] : 0u) + s_base[w];
-    uint32_t st[kScanItems];
+    uint32_t st[kScanItems], ex[kScanItems];
     const uint32_t last = cells - 1;  // the out-of-grid key
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
+        ex[k] = run;
         st[k] = v[k] ? run : kEmpty;
         if (v[k]) {
             cell_end[c0 + k] = run + v[k];
@@ -246,12 +250,19 @@ __global__ void __launch_bounds__(ST) k_cell_scan(uint32_t* __restrict__ count, 
             s4[k] = make_uint4(st[4 * k], st[4 * k + 1], st[4 * k + 2], st[4 * k + 3]);
             z4[k] = make_uint4(0u, 0u, 0u, 0u);
         }
+        if (pre != nullptr) {
+            uint4* p4 = reinterpret_cast<uint4*>(pre + c0);
+#pragma unroll
+            for (int k = 0; k < kScanItems / 4; ++k)
+                p4[k] = make_uint4(ex[4 * k], ex[4 * k + 1], ex[4 * k + 2], ex[4 * k + 3]);
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
             if (c0 + k < cells) {
                 cell_start[c0 + k] = st[k];
                 count[c0 + k] = 0u;
+                if (pre != nullptr) pre[c0 + k] = ex[k];
             }
         }
     }
@@ -361,16 +372,16 @@ void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, 
 }
 
 void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
-                      uint32_t cells, int tile_cells, cudaStream_t st) {
+                      uint32_t cells, int tile_cells, cudaStream_t st, uint32_t* pre) {
     const int tiles = cell_scan_tiles((int)cells, tile_cells);
     const int prescanned = tiles > kDirectTiles;
     if (prescanned) k_cell_tile_scan<<<1, kTileScanThreads, 0, st>>>(tile_total, tiles);
     if (tile_cells == 2048)
-        k_cell_scan<128><<<tiles, 128, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
+        k_cell_scan<128><<<tiles, 128, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned, pre);
     else if (tile_cells == 8192)
-        k_cell_scan<512><<<tiles, 512, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
+        k_cell_scan<512><<<tiles, 512, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned, pre);
     else
-        k_cell_scan<256><<<tiles, 256, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned);
+        k_cell_scan<256><<<tiles, 256, 0, st>>>(count, cell_start, cell_end, tile_total, info, cells, prescanned, pre);
 }
 
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,

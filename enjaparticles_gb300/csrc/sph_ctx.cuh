@@ -51,6 +51,7 @@ struct sph_ctx {
     uint32_t *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
     uint32_t *keys_cur = nullptr, *idx_cur = nullptr;  // what SORT_HASHES / SORT_INDICES show
     uint32_t *cell_start = nullptr, *cell_end = nullptr;
+    uint32_t* cell_pre = nullptr;  // the counting sort's prefix of the cell counts, every cell
     int* info = nullptr;
     uint32_t* scratch = nullptr;
     size_t scratch_words = 0;

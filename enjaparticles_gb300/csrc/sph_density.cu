@@ -45,6 +45,9 @@ struct DensityArgs {
     // sorted cell keys (the counting sort's), for the cell-pair pass; null
     // where the pass is not used
     const uint32_t* keys;
+    // the counting sort's prefix of the cell counts (launch_cell_scan), for
+    // the cell-pair pass's row runs; null: the runs from cs0 / ce0
+    const uint32_t* pre;
 };
 
 // Sorted particle i, scalar candidates (every operation rounded on its own
@@ -388,20 +391,32 @@ __device__ __forceinline__ void density_cellpair(const uint32_t a, const bool ha
 #pragma unroll 1
         for (int dy = -1; dy <= 1; ++dy) {
             const int base = ((c.z + dz) * P.res_y + (c.y + dy)) * P.res_x + c.x;
-            uint32_t rs = kEmpty, last = 0;
+            uint32_t rs, re;
+            if (A.pre != nullptr) {
+                // the row's cells base-1 .. base+1 within the grid: two loads
+                const int lo = base - 1 < 0 ? 0 : base - 1;
+                const int hi = base + 1 > (int)C - 1 ? (int)C - 1 : base + 1;
+                if (lo > hi) continue;
+                rs = __ldg(A.pre + lo);
+                re = __ldg(A.pre + hi + 1);
+                if (rs >= re) continue;
+            } else {
+                uint32_t last = 0;
+                rs = kEmpty;
 #pragma unroll
-            for (int dx = -1; dx <= 1; ++dx) {
-                const uint32_t h = (uint32_t)(base + dx);
-                if (h < C) {
-                    const uint32_t s0 = __ldg(cs + h);
-                    if (s0 != kEmpty) {
-                        if (rs == kEmpty) rs = s0;
-                        last = h;
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const uint32_t h = (uint32_t)(base + dx);
+                    if (h < C) {
+                        const uint32_t s0 = __ldg(cs + h);
+                        if (s0 != kEmpty) {
+                            if (rs == kEmpty) rs = s0;
+                            last = h;
+                        }
                     }
                 }
+                if (rs == kEmpty) continue;
+                re = __ldg(ce + last);
             }
-            if (rs == kEmpty) continue;
-            const uint32_t re = __ldg(ce + last);
             if (!run_ok(P, rs, re)) continue;  // bounds-checked builds
             const uint32_t kend = (re + 1u) >> 1;
             for (uint32_t ks = rs >> 1; ks < kend; ks += kPairSegment) {
@@ -543,11 +558,11 @@ void launch_density_tt(const float4* pos_s, const float4* veleval_s, float* dens
                        uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                        const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
                        int grid_items, float4* pxy, float2* pz, bool pack, cudaStream_t st,
-                       const uint32_t* keys) {
+                       const uint32_t* keys, const uint32_t* cell_pre = nullptr) {
     int blocks = (grid_items + T - 1) / T;
     if (blocks < 1) blocks = 1;
     const DensityArgs A{pos_s, pxy, pz, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                        cell_end, keys};
+                        cell_end, keys, cell_pre};
     if (pxy != nullptr && pz != nullptr && unit && !exact) {
         if (pack) {
             const int pb = ((grid_items + 1) / 2 + 255) / 256;
@@ -577,19 +592,19 @@ void launch_density_t(const float4* pos_s, const float4* veleval_s, float* densi
                       uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                       const uint32_t* cell_end, const int* info, const Scenes& R, bool unit, bool exact,
                       int grid_items, float4* pxy, float2* pz, bool pack, int threads, cudaStream_t st,
-                      const uint32_t* keys = nullptr) {
+                      const uint32_t* keys = nullptr, const uint32_t* cell_pre = nullptr) {
     switch (threads) {
         case 128:
             launch_density_tt<128>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys);
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys, cell_pre);
             break;
         case 512:
             launch_density_tt<512>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys);
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys, cell_pre);
             break;
         default:
             launch_density_tt<256>(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start,
-                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys);
+                                   cell_end, info, R, unit, exact, grid_items, pxy, pz, pack, st, keys, cell_pre);
     }
 }
 
@@ -646,9 +661,11 @@ void launch_density_queue(const float4* pos_s, const float4* veleval_s, float* d
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
-                    float2* pz, bool pack, int threads, cudaStream_t st, const uint32_t* keys) {
+                    float2* pz, bool pack, int threads, cudaStream_t st, const uint32_t* keys,
+                    const uint32_t* cell_pre) {
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, pxy, pz, pack, threads, st, keys);
+                     OneScene{p}, p.unit_scale != 0, p.exact != 0, grid_items, pxy, pz, pack, threads, st, keys,
+                     cell_pre);
 }
 
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,

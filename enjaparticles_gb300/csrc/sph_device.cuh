@@ -208,8 +208,11 @@ constexpr int kDirectTiles = 2048;
 constexpr int kScanTileMin = 2048;
 void launch_cell_totals(const uint32_t* count, uint32_t* tile_total, int* info, uint32_t cells, int tile_cells,
                         cudaStream_t st);
+// pre (nullable): the exclusive prefix of the counts over every cell, empty
+// ones included (pre[k]: sorted particles with a key below k), so that the
+// sorted particles of cells lo..hi are pre[lo] .. pre[hi + 1] - 1.
 void launch_cell_scan(uint32_t* count, uint32_t* cell_start, uint32_t* cell_end, uint32_t* tile_total, int* info,
-                      uint32_t cells, int tile_cells, cudaStream_t st);
+                      uint32_t cells, int tile_cells, cudaStream_t st, uint32_t* pre = nullptr);
 void launch_cell_place(const uint32_t* key_of, const uint32_t* slot_of, const uint32_t* cell_start, uint2* entries,
                        const int* info, int grid_items, cudaStream_t st);
 // pxy / pz (nullable): the sorted positions also as pairs (launch_density).
@@ -228,7 +231,8 @@ void launch_cells_permute(const uint32_t* keys, const uint32_t* idx, uint32_t* c
 void launch_density(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd, float4* rec_vi,
                     uint32_t* nbr, uint32_t* mask, size_t mask_stride, const uint32_t* cell_start,
                     const uint32_t* cell_end, const int* info, const StepParams& p, int grid_items, float4* pxy,
-                    float2* pz, bool pack, int threads, cudaStream_t st, const uint32_t* keys = nullptr);
+                    float2* pz, bool pack, int threads, cudaStream_t st, const uint32_t* keys = nullptr,
+                    const uint32_t* cell_pre = nullptr);
 // The fused step's velocity pass, beside density and before force (the first
 // passes that need the uploaded velocities): the veleval lanes of rec_vi in
 // sorted order, and the out-of-grid bookkeeping (kept velocities into vel_s
@@ -245,7 +249,7 @@ void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_v
                   size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                   float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
                   float4* veleval_u, float4* keep_f, float4* keep_v, const StepParams& p, float dt, int fused,
-                  int exact, int grid_items, int threads, cudaStream_t st);
+                  int exact, int grid_items, int threads, cudaStream_t st, const uint32_t* cell_pre = nullptr);
 // Batch forms of the neighbour passes (fused force only).
 void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* density, float4* rec_pd,
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,

@@ -113,6 +113,9 @@ struct ForceArgs {
     float4* keep_f;
     float4* keep_v;
     float dt;
+    // the counting sort's prefix of the cell counts (launch_cell_scan), for
+    // the row runs of one system; null: the runs from cs0 / ce0
+    const uint32_t* pre;
 };
 
 // Sorted particle i (in_range: i below the step's particle count) with the
@@ -181,12 +184,16 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     int nrows = 0;
     uint32_t M = 0;
     const int3 c = grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
+    auto add_row = [&](uint32_t rs, uint32_t re) {  // at most 9 runs
+        s_row[nrows][t] = make_uint2(M + (re - rs), rs - M);
+        M += re - rs;
+        ++nrows;
+    };
     if (cell_fast(P, c)) {
-        walk_rows_fast_batched(P, cs, ce, c, [&](uint32_t rs, uint32_t re) {  // at most 9 runs
-            s_row[nrows][t] = make_uint2(M + (re - rs), rs - M);
-            M += re - rs;
-            ++nrows;
-        });
+        if (!Scenes::kBatch && G.pre != nullptr)
+            walk_rows_prefix(P, G.pre, c, add_row);
+        else
+            walk_rows_fast_batched(P, cs, ce, c, add_row);
     } else {
         // Cells beyond the integer-hash range (particles far outside the
         // walls): the 27 cells tested one by one, pairs accumulated at once.
@@ -394,11 +401,12 @@ void launch_force_tt(const float4* pos_s, const float4* rec_pd, const float4* re
                      size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end,
                      const int* info, float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s,
                      float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f, float4* keep_v, const Scenes& R,
-                     bool unit, float dt, int fused, int exact, int grid_items, cudaStream_t st) {
+                     bool unit, float dt, int fused, int exact, int grid_items, cudaStream_t st,
+                     const uint32_t* cell_pre) {
     int blocks = (grid_items + T - 1) / T;
     if (blocks < 1) blocks = 1;
     const ForceArgs A{pos_s, rec_pd,  rec_vi, mask,      mask_stride, nbr,    cell_start, cell_end, force_s,
-                      xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, dt};
+                      xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, dt, cell_pre};
 #define SPH_FORCE_LAUNCH(F, E, U) k_force<T, F, E, U, Scenes><<<blocks, T, 0, st>>>(A, info, R)
     if (fused) {
         if (exact) {
@@ -421,20 +429,21 @@ void launch_force_t(const float4* pos_s, const float4* rec_pd, const float4* rec
                     size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end,
                     const int* info, float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s,
                     float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f, float4* keep_v, const Scenes& R,
-                    bool unit, float dt, int fused, int exact, int grid_items, int threads, cudaStream_t st) {
+                    bool unit, float dt, int fused, int exact, int grid_items, int threads, cudaStream_t st,
+                    const uint32_t* cell_pre = nullptr) {
     // the staged (unfused) pass keeps the default shape
     if (fused && threads == 64)
         launch_force_tt<64>(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, force_s,
                             xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, R, unit, dt, fused, exact,
-                            grid_items, st);
+                            grid_items, st, cell_pre);
     else if (fused && threads == 256)
         launch_force_tt<256>(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, force_s,
                              xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, R, unit, dt, fused, exact,
-                             grid_items, st);
+                             grid_items, st, cell_pre);
     else
         launch_force_tt<kForceThreads>(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info,
                                        force_s, xsph_s, idx, vel_s, pos_u, vel_u, veleval_u, keep_f, keep_v, R, unit,
-                                       dt, fused, exact, grid_items, st);
+                                       dt, fused, exact, grid_items, st, cell_pre);
 }
 
 // The batch's fused force pass under the queue scheduler (sph_queue.cuh).
@@ -483,10 +492,10 @@ void launch_force(const float4* pos_s, const float4* rec_pd, const float4* rec_v
                   size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                   float4* force_s, float4* xsph_s, uint32_t* idx, const float4* vel_s, float4* pos_u, float4* vel_u,
                   float4* veleval_u, float4* keep_f, float4* keep_v, const StepParams& p, float dt, int fused,
-                  int exact, int grid_items, int threads, cudaStream_t st) {
+                  int exact, int grid_items, int threads, cudaStream_t st, const uint32_t* cell_pre) {
     launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, force_s, xsph_s, idx, vel_s,
                    pos_u, vel_u, veleval_u, keep_f, keep_v, OneScene{p}, p.unit_scale != 0, dt, fused, exact,
-                   grid_items, threads, st);
+                   grid_items, threads, st, cell_pre);
 }
 
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,

@@ -104,6 +104,28 @@ __device__ __forceinline__ void walk_rows_fast_batched(const StepParams& P, cons
         if (rs[r] != kEmpty && run_ok(P, rs[r], re[r])) f(rs[r], re[r]);
 }
 
+// The same 9 row runs from the exclusive prefix of the cell counts (pre[k]:
+// sorted particles with a key below k, k = 0..C): the row's cells lo..hi
+// (base - 1 .. base + 1 within the grid) hold sorted particles
+// pre[lo] .. pre[hi + 1] - 1, empty cells included, so each run is two loads.
+template <class F>
+__device__ __forceinline__ void walk_rows_prefix(const StepParams& P, const uint32_t* __restrict__ pre, const int3& c,
+                                                 F&& f) {
+    const int C = P.nb_cells;
+    uint32_t rs[9], re[9];
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        const int base = ((c.z + r / 3 - 1) * P.res_y + (c.y + r % 3 - 1)) * P.res_x + c.x;
+        const int lo = base - 1 < 0 ? 0 : base - 1;
+        const int hi = base + 1 > C - 1 ? C - 1 : base + 1;
+        rs[r] = lo <= hi ? __ldg(pre + lo) : 0u;
+        re[r] = lo <= hi ? __ldg(pre + hi + 1) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+        if (rs[r] < re[r] && run_ok(P, rs[r], re[r])) f(rs[r], re[r]);
+}
+
 // The 27 cells one by one with the reference's float hash (up to 27 calls).
 template <class F>
 __device__ __forceinline__ void walk_rows_slow(const StepParams& P, const uint32_t* __restrict__ cs,
