@@ -211,7 +211,7 @@ static void batch_free(sph_batch* b) {
                     b->mask, b->keys_a, b->idx_a, b->keys_b, b->idx_b, b->cell_start, b->cell_end, b->scene_of,
                     b->d_slot_off, b->d_cbase, b->d_num, b->d_table, b->info_nb, b->cell_count, b->cell_tile_total,
                     b->cell_entries, b->pos_xy, b->pos_z, b->vel_s, b->d_seg, b->d_del, b->nbr, b->q_state,
-                    b->q_tiles};
+                    b->q_tiles, b->cell_pre};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->host_info) cudaFreeHost(b->host_info);
@@ -250,7 +250,7 @@ int batch_enqueue_step(sph_batch* b, float dt, cudaEvent_t* ev) {
     if (ev) BCK(b, cudaEventRecord(ev[0], st));
     sphk::launch_cell_totals(b->cell_count, b->cell_tile_total, nullptr, cells, b->lc.scan_tile_cells, st);
     sphk::launch_cell_scan(b->cell_count, b->cell_start, b->cell_end, b->cell_tile_total, nullptr, cells,
-                           b->lc.scan_tile_cells, st);
+                           b->lc.scan_tile_cells, st, b->cell_pre);
     if (ev) BCK(b, cudaEventRecord(ev[1], st));
     k_bplace<<<blocks < 1 ? 1 : blocks, 256, 0, st>>>(b->keys_b, b->idx_b, b->cell_start, b->d_cbase, b->cell_entries,
                                                        b->nslots, b->cell_bits, b->invalid_key);
@@ -283,11 +283,12 @@ int batch_enqueue_step(sph_batch* b, float dt, cudaEvent_t* ev) {
     }
     sphk::launch_density_batch(b->pos_s, b->veleval_s, b->density, b->rec_pd, b->rec_vi, b->nbr, b->mask,
                                (size_t)b->nslots, b->cell_start, b->cell_end, b->info_nb, scenes, b->unit != 0,
-                               b->exact, b->nvalid, b->pos_xy, b->pos_z, false, b->lc.density_threads, st);
+                               b->exact, b->nvalid, b->pos_xy, b->pos_z, false, b->lc.density_threads, st,
+                               b->cell_pre);
     if (ev) BCK(b, cudaEventRecord(ev[3], st));
     sphk::launch_force_batch(b->pos_s, b->rec_pd, b->rec_vi, b->mask, (size_t)b->nslots, b->nbr, b->cell_start, b->cell_end,
                              b->info_nb, b->idx_a, b->pos_u, b->vel_u, b->veleval_u, b->keep_f, b->keep_v, scenes,
-                             b->unit != 0, dt, b->exact, b->nvalid, b->lc.force_threads, st);
+                             b->unit != 0, dt, b->exact, b->nvalid, b->lc.force_threads, st, b->cell_pre);
     if (ev) BCK(b, cudaEventRecord(ev[4], st));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return berr(b, SPH_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
@@ -375,6 +376,7 @@ int sph_batch_create(int nscenes, const SPHParams* sphp, const GridParams* grids
     BALLOC(b->idx_b, N * 4);
     BALLOC(b->cell_start, cells * 4);
     BALLOC(b->cell_end, cells * 4);
+    BALLOC(b->cell_pre, cells * 4);
     BALLOC(b->scene_of, N * 2);
     BALLOC(b->d_slot_off, nscenes * 4);
     BALLOC(b->d_cbase, nscenes * 4);

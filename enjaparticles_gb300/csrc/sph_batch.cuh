@@ -46,6 +46,7 @@ struct sph_batch {
     uint32_t* nbr = nullptr;   // neighbour counts (density pass) for the force pass
     uint32_t *mask = nullptr, *keys_a = nullptr, *idx_a = nullptr, *keys_b = nullptr, *idx_b = nullptr;
     uint32_t *cell_start = nullptr, *cell_end = nullptr;
+    uint32_t* cell_pre = nullptr;  // prefix of the cell counts over every cell of every scene
     uint16_t* scene_of = nullptr;
     uint32_t *d_slot_off = nullptr, *d_cbase = nullptr;
     int* d_num = nullptr;

@@ -369,6 +369,7 @@ __device__ __forceinline__ void density_cellpair(const uint32_t a, const bool ha
     const float4 pb = has_b ? __ldg(A.pos_s + a + 1) : pa;
     const uint32_t* __restrict__ cs = A.cs0 + R.cell_base((int)a);
     const uint32_t* __restrict__ ce = A.ce0 + R.cell_base((int)a);
+    const uint32_t* __restrict__ pre = A.pre != nullptr ? A.pre + R.cell_base((int)a) : nullptr;
     const float4* __restrict__ pxy = A.pxy;
     const float2* __restrict__ pz = A.pz;
     const uint32_t C = (uint32_t)P.nb_cells;
@@ -392,13 +393,13 @@ __device__ __forceinline__ void density_cellpair(const uint32_t a, const bool ha
         for (int dy = -1; dy <= 1; ++dy) {
             const int base = ((c.z + dz) * P.res_y + (c.y + dy)) * P.res_x + c.x;
             uint32_t rs, re;
-            if (A.pre != nullptr) {
+            if (pre != nullptr) {
                 // the row's cells base-1 .. base+1 within the grid: two loads
                 const int lo = base - 1 < 0 ? 0 : base - 1;
                 const int hi = base + 1 > (int)C - 1 ? (int)C - 1 : base + 1;
                 if (lo > hi) continue;
-                rs = __ldg(A.pre + lo);
-                re = __ldg(A.pre + hi + 1);
+                rs = __ldg(pre + lo);
+                re = __ldg(pre + hi + 1);
                 if (rs >= re) continue;
             } else {
                 uint32_t last = 0;
@@ -672,10 +673,10 @@ void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* d
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                           const ManyScenes& scenes, bool unit, int exact, int grid_items, float4* pxy, float2* pz,
-                          bool pack, int threads, cudaStream_t st) {
+                          bool pack, int threads, cudaStream_t st, const uint32_t* cell_pre) {
     // the batch's sort leaves every particle's (scene, cell) key in scenes.keys
     launch_density_t(pos_s, veleval_s, density, rec_pd, rec_vi, nbr, mask, mask_stride, cell_start, cell_end, info,
-                     scenes, unit, exact != 0, grid_items, pxy, pz, pack, threads, st, scenes.keys);
+                     scenes, unit, exact != 0, grid_items, pxy, pz, pack, threads, st, scenes.keys, cell_pre);
 }
 
 }  // namespace sphk

@@ -255,12 +255,12 @@ void launch_density_batch(const float4* pos_s, const float4* veleval_s, float* d
                           float4* rec_vi, uint32_t* nbr, uint32_t* mask, size_t mask_stride,
                           const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                           const ManyScenes& scenes, bool unit, int exact, int grid_items, float4* pxy, float2* pz,
-                          bool pack, int threads, cudaStream_t st);
+                          bool pack, int threads, cudaStream_t st, const uint32_t* cell_pre = nullptr);
 void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4* rec_vi, const uint32_t* mask,
                         size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                         uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,
                         float4* keep_v, const ManyScenes& scenes, bool unit, float dt, int exact, int grid_items,
-                        int threads, cudaStream_t st);
+                        int threads, cudaStream_t st, const uint32_t* cell_pre = nullptr);
 // The batch's neighbour passes under the queue scheduler (sph_queue.cuh):
 // persistent blocks taking (scene, tile) items from Q.
 struct BatchQueue;

@@ -190,8 +190,8 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
         ++nrows;
     };
     if (cell_fast(P, c)) {
-        if (!Scenes::kBatch && G.pre != nullptr)
-            walk_rows_prefix(P, G.pre, c, add_row);
+        if (G.pre != nullptr)
+            walk_rows_prefix(P, G.pre + R.cell_base(i), c, add_row);
         else
             walk_rows_fast_batched(P, cs, ce, c, add_row);
     } else {
@@ -502,10 +502,10 @@ void launch_force_batch(const float4* pos_s, const float4* rec_pd, const float4*
                         size_t mask_stride, const uint32_t* nbr, const uint32_t* cell_start, const uint32_t* cell_end, const int* info,
                         uint32_t* idx, float4* pos_u, float4* vel_u, float4* veleval_u, float4* keep_f,
                         float4* keep_v, const ManyScenes& scenes, bool unit, float dt, int exact, int grid_items,
-                        int threads, cudaStream_t st) {
+                        int threads, cudaStream_t st, const uint32_t* cell_pre) {
     launch_force_t(pos_s, rec_pd, rec_vi, mask, mask_stride, nbr, cell_start, cell_end, info, nullptr, nullptr, idx,
                    nullptr, pos_u, vel_u, veleval_u, keep_f, keep_v, scenes, unit, dt, 1, exact, grid_items, threads,
-                   st);
+                   st, cell_pre);
 }
 
 }  // namespace sphk
