@@ -122,10 +122,14 @@ __device__ __forceinline__ void density_one(const int i, const DensityArgs& A, c
         }
     };
     const int3 c = grid_cell(pi.x, pi.y, pi.z, P.gs_min, P.gs_delta);
-    if (cell_fast(P, c))
-        walk_rows_fast(P, cs, ce, c, run);
-    else
+    if (cell_fast(P, c)) {
+        if (A.pre != nullptr)
+            walk_rows_prefix(P, A.pre + R.cell_base(i), c, run);
+        else
+            walk_rows_fast(P, cs, ce, c, run);
+    } else {
         walk_rows_slow(P, cs, ce, c, run);
+    }
     if ((p & 31u) != 0 && (p >> 5) < (uint32_t)kMaskWords) {
         if ((p >> 5) == (pself >> 5)) cur &= ~(1u << (pself & 31u));
         mrow[(size_t)(p >> 5) * mstride] = cur;
