@@ -51,14 +51,14 @@ FALLBACK_HBM_GBS = 6800.0
 # at the state named here; reported as roofline.traffic (with that state) for
 # the dominant kernel at that workload.
 TRAFFIC_STATE = "one launch at step 6 of the 2,097,152-particle dam break from the lattice at rest (ncu)"
-MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 211.976448e6 + 71.048704e6,
-                    "k_density": 94.954240e6 + 84.894976e6}
+MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 210.408960e6 + 70.907136e6,
+                    "k_density": 94.956032e6 + 85.051904e6}
 # The same captures' instruction-issue roofline, the bound these neighbour
 # passes meet first: warp instructions (smsp__inst_executed.sum) over the 4
 # an SM can issue per cycle in the launch's SM cycles (sm__cycles_elapsed.avg),
 # on 152 SMs.
-MEASURED_ISSUE = {"k_force(fused collision+leapfrog)": (247990396, 589674.09),
-                  "k_density": (197453326, 505033.82)}
+MEASURED_ISSUE = {"k_force(fused collision+leapfrog)": (237963388, 568786.58),
+                  "k_density": (193414542, 490255.32)}
 
 
 def parse():
