@@ -256,12 +256,20 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
         // its own count, taking its next set bit each time (the warp runs
         // while any lane has one left).
         const uint32_t cnt = M > 0 ? __ldg(nbr + i) - 1u : 0u;
-        for (uint32_t k = 0; k < cnt; ++k) {
+        auto visit = [&]() {
             const uint32_t p = next_bit();
-            if (!in_bounds(p, M, P.chk_err)) continue;  // a mask bit past the walk's candidates
+            if (!in_bounds(p, M, P.chk_err)) return;  // a mask bit past the walk's candidates
             const uint32_t j = index_of(p);
             if (in_bounds(j, P.chk_cap, P.chk_err))
                 force_pair<Exact>(a, pi, vi, di, Pi, __ldg(rec_pd + j), __ldg(rec_vi + j), P);
+        };
+        if constexpr (!Exact && !Scenes::kBatch) {
+            // two neighbours per loop trip (measured 1 % faster; the exact and
+            // batched variants would spill)
+#pragma unroll 2
+            for (uint32_t k = 0; k < cnt; ++k) visit();
+        } else {
+            for (uint32_t k = 0; k < cnt; ++k) visit();
         }
     } else {
         // Some lane has candidates past the bitmask (crowded cells): the
