@@ -209,7 +209,9 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     // Cursor: bit position p of the last neighbour taken, row r containing it.
     const uint32_t* mrow = mask + i;
     const uint32_t mbits = M < (uint32_t)kMaskBits ? M : (uint32_t)kMaskBits;
-    uint32_t w = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
+    // wb: walk position of the current word's bit 0; mnext: the word after it
+    uint32_t wb = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
+    const uint32_t* mnext = mrow + mstride;
     // the next mask word, in flight while this one's neighbours are processed
     uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     int r = 0;
@@ -242,11 +244,12 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     // the lane's next neighbour from the bitmask (one is left)
     auto next_bit = [&]() -> uint32_t {
         while (m == 0) {
-            ++w;
+            wb += 32u;
             m = m_next;
-            m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
+            mnext += mstride;
+            m_next = (wb + 32u < mbits) ? __ldg(mnext) : 0u;
         }
-        const uint32_t p = w * 32u + (uint32_t)(__ffs(m) - 1);
+        const uint32_t p = wb + (uint32_t)(__ffs(m) - 1);
         m &= m - 1u;
         return p;
     };
@@ -279,13 +282,14 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
             // next neighbour of this lane, as its walk-order position p
             bool have = false;
             uint32_t p = 0;
-            while (m == 0 && (w + 1) * 32u < mbits) {
-                ++w;
+            while (m == 0 && wb + 32u < mbits) {
+                wb += 32u;
                 m = m_next;
-                m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
+                mnext += mstride;
+                m_next = (wb + 32u < mbits) ? __ldg(mnext) : 0u;
             }
             if (m != 0) {
-                p = w * 32u + (uint32_t)(__ffs(m) - 1);
+                p = wb + (uint32_t)(__ffs(m) - 1);
                 m &= m - 1u;
                 have = true;
             } else {
