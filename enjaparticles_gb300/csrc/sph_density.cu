@@ -437,18 +437,17 @@ __device__ __forceinline__ void density_cellpair(const uint32_t a, const bool ha
                     ++k;
                 }
                 const uint32_t kin = (2u * ke <= re) ? ke : ke - 1u;
+                uint32_t bit = 1u << (2u * (k - ks));  // bit of pair k's first element in sa / sb
 #pragma unroll 2
-                for (; k < kin; ++k) {
+                for (; k < kin; ++k, bit <<= 2) {
                     const float4 xy = __ldg(pxy + k);
                     const float2 zz = __ldg(pz + k);
-                    const uint32_t bit = 1u << (2u * (k - ks));
                     cellpair_pair(La, xy, zz, true, true, rc2, h2, sa, bit);
                     cellpair_pair(Lb, xy, zz, true, true, rc2, h2, sb, bit);
                 }
                 if (k < ke) {  // the run's last pair (its element 2k+1 may be re)
                     const float4 xy = __ldg(pxy + k);
                     const float2 zz = __ldg(pz + k);
-                    const uint32_t bit = 1u << (2u * (k - ks));
                     const bool v1 = 2u * k + 1u < re;
                     cellpair_pair(La, xy, zz, true, v1, rc2, h2, sa, bit);
                     cellpair_pair(Lb, xy, zz, true, v1, rc2, h2, sb, bit);
