@@ -192,7 +192,9 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
     s_off[nrows][t] = M;
     const uint32_t* mrow = T.mask + i;
     const uint32_t mbits = M < (uint32_t)sphk::kMaskBits ? M : (uint32_t)sphk::kMaskBits;
-    uint32_t w = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
+    // wb: walk position of the current word's bit 0; mnext: the word after it
+    uint32_t wb = 0, m = (mbits > 0) ? __ldg(mrow) : 0u;
+    const uint32_t* mnext = mrow + mstride;
     // the next mask word, in flight while this one's neighbours are processed
     uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     uint32_t q = (uint32_t)sphk::kMaskBits;
@@ -202,13 +204,14 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
         // Every lane's candidates fit the bitmask: each lane runs through its
         // own set bits, with no vote per neighbour.
         for (;;) {
-            while (m == 0 && (w + 1) * 32u < mbits) {
-                ++w;
+            while (m == 0 && wb + 32u < mbits) {
+                wb += 32u;
                 m = m_next;
-                m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
+                mnext += mstride;
+                m_next = (wb + 32u < mbits) ? __ldg(mnext) : 0u;
             }
             if (m == 0) return;
-            const uint32_t p = w * 32u + (uint32_t)(__ffs(m) - 1);
+            const uint32_t p = wb + (uint32_t)(__ffs(m) - 1);
             m &= m - 1u;
             while (p >= next_off) {
                 ++r;
@@ -221,13 +224,14 @@ __device__ __forceinline__ void for_each_neighbour(const StepParams& P, const ui
     for (;;) {
         bool have = false;
         uint32_t p = 0;
-        while (m == 0 && (w + 1) * 32u < mbits) {
-            ++w;
+        while (m == 0 && wb + 32u < mbits) {
+            wb += 32u;
             m = m_next;
-            m_next = ((w + 1) * 32u < mbits) ? __ldg(mrow + (size_t)(w + 1) * mstride) : 0u;
+            mnext += mstride;
+            m_next = (wb + 32u < mbits) ? __ldg(mnext) : 0u;
         }
         if (m != 0) {
-            p = w * 32u + (uint32_t)(__ffs(m) - 1);
+            p = wb + (uint32_t)(__ffs(m) - 1);
             m &= m - 1u;
             have = true;
         } else {
