@@ -215,6 +215,7 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     // the next mask word, in flight while this one's neighbours are processed
     uint32_t m_next = (mbits > 32u) ? __ldg(mrow + mstride) : 0u;
     int r = 0;
+    const uint2* srow = &s_row[0][t];  // the cursor's row entry (one system)
     // One scene: row r's end and index offset in registers, reloaded when the
     // cursor changes row.  Batches read them from shared memory: with the
     // scene lookups the registers would spill (measured slower).
@@ -229,8 +230,8 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
     auto index_of = [&](uint32_t p) -> uint32_t {
         if constexpr (kRegCursor) {
             while (p >= next_off) {
-                ++r;
-                const uint2 e = s_row[r][t];
+                srow += T;  // the next row's entry of this thread's column
+                const uint2 e = *srow;
                 next_off = e.x;
                 delta = e.y;
             }
