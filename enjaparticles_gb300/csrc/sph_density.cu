@@ -307,20 +307,30 @@ struct CellPairLane {
     float2 px, py, pz;  // the particle's coordinates in both lanes
     float2 acc;         // poly6 sums of the even and the odd candidates
     uint32_t cnt;       // neighbours, itself included
-    uint32_t cur, fill, wo;  // mask word stream: `cur` holds `fill` bits of word `wo`
+    uint32_t cur;       // the mask word being filled (the item's stream position below)
     uint32_t self;      // its sorted index
 };
 
-__device__ __forceinline__ void cellpair_append(CellPairLane& L, uint32_t* __restrict__ mrow, size_t mstride,
-                                                uint32_t v, uint32_t len, bool store) {
-    L.cur |= v << L.fill;
-    if (L.fill + len >= 32u) {
-        if (store && L.wo < (uint32_t)kMaskWords) mrow[(size_t)L.wo * mstride] = L.cur;
-        ++L.wo;
-        L.cur = L.fill ? (v >> (32u - L.fill)) : 0u;
-        L.fill = L.fill + len - 32u;
+// The two particles' mask word streams advance together (both walk the same
+// candidates): `fill` bits of word `wo` are in each lane's `cur`.  Appends
+// len bits of each (va, vb) and stores the words that fill up.
+__device__ __forceinline__ void cellpair_append2(CellPairLane& La, CellPairLane& Lb, uint32_t& fill, uint32_t& wo,
+                                                 uint32_t* __restrict__ mrow_a, uint32_t* __restrict__ mrow_b,
+                                                 size_t mstride, uint32_t va, uint32_t vb, uint32_t len,
+                                                 bool store_b) {
+    La.cur |= va << fill;
+    Lb.cur |= vb << fill;
+    if (fill + len >= 32u) {
+        if (wo < (uint32_t)kMaskWords) {
+            mrow_a[(size_t)wo * mstride] = La.cur;
+            if (store_b) mrow_b[(size_t)wo * mstride] = Lb.cur;
+        }
+        ++wo;
+        La.cur = fill ? (va >> (32u - fill)) : 0u;
+        Lb.cur = fill ? (vb >> (32u - fill)) : 0u;
+        fill = fill + len - 32u;
     } else {
-        L.fill += len;
+        fill += len;
     }
 }
 
@@ -342,10 +352,11 @@ __device__ __forceinline__ void cellpair_pair(CellPairLane& L, const float4& xy,
     if (n1) seg |= bit << 1;
 }
 
-__device__ __forceinline__ void cellpair_finish(const CellPairLane& L, const float4& p, const DensityArgs& A,
-                                                const StepParams& P, uint32_t* __restrict__ mrow) {
+__device__ __forceinline__ void cellpair_finish(const CellPairLane& L, uint32_t fill, uint32_t wo, const float4& p,
+                                                const DensityArgs& A, const StepParams& P,
+                                                uint32_t* __restrict__ mrow) {
     const uint32_t i = L.self;
-    if (L.fill != 0 && L.wo < (uint32_t)kMaskWords) mrow[(size_t)L.wo * A.mstride] = L.cur;
+    if (fill != 0 && wo < (uint32_t)kMaskWords) mrow[(size_t)wo * A.mstride] = L.cur;
     const float rho = P.dens_coef * (L.acc.x + L.acc.y);
     A.density[i] = rho;
     A.rec_pd[i] = make_float4(p.x, p.y, p.z, rho);
@@ -384,8 +395,8 @@ __device__ __forceinline__ void density_cellpair(const uint32_t a, const bool ha
     Lb.px = make_float2(pb.x, pb.x), Lb.py = make_float2(pb.y, pb.y), Lb.pz = make_float2(pb.z, pb.z);
     La.acc = Lb.acc = make_float2(0.f, 0.f);
     La.cnt = Lb.cnt = 0;
-    La.cur = La.fill = La.wo = 0;
-    Lb.cur = Lb.fill = Lb.wo = 0;
+    La.cur = Lb.cur = 0;
+    uint32_t fill = 0, wo = 0;  // the mask word streams' position
     La.self = a;
     Lb.self = a + 1u;
     uint32_t* mrow_a = A.mask + a;
@@ -459,13 +470,12 @@ __device__ __forceinline__ void density_cellpair(const uint32_t a, const bool ha
                 Lb.cnt += (uint32_t)__popc(sb);
                 if (a - e0 < 32u) sa &= ~(1u << (a - e0));
                 if (a + 1u - e0 < 32u) sb &= ~(1u << (a + 1u - e0));
-                cellpair_append(La, mrow_a, ms, sa >> lo, hi - lo, true);
-                cellpair_append(Lb, mrow_b, ms, sb >> lo, hi - lo, has_b);
+                cellpair_append2(La, Lb, fill, wo, mrow_a, mrow_b, ms, sa >> lo, sb >> lo, hi - lo, has_b);
             }
         }
     }
-    cellpair_finish(La, pa, A, P, mrow_a);
-    if (has_b) cellpair_finish(Lb, pb, A, P, mrow_b);
+    cellpair_finish(La, fill, wo, pa, A, P, mrow_a);
+    if (has_b) cellpair_finish(Lb, fill, wo, pb, A, P, mrow_b);
 }
 
 // Particles per block of the cell-pair pass: about two per thread, less the
