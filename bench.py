@@ -51,14 +51,14 @@ FALLBACK_HBM_GBS = 6800.0
 # at the state named here; reported as roofline.traffic (with that state) for
 # the dominant kernel at that workload.
 TRAFFIC_STATE = "one launch at step 6 of the 2,097,152-particle dam break from the lattice at rest (ncu)"
-MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 210.408192e6 + 71.148544e6,
-                    "k_density": 94.925312e6 + 85.062912e6}
+MEASURED_TRAFFIC = {"k_force(fused collision+leapfrog)": 210.459904e6 + 71.135488e6,
+                    "k_density": 94.924544e6 + 87.544064e6}
 # The same captures' instruction-issue roofline, the bound these neighbour
 # passes meet first: warp instructions (smsp__inst_executed.sum) over the 4
 # an SM can issue per cycle in the launch's SM cycles (sm__cycles_elapsed.avg),
 # on 152 SMs.
-MEASURED_ISSUE = {"k_force(fused collision+leapfrog)": (222298374, 542126.91),
-                  "k_density": (188826510, 470011.05)}
+MEASURED_ISSUE = {"k_force(fused collision+leapfrog)": (222298374, 541018.80),
+                  "k_density": (183728966, 456453.39)}
 
 
 def parse():
