@@ -391,8 +391,8 @@ __device__ __forceinline__ void force_one(const int i, const bool in_range, cons
 //     no spills), 3 % faster;
 //   one system, exact arithmetic: 1152 (9 blocks of 128, 56 registers, no
 //     spills; unbounded it took 56 with 24 B of spills), 2 % faster;
-//   a batch, default arithmetic: 1152 (56 registers, 40 B of spills against
-//     64 and 4 B), the batch step 2 % faster;
+//   a batch, default arithmetic: 1152 (56 registers and a few bytes of
+//     spills against 64 unbounded), the batch step 2 % faster;
 //   a batch, exact arithmetic: unbounded.
 template <int T, bool Exact, class Scenes>
 constexpr int force_min_blocks() {
